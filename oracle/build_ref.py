@@ -1,0 +1,133 @@
+#!/usr/bin/env python3
+"""Build the reference's own CPU hot path into oracle/_ref/ (checker only).
+
+TEST INFRASTRUCTURE.  This recipe compiles rfdougherty/dSim's CPU code --
+dSim3/src/spinSystem.cpp (which #includes spinKernelCpu.cpp) and
+dSim2/src/spinSystem.cpp -- from the sources where they lie, into two
+harness executables that the golden-fixture generator
+(tests/golden/make_golden.py) runs to pin the C restatement in oracle/.
+
+Nothing here is shipped: outputs go to oracle/_ref/ (git-ignored).  The
+reference tree is read-only, so the few mechanical edits are applied to a
+scratch copy in oracle/_ref/src{2,3}/:
+
+  * display-only OpenGL code is removed: the GL header include is dropped,
+    every statement that is an OpenGL call is deleted, GLuint becomes an
+    unsigned int and glMapBufferARB(...) becomes a null pointer.  These lines
+    sit only on the useDisplay/useVbo branches, which the harnesses never take
+    (no OpenGL is loaded, stubbed or run);
+  * dSim3 SpinSystem::initFibers (dSim3/src/spinSystem.cpp:290-673) has no
+    return statement; "return true;" is added before its closing brace;
+  * dSim3 HITARRAYSIZE (spinSystem.cpp:1608, a stack buffer of 2000 hits for
+    compartment assignment) is raised to 65536;
+  * dSim2 spinSystem.cpp includes the unused radix-sort header
+    (radixsort.cuh, never called); that include is dropped.
+The host side of the C-ABI (allocateArray -> malloc, copy* -> memcpy) and the
+cutil timer macros are provided by oracle/refharness/.
+
+Usage: python3 oracle/build_ref.py [--reference /root/reference]
+"""
+import argparse
+import os
+import re
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+HARNESS = os.path.join(HERE, "refharness")
+
+DSIM3_FILES = ["spinSystem.cpp", "spinKernelCpu.cpp", "spinSystem.h", "spinSystem.cuh",
+               "RTree.h", "dSimDataTypes.h"]
+DSIM2_FILES = ["spinSystem.cpp", "spinKernelCpu.cpp", "spinSystem.h", "spinSystem.cuh",
+               "spinKernel.cuh", "options.h"]
+
+GL_STMT = re.compile(r"^\s*gl[A-Z]\w*\s*\(.*\)\s*;\s*(//.*)?$")
+GL_REGISTER = re.compile(r"^\s*(un)?registerGLBufferObject\s*\(.*\)\s*;\s*(//.*)?$")
+
+
+def strip_gl(text):
+    out = []
+    for line in text.split("\n"):
+        if re.match(r"^\s*#include\s*<GL/", line):
+            out.append("/* OpenGL include removed */")
+            continue
+        if GL_STMT.match(line) or GL_REGISTER.match(line):
+            out.append("/* OpenGL call removed */")
+            continue
+        line = line.replace("glMapBufferARB(GL_ARRAY_BUFFER, GL_WRITE_ONLY)", "0")
+        line = re.sub(r"\bGLuint\b", "unsigned int", line)
+        out.append(line)
+    return "\n".join(out)
+
+
+def patch_dsim3(src):
+    text = strip_gl(src)
+    lines = text.split("\n")
+    # initFibers ends at spinSystem.cpp:673; the loop closing braces precede it.
+    idx = None
+    for i, ln in enumerate(lines):
+        if ln.startswith("bool SpinSystem::initFibers("):
+            depth = 0
+            for j in range(i, len(lines)):
+                depth += lines[j].count("{") - lines[j].count("}")
+                if depth == 0 and "}" in lines[j]:
+                    idx = j
+                    break
+            break
+    assert idx is not None, "initFibers not found"
+    lines.insert(idx, "\treturn true; /* added: the function has no return */")
+    text = "\n".join(lines)
+    text, n = re.subn(r"#define HITARRAYSIZE 2000", "#define HITARRAYSIZE 65536", text)
+    assert n == 1
+    return text
+
+
+def patch_dsim2(src):
+    text = strip_gl(src)
+    text, n = re.subn(r'#include "radixsort.cuh"', "/* unused radix sort header removed */", text)
+    assert n == 1
+    return text
+
+
+def build(reference):
+    os.makedirs(OUT, exist_ok=True)
+    for tree, files, patch in (("dSim3", DSIM3_FILES, patch_dsim3),
+                               ("dSim2", DSIM2_FILES, patch_dsim2)):
+        dst = os.path.join(OUT, "src" + tree[-1])
+        os.makedirs(dst, exist_ok=True)
+        for f in files:
+            shutil.copyfile(os.path.join(reference, tree, "src", f), os.path.join(dst, f))
+        p = os.path.join(dst, "spinSystem.cpp")
+        with open(p) as fh:
+            text = fh.read()
+        with open(p, "w") as fh:
+            fh.write(patch(text))
+    cxx = os.environ.get("CXX", "g++")
+    common = [cxx, "-O2", "-ffp-contract=off", "-w", "-I", os.path.join(HARNESS, "include")]
+    jobs = [
+        common + ["-I", os.path.join(OUT, "src3"), os.path.join(OUT, "src3", "spinSystem.cpp"),
+                  os.path.join(HARNESS, "host_abi.cpp"), os.path.join(HARNESS, "harness3.cpp"),
+                  "-o", os.path.join(OUT, "harness3")],
+        common + ["-I", os.path.join(OUT, "src2"), "-DDSIM2_ABI",
+                  os.path.join(OUT, "src2", "spinSystem.cpp"),
+                  os.path.join(HARNESS, "host_abi.cpp"), os.path.join(HARNESS, "harness2.cpp"),
+                  "-o", os.path.join(OUT, "harness2")],
+    ]
+    procs = [subprocess.Popen(j) for j in jobs]
+    rc = [p.wait() for p in procs]
+    if any(rc):
+        raise SystemExit("reference harness build failed: %r" % rc)
+    return [os.path.join(OUT, "harness3"), os.path.join(OUT, "harness2")]
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    a = ap.parse_args()
+    if not os.path.isdir(a.reference):
+        print("reference tree not present; nothing to build")
+        sys.exit(0)
+    for p in build(a.reference):
+        print(p)
