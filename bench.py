@@ -1,0 +1,486 @@
+#!/usr/bin/env python3
+"""Throughput of the mesh hot path on one GB300 (spin-steps/s).
+
+Workload (the reference's mesh-scale plain configuration): 400 beaded axons
+tessellated with 32 vertices per ring and a ring every 0.5 um over 50 um
+(2.56M triangles), base radius LogNormal(median 1 um, sigma 0.4) clipped to
+[0.5, 3] um, 20 % sinusoidal beading with a 10 um period, reflecting glia
+membranes, in a 50 um cube (spaceScale 25, 50^3 grid of 1 um cells);
+1,048,576 spins; D = 2.0 um^2/ms; dt = 5 us; PGSE delta 15 ms, Delta 40 ms,
+b = 3000 s/mm^2 along one Fibonacci direction.  Synthetic substrate and
+spins, seeded.  One bench step = one launch advancing every spin 1000 time
+steps (1.05e9 spin-steps); K steps cover the 10,000-step unit of work.
+
+Reported: value = spin-steps/s from CUDA events around each launch on the
+engine's stream (L2 flushed between launches); e2e = the same through the
+reference-facing dSim3 C-ABI (libdsim3.so), with the reference host loop's
+copies (state to the device, integrateSystem, state back) from pinned host
+buffers inside the timed region; roofline of the step kernel; CPU baseline
+of the oracle port on a bounded sample.
+
+--impl reference times the reference's CPU algorithm (the oracle port of
+dSim3's cpuIntegrate, all host threads) on a bounded sample of the same
+workload.  Multi-GPU (--gpus N under torchrun): independent replicas, one
+per rank, no collective on the data path (weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+F = np.float32
+METRIC = "spin-steps/s"
+UNIT = "spin-steps/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------
+# workload
+# --------------------------------------------------------------------------
+class Workload:
+    def __init__(self, axons=400, spins=1 << 20, seed=1):
+        from dsim_gb300 import substrates as S
+        from dsim_gb300.engine import grad_scaled, phase_constant, std_devs
+        t0 = time.time()
+        self.axons = axons
+        self.tube = S.beaded_tubes(n_axons=axons, verts_per_ring=32, ring_spacing=0.5, length=50.0,
+                                   box=50.0, seed=seed, membranes="G", allow_overlap=True)
+        self.spaceScale = 25.0
+        self.numCubes = 50
+        self.N = spins
+        self.D, self.dt = 2.0, 0.005
+        self.delta, self.Delta = 15.0, 40.0
+        self.steps_per_launch = 1000
+        rng = np.random.default_rng(seed + 1)
+        pos = rng.uniform(-0.99, 0.99, (self.N, 3)).astype(F)
+        self.pos = pos.reshape(-1).copy()
+        self.comp, self.fiber = self._compartments(pos)
+        self.stdDevs = std_devs(self.D, self.D, 0.1 * self.D, self.spaceScale, self.dt)
+        self.T2 = np.array([80.0, 80.0, 7.5, 80.0], F)
+        self.pc = phase_constant(42576.0, self.dt)
+        # b = 3000 s/mm^2 = 3 ms/um^2, first direction of a 64-point Fibonacci sphere
+        b = 3.0
+        gmag = np.sqrt(b / (self.Delta - self.delta / 3.0)) / (2 * np.pi * 42576.0 * 1e-9 * self.delta)
+        k = 0.5
+        zc = 1 - 2 * k / 64
+        rr = np.sqrt(1 - zc * zc)
+        phi = np.pi * (3 - np.sqrt(5)) * k
+        self.G = gmag * np.array([rr * np.cos(phi), rr * np.sin(phi), zc])
+        self.g = grad_scaled(self.G, self.spaceScale)
+        nd, nD = int(round(self.delta / self.dt)), int(round(self.Delta / self.dt))
+        self.total_steps = 10000
+        w = np.zeros(self.total_steps, F)
+        w[:nd] = 1
+        w[nD:nD + nd] = -1
+        self.grad = (w[:, None] * self.g[None, :]).astype(F)
+        log("workload: %d triangles, %d vertices, overlap=%s, %.1fs" % (
+            len(self.tube["trgls"]), len(self.tube["vertices"]), self.tube["overlap"], time.time() - t0))
+
+    def _compartments(self, pos):
+        um = pos.astype(np.float64) * self.spaceScale
+        comp = np.zeros(len(pos), np.uint8)
+        fib = np.full(len(pos), 0xFFFF, np.uint16)
+        cx, cy = self.tube["centres"][:, 0], self.tube["centres"][:, 1]
+        r0 = self.tube["radii"]
+        # cells of 2 um to find candidate tubes
+        for i in range(len(r0)):
+            rz = r0[i] * (1 + 0.2 * np.sin(2 * np.pi * um[:, 2] / 10.0))
+            sel = (np.abs(um[:, 0] - cx[i]) < rz) & (np.abs(um[:, 1] - cy[i]) < rz)
+            sel &= np.hypot(um[:, 0] - cx[i], um[:, 1] - cy[i]) < rz * np.cos(np.pi / 32)
+            sel &= comp == 0
+            comp[sel] = 3
+            fib[sel] = i
+        return comp, fib
+
+
+def make_mesh(W):
+    from dsim_gb300.engine import Mesh
+    t0 = time.time()
+    m = Mesh.from_arrays(W.tube["vertices"], W.tube["trgls"], W.tube["membrane"], W.tube["fiber"],
+                         W.spaceScale, W.numCubes)
+    log("mesh on device: %d entries, max %d per cell, %.1f MB, built in %.2fs" % (
+        m.entries, m.max_per_cell, m.nbytes / 1e6, time.time() - t0))
+    return m
+
+
+def mesh_params_of(W):
+    from dsim_gb300.engine import mesh_params
+    return mesh_params(W.stdDevs, W.T2, 0.0, W.dt, W.pc)
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for k, n in enumerate(names):
+                if len(s) > 5 + k and s[5 + k] == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the oracle port of dSim3's cpuIntegrate on a bounded sample
+# --------------------------------------------------------------------------
+def cpu_sample(W, m, threads, budget_s=12.0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    start, tri = m.grid()
+    counts = np.diff(start.astype(np.int64)).astype(np.uint32)
+    maxtpc = int(counts.max())
+    dense = np.zeros((len(counts), maxtpc), np.uint32)
+    idx = np.repeat(np.arange(len(counts)), counts)
+    off = np.arange(len(tri)) - np.repeat(start[:-1].astype(np.int64), counts)
+    dense[idx, off] = tri
+    dense = dense.reshape(-1)
+    v, ti = m.arrays()
+    # helpers as the reference computes them (initFibers), from the device's vertices
+    H = _helpers(v, W.tube["trgls"].reshape(-1))
+    p = O.params3(W.stdDevs, W.T2, 0.0, W.dt, W.numCubes, maxtpc)
+    n = 4096 if threads == 1 else 4096 * threads
+    sel = np.random.default_rng(5).choice(W.N, n, replace=False)
+    pos = W.pos.reshape(-1, 3)[sel].reshape(-1).copy()
+    seed = np.random.default_rng(6).integers(1, 2 ** 32 - 1, 2 * n, dtype=np.uint64).astype(np.uint32)
+    mag = np.ones(n, F)
+    ph = np.zeros(n, F)
+    comp = W.comp[sel].copy()
+    fib = W.fiber[sel].copy()
+    L = O.lib()
+    # calibrate, then run ~budget seconds
+    t0 = time.perf_counter()
+    L.or3_integrate_mt(p, n, pos, seed, mag, ph, comp, fib, v, H, ti, counts, dense,
+                       float(W.g[0]), float(W.g[1]), float(W.g[2]), float(W.pc), 5, threads)
+    dt5 = time.perf_counter() - t0
+    iters = max(5, int(budget_s / max(dt5 / 5, 1e-6)))
+    t0 = time.perf_counter()
+    L.or3_integrate_mt(p, n, pos, seed, mag, ph, comp, fib, v, H, ti, counts, dense,
+                       float(W.g[0]), float(W.g[1]), float(W.g[2]), float(W.pc), iters, threads)
+    el = time.perf_counter() - t0
+    rate = n * iters / el
+    return rate, "%d spins x %d steps of the workload (mesh, grid and draws as on the GPU; %.1f s)" % (
+        n, iters, el)
+
+
+def _helpers(v, trgls):
+    """Triangle helpers in float32 with the reference's expression order
+    (dSim3/src/spinSystem.cpp:612-648)."""
+    V = v.reshape(-1, 3)
+    T = trgls.reshape(-1, 3)
+    p1, p2, p3 = V[T[:, 0]], V[T[:, 1]], V[T[:, 2]]
+    x1, y1, z1 = p1[:, 0], p1[:, 1], p1[:, 2]
+    x2, y2, z2 = p2[:, 0], p2[:, 1], p2[:, 2]
+    x3, y3, z3 = p3[:, 0], p3[:, 1], p3[:, 2]
+    nx = (y2 - y1) * (z3 - z1) - (z2 - z1) * (y3 - y1)
+    ny = (z2 - z1) * (x3 - x1) - (x2 - x1) * (z3 - z1)
+    nz = (x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1)
+    ln = np.sqrt(nx * nx + ny * ny + nz * nz)
+    H = np.stack([nx / ln, ny / ln, nz / ln, x3 - x1, y3 - y1, z3 - z1, x2 - x1, y2 - y1, z2 - z1,
+                  (x3 - x1) * (x2 - x1) + (y3 - y1) * (y2 - y1) + (z3 - z1) * (z2 - z1),
+                  (x3 - x1) * (x3 - x1) + (y3 - y1) * (y3 - y1) + (z3 - z1) * (z3 - z1),
+                  (x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1) + (z2 - z1) * (z2 - z1)], -1)
+    return np.ascontiguousarray(H.astype(F).reshape(-1))
+
+
+# --------------------------------------------------------------------------
+# e2e through the reference-facing dSim3 C-ABI
+# --------------------------------------------------------------------------
+def e2e_abi3(W, m, steps, warmup, pinned):
+    import ctypes as C
+    from dsim_gb300 import _lib
+    L = _lib.abi3()
+    start, tri = m.grid()
+    counts = np.diff(start.astype(np.int64)).astype(np.uint32)
+    maxtpc = int(counts.max())
+    dense = np.zeros((len(counts), maxtpc), np.uint32)
+    idx = np.repeat(np.arange(len(counts)), counts)
+    off = np.arange(len(tri)) - np.repeat(start[:-1].astype(np.int64), counts)
+    dense[idx, off] = tri
+    v, ti = m.arrays()
+    H = _helpers(v, W.tube["trgls"].reshape(-1))
+
+    allocs = []
+
+    def dev(arr):
+        p = C.c_void_p()
+        L.allocateArray(C.byref(p), arr.nbytes)
+        L.copyArrayToDevice(p, arr.ctypes.data, 0, arr.nbytes)
+        allocs.append(p)
+        return p
+
+    dV, dH, dTI = dev(v), dev(H), dev(ti)
+    L.bindVertices(dV, len(v)); L.bindTriangleHelpers(dH, len(H)); L.bindTriInfo(dTI, len(ti))
+    dTic, dCc = dev(dense.reshape(-1)), dev(counts)
+    for name, val, ty in (("k_numCubes", W.numCubes, np.uint32), ("k_totalNumCubes", W.numCubes ** 3, np.uint32),
+                          ("k_maxTrianglesPerCube", maxtpc, np.uint32),
+                          ("k_cubeLength", F(2.0) / F(W.numCubes), F), ("k_reflectionType", 1, np.uint32),
+                          ("k_permeability", 0.0, F), ("k_deltaTime", W.dt, F)):
+        a = np.array([val], ty)
+        L.copyConstantToDevice(name.encode(), a.ctypes.data, 0, 4)
+    for name, tab in (("k_T2Values", W.T2), ("k_stdDevs", W.stdDevs)):
+        a = np.ascontiguousarray(tab, F)
+        L.copyConstantToDevice(name.encode(), a.ctypes.data, 0, 16)
+    N = W.N
+    spins = np.zeros(N, np.dtype([("mag", "<f4"), ("phase", "<f4"), ("comp", "u1"), ("pad", "u1"),
+                                  ("fiber", "<u2")]))
+    spins["mag"] = 1.0
+    spins["comp"], spins["fiber"] = W.comp, W.fiber
+    seeds = np.random.default_rng(9).integers(1, 2 ** 32 - 1, 2 * N, dtype=np.uint64).astype(np.uint32)
+    hpos, hseed, hspin = pinned(W.pos.nbytes), pinned(seeds.nbytes), pinned(spins.nbytes)
+    hpos[:] = W.pos.view(np.uint8)
+    hseed[:] = seeds.view(np.uint8)
+    hspin[:] = spins.view(np.uint8)
+    dPos, dSeed, dSpin = dev(W.pos), dev(seeds), dev(spins)
+    g = _lib.Float3(*[float(x) for x in W.g])
+    it = W.steps_per_launch
+
+    def one():
+        # the reference host loop per update: setArray/setSpinArray, integrateSystem, getArray/getSpinArray
+        L.copyArrayToDevice(dPos, hpos.ctypes.data, 0, hpos.nbytes)
+        L.copyArrayToDevice(dSeed, hseed.ctypes.data, 0, hseed.nbytes)
+        L.copyArrayToDevice(dSpin, hspin.ctypes.data, 0, hspin.nbytes)
+        L.integrateSystem(dPos, dSeed, dSpin, float(W.dt), 0.0, N, g, float(W.pc), it, dTic, dCc)
+        L.copyArrayFromDevice(hpos.ctypes.data, dPos, 0, hpos.nbytes)
+        L.copyArrayFromDevice(hspin.ctypes.data, dSpin, 0, hspin.nbytes)
+
+    for _ in range(warmup):
+        one()
+    L.threadSync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        one()
+    L.threadSync()
+    el = time.perf_counter() - t0
+    st = L.dsim3_last_status()
+    if st != 0:
+        raise RuntimeError("dSim3 ABI: %s" % L.dsim3_last_error())
+    for p in allocs:
+        L.freeArray(p)
+    return {"value": steps * it * N / el, "unit": UNIT, "h2d_bytes_per_step": int(hpos.nbytes + hseed.nbytes + hspin.nbytes),
+            "d2h_bytes_per_step": int(hpos.nbytes + hspin.nbytes), "ms_per_step": 1e3 * el / steps,
+            "path": "libdsim3.so integrateSystem, pinned host buffers"}
+
+
+def pinned_factory():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            def pinned(nbytes):
+                return torch.empty(nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+            return pinned, True
+    except Exception:
+        pass
+    return (lambda nbytes: np.empty(nbytes, np.uint8)), False
+
+
+# --------------------------------------------------------------------------
+def run_ours(args, rank, world):
+    from dsim_gb300.engine import DeviceInfo, Spins, mesh_run
+    dev = DeviceInfo()
+    W = Workload(axons=args.axons, spins=args.spins, seed=1 + rank)
+    m = make_mesh(W)
+    p = mesh_params_of(W)
+    s = Spins(W.N)
+    it = W.steps_per_launch
+
+    def reset():
+        s.set(W.pos, np.ones(W.N, F), np.zeros(W.N, F), W.comp, W.fiber)
+
+    # T-bar and per-step statistics on an untimed launch with counters on
+    reset()
+    mesh_run(m, s, p, grad_per_step=W.grad[:it], iterations=it, seed=11, step0=0, count=True, scanned=True)
+    scanned = s.scanned(reset=True).astype(np.float64)
+    cnt = s.counts(reset=True)
+    Tbar = scanned.sum() / (W.N * it)
+    refl_per_step = cnt[:, 0].sum() / (W.N * it)
+    if s.status() != 0:
+        raise RuntimeError("kernel status flags set")
+    # warm-up
+    reset()
+    for k in range(args.warmup):
+        mesh_run(m, s, p, grad_per_step=W.grad[(k * it) % W.total_steps:][:it], iterations=it, seed=3,
+                 step0=k * it)
+    s.sync()
+    reset()
+    times = []
+    barrier(world)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        for k in range(args.steps):
+            s.flush_l2(512 << 20)
+            s.timer_start()
+            lo = (k * it) % W.total_steps
+            mesh_run(m, s, p, grad_per_step=W.grad[lo:lo + it], iterations=it, seed=1, step0=k * it)
+            times.append(s.timer_stop())
+        s.sync()
+    barrier(world)
+    assert s.status() == 0
+    total_ms = sum(times)
+    total_ms = max_over_ranks(total_ms, world)
+    spin_steps = args.steps * it * W.N * world
+    value = spin_steps / (total_ms / 1e3)
+    # signal after the unit of work (sanity, reported)
+    sums = s.signal()
+    from dsim_gb300.engine import signal_from_sums
+    S = signal_from_sums(sums)[0]
+
+    hbm, kind = peaks()
+    S_bytes = 12 + 4 + 4
+    B_step = 2 * S_bytes + 40 * Tbar
+    mean_launch_ms = (sum(times) / len(times))
+    achieved = B_step * (it * W.N) / (mean_launch_ms / 1e3) / 1e9
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "mesh: %d beaded tubes, %d triangles, 50 um cube, 1 um cells, %d spins, "
+                               "dt 5 us, PGSE delta 15 Delta 40 ms, b 3000 s/mm2, 1000 steps per launch"
+                               % (W.axons, len(W.tube["trgls"]), W.N),
+                   "spins": W.N, "triangles": int(len(W.tube["trgls"])), "steps_per_launch": it,
+                   "form": "plain", "rng": "philox4x32-10", "l2": "flushed between launches (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind,
+                     "bytes_per_spin_step": B_step, "T_bar": Tbar,
+                     "note": "B_step = 2*S + 40*T_bar, S = 20 B, T_bar = grid entries scanned per step (kernel counter)"},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "device": dev.name,
+        "signal_after_run": S,
+        "reflections_per_step": refl_per_step,
+    }
+    if rank == 0 and not args.no_e2e:
+        pinned, is_pinned = pinned_factory()
+        e = e2e_abi3(W, m, max(2, min(args.steps, 5)), 1, pinned)
+        e["pinned"] = is_pinned
+        res["e2e"] = e
+    if rank == 0 and not args.no_cpu:
+        threads = 1
+        rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
+        res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": sample}
+    return res
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from dsim_gb300.engine import DeviceInfo  # noqa: F401  (GPU not used by this arm)
+    W = Workload(axons=args.axons, spins=args.spins, seed=1)
+    m = make_mesh(W)
+    threads = os.cpu_count() or 1
+    rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
+    return {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "mesh: %d beaded tubes, %d triangles, %d spins (sampled)" % (
+                W.axons, len(W.tube["trgls"]), W.N)},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# --------------------------------------------------------------------------
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--axons", type=int, default=400)
+    ap.add_argument("--spins", type=int, default=1 << 20)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        import ctypes
+        # one GPU per rank
+        os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")
+    res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

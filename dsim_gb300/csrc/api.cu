@@ -1,0 +1,705 @@
+// api.cu -- host side of the native engine: substrate loading and grid build,
+// device-resident spin state, launches, and the dsim_* C-ABI (include/dsim.h).
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#pragma GCC visibility push(default)
+#include "../../include/dsim.h"
+#pragma GCC visibility pop
+#include "common.cuh"
+#include "engine.h"
+#include "host_formats.h"
+
+namespace dsim {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = std::string("dsim error ") + std::to_string(code) + ": " + buf;
+}
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    set_last_error(kErrCuda, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+const char* last_error_message() { return g_last_error.c_str(); }
+
+template <typename T>
+static int dev_alloc(T** p, size_t count, uint64_t* bytes = nullptr) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        set_last_error(kErrNoMem, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+        cudaGetLastError();
+        return kErrNoMem;
+    }
+    if (bytes) *bytes += count * sizeof(T);
+    return kOk;
+}
+
+}  // namespace dsim
+
+using namespace dsim;
+
+struct dsim_mesh {
+    uint32_t nV = 0, nT = 0, nFibers = 0, n = 50;
+    float L = 0.04f;
+    uint64_t entries = 0, maxPerCell = 0, nonempty = 0, bytes = 0;
+    float* V = nullptr;
+    uint32_t* trgls = nullptr;
+    uint32_t* membrane = nullptr;
+    uint32_t* fiber = nullptr;
+    TriPlane* plane = nullptr;
+    TriBary* bary = nullptr;
+    uint32_t* cell_start = nullptr;
+    uint32_t* cell_tri = nullptr;
+    MeshDev dev() const {
+        MeshDev g;
+        g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
+        g.n = n; g.L = L;
+        return g;
+    }
+};
+
+struct dsim_cyl {
+    CylHost host;
+    float4* fibers = nullptr;
+    uint32_t* cc = nullptr;
+    uint32_t* cubes = nullptr;
+    uint64_t bytes = 0;
+    CylDev dev() const {
+        CylDev g;
+        g.fibers = fibers; g.cube_count = cc; g.cubes = cubes;
+        g.n = host.numCubes; g.maxFPC = host.maxFPC; g.L = host.cubeLength;
+        g.nF = host.nF;
+        return g;
+    }
+};
+
+struct dsim_spins {
+    uint32_t N = 0;
+    cudaStream_t st = nullptr;
+    float *x = nullptr, *y = nullptr, *z = nullptr, *mag = nullptr, *phase = nullptr;
+    uint32_t* meta = nullptr;
+    float4* cpos = nullptr;     // cylinder layout (lazy)
+    uint32_t* cseed = nullptr;  // cylinder layout (lazy)
+    uint32_t* counts = nullptr;
+    uint32_t* tested = nullptr;  // per-spin scanned grid entries (lazy)
+    uint32_t* status = nullptr;
+    float4* draws = nullptr;    // replay buffer (lazy, grows)
+    size_t drawsCap = 0;
+    float4* grad = nullptr;     // per-step gradient table (lazy, grows)
+    size_t gradCap = 0;
+    double* partials = nullptr; // signal scratch
+    double* sig = nullptr;      // 15 doubles
+    void* flush = nullptr;
+    size_t flushCap = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint64_t bytes = 0;
+    SpinsDev dev() const {
+        SpinsDev S;
+        S.x = x; S.y = y; S.z = z; S.mag = mag; S.phase = phase; S.meta = meta; S.seed = nullptr;
+        S.N = N;
+        return S;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// mesh construction
+// ---------------------------------------------------------------------------
+static void mesh_release(dsim_mesh* m) {
+    if (!m) return;
+    cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
+    cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
+    delete m;
+}
+
+// Upload normalised vertices and triangles, compute records, build the grid.
+static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vector<uint32_t>& trgls,
+                      const std::vector<uint32_t>& membrane, const std::vector<uint32_t>& fiber) {
+    int rc;
+    m->nV = (uint32_t)(Vn.size() / 3);
+    m->nT = (uint32_t)(trgls.size() / 3);
+    for (uint32_t t = 0; t < m->nT; t++)
+        for (int k = 0; k < 3; k++)
+            if (trgls[3 * t + k] >= m->nV) {
+                set_last_error(kErrFormat, "triangle %u references vertex %u of %u", t, trgls[3 * t + k], m->nV);
+                return kErrFormat;
+            }
+    if ((rc = dev_alloc(&m->V, Vn.size(), &m->bytes))) return rc;
+    if ((rc = dev_alloc(&m->trgls, trgls.size(), &m->bytes))) return rc;
+    if ((rc = dev_alloc(&m->membrane, m->nT, &m->bytes))) return rc;
+    if ((rc = dev_alloc(&m->fiber, m->nT, &m->bytes))) return rc;
+    if ((rc = dev_alloc(&m->plane, m->nT, &m->bytes))) return rc;
+    if ((rc = dev_alloc(&m->bary, m->nT, &m->bytes))) return rc;
+    cudaStream_t st = 0;
+    DSIM_CUDA_TRY(cudaMemcpyAsync(m->V, Vn.data(), Vn.size() * 4, cudaMemcpyHostToDevice, st));
+    DSIM_CUDA_TRY(cudaMemcpyAsync(m->trgls, trgls.data(), trgls.size() * 4, cudaMemcpyHostToDevice, st));
+    if (m->nT) {
+        DSIM_CUDA_TRY(cudaMemcpyAsync(m->membrane, membrane.data(), m->nT * 4, cudaMemcpyHostToDevice, st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(m->fiber, fiber.data(), m->nT * 4, cudaMemcpyHostToDevice, st));
+    }
+    if ((rc = launch_records_from_mesh(m->nT, m->V, m->trgls, m->membrane, m->fiber, m->plane, m->bary, st)))
+        return rc;
+    // grid: count -> scan -> fill -> sort (populateCubes membership)
+    uint32_t ncells = m->n * m->n * m->n;
+    uint32_t* counter = nullptr;
+    uint32_t* scratch = nullptr;
+    if ((rc = dev_alloc(&counter, ncells))) return rc;
+    if ((rc = dev_alloc(&scratch, scan_scratch_words(ncells)))) { cudaFree(counter); return rc; }
+    if ((rc = dev_alloc(&m->cell_start, (size_t)ncells + 1, &m->bytes))) { cudaFree(counter); cudaFree(scratch); return rc; }
+    rc = kOk;
+    do {
+        if (cudaMemsetAsync(counter, 0, ncells * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
+        if ((rc = launch_tri_cells(false, m->nT, m->V, m->trgls, m->n, m->L, counter, nullptr, nullptr, st))) break;
+        if ((rc = launch_scan_exclusive(counter, m->cell_start, ncells, scratch, st))) break;
+        uint32_t total = 0;
+        if (cudaMemcpyAsync(&total, m->cell_start + ncells, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
+        m->entries = total;
+        if ((rc = dev_alloc(&m->cell_tri, total, &m->bytes))) break;
+        if (cudaMemsetAsync(counter, 0, ncells * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
+        if ((rc = launch_tri_cells(true, m->nT, m->V, m->trgls, m->n, m->L, counter, m->cell_start, m->cell_tri, st))) break;
+        if ((rc = launch_sort_cells(ncells, m->cell_start, m->cell_tri, st))) break;
+        std::vector<uint32_t> cs(ncells + 1);
+        if (cudaMemcpyAsync(cs.data(), m->cell_start, cs.size() * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
+        uint64_t mx = 0, ne = 0;
+        for (uint32_t c = 0; c < ncells; c++) {
+            uint32_t k = cs[c + 1] - cs[c];
+            if (k > mx) mx = k;
+            if (k) ne++;
+        }
+        m->maxPerCell = mx;
+        m->nonempty = ne;
+    } while (0);
+    if (rc == kErrCuda) set_last_error(kErrCuda, "grid build: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(counter);
+    cudaFree(scratch);
+    return rc;
+}
+
+extern "C" {
+
+const char* dsim_last_error(void) { return last_error_message(); }
+int dsim_version(void) { return 1; }
+
+int dsim_device_info(char* name, int len, int* smCount, size_t* totalMem) {
+    int dev = 0;
+    DSIM_CUDA_TRY(cudaGetDevice(&dev));
+    cudaDeviceProp p;
+    DSIM_CUDA_TRY(cudaGetDeviceProperties(&p, dev));
+    if (name && len > 0) { strncpy(name, p.name, len - 1); name[len - 1] = 0; }
+    if (smCount) *smCount = p.multiProcessorCount;
+    if (totalMem) *totalMem = p.totalGlobalMem;
+    return kOk;
+}
+
+int dsim_mesh_load(const char* path, float spaceScale, uint32_t numCubes, dsim_mesh** out) {
+    if (!path || !out || !(spaceScale > 0) || numCubes == 0 || numCubes > 1024) {
+        set_last_error(kErrInvalid, "dsim_mesh_load: bad argument");
+        return kErrInvalid;
+    }
+    *out = nullptr;
+    MeshHost h;
+    int rc = parse_mesh_file(path, spaceScale, h);
+    if (rc) return rc;
+    dsim_mesh* m = new dsim_mesh();
+    m->n = numCubes;
+    m->L = 2.0f / (float)numCubes;
+    m->nFibers = h.nFibers;
+    rc = mesh_build(m, h.vertices, h.trgls, h.membrane, h.fiber);
+    if (rc) { mesh_release(m); return rc; }
+    *out = m;
+    return kOk;
+}
+
+int dsim_mesh_create(const float* vertices_um, uint32_t nVertices, const uint32_t* trgls,
+                     const uint32_t* membrane, const uint32_t* fiber, uint32_t nTriangles,
+                     float spaceScale, uint32_t numCubes, dsim_mesh** out) {
+    if (!out || (!vertices_um && nVertices) || (!trgls && nTriangles) || !(spaceScale > 0) ||
+        numCubes == 0 || numCubes > 1024) {
+        set_last_error(kErrInvalid, "dsim_mesh_create: bad argument");
+        return kErrInvalid;
+    }
+    *out = nullptr;
+    std::vector<float> Vn((size_t)nVertices * 3);
+    for (size_t k = 0; k < Vn.size(); k++) Vn[k] = vertices_um[k] / spaceScale;
+    std::vector<uint32_t> T(trgls, trgls + (size_t)nTriangles * 3);
+    std::vector<uint32_t> mem(nTriangles, 0u), fib(nTriangles, 0u);
+    uint32_t nf = 0;
+    for (uint32_t t = 0; t < nTriangles; t++) {
+        mem[t] = membrane ? membrane[t] : 2u;
+        fib[t] = fiber ? fiber[t] : 0u;
+        if (mem[t] > 2u) { set_last_error(kErrInvalid, "membrane type %u > 2", mem[t]); return kErrInvalid; }
+        if (fib[t] + 1 > nf) nf = fib[t] + 1;
+    }
+    dsim_mesh* m = new dsim_mesh();
+    m->n = numCubes;
+    m->L = 2.0f / (float)numCubes;
+    m->nFibers = nf;
+    int rc = mesh_build(m, Vn, T, mem, fib);
+    if (rc) { mesh_release(m); return rc; }
+    *out = m;
+    return kOk;
+}
+
+int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]) {
+    if (!m || !info) return kErrInvalid;
+    info[0] = m->nV; info[1] = m->nT; info[2] = m->nFibers; info[3] = m->n;
+    info[4] = m->entries; info[5] = m->maxPerCell; info[6] = m->bytes; info[7] = m->nonempty;
+    return kOk;
+}
+
+int dsim_mesh_grid(const dsim_mesh* m, uint32_t* cellStart, uint32_t* cellTri) {
+    if (!m) return kErrInvalid;
+    size_t nc = (size_t)m->n * m->n * m->n;
+    if (cellStart) DSIM_CUDA_TRY(cudaMemcpy(cellStart, m->cell_start, (nc + 1) * 4, cudaMemcpyDeviceToHost));
+    if (cellTri && m->entries) DSIM_CUDA_TRY(cudaMemcpy(cellTri, m->cell_tri, m->entries * 4, cudaMemcpyDeviceToHost));
+    return kOk;
+}
+
+int dsim_mesh_arrays(const dsim_mesh* m, float* vertices, uint32_t* triInfo) {
+    if (!m) return kErrInvalid;
+    if (vertices && m->nV) DSIM_CUDA_TRY(cudaMemcpy(vertices, m->V, (size_t)m->nV * 12, cudaMemcpyDeviceToHost));
+    if (triInfo && m->nT) {
+        std::vector<uint32_t> T((size_t)m->nT * 3), mem(m->nT), fib(m->nT);
+        DSIM_CUDA_TRY(cudaMemcpy(T.data(), m->trgls, T.size() * 4, cudaMemcpyDeviceToHost));
+        DSIM_CUDA_TRY(cudaMemcpy(mem.data(), m->membrane, m->nT * 4, cudaMemcpyDeviceToHost));
+        DSIM_CUDA_TRY(cudaMemcpy(fib.data(), m->fiber, m->nT * 4, cudaMemcpyDeviceToHost));
+        for (uint32_t t = 0; t < m->nT; t++) {
+            triInfo[3 * t] = fib[t]; triInfo[3 * t + 1] = mem[t]; triInfo[3 * t + 2] = T[3 * t];
+        }
+    }
+    return kOk;
+}
+
+void dsim_mesh_free(dsim_mesh* m) { mesh_release(m); }
+
+// ---------------------------------------------------------------------------
+// cylinders
+// ---------------------------------------------------------------------------
+static void cyl_release(dsim_cyl* c) {
+    if (!c) return;
+    cudaFree(c->fibers); cudaFree(c->cc); cudaFree(c->cubes);
+    delete c;
+}
+
+static int cyl_upload(dsim_cyl* c) {
+    int rc;
+    CylHost& h = c->host;
+    if ((rc = dev_alloc(&c->fibers, h.nF, &c->bytes))) return rc;
+    if ((rc = dev_alloc(&c->cc, h.cubeCounter.size(), &c->bytes))) return rc;
+    if ((rc = dev_alloc(&c->cubes, h.cubes.size(), &c->bytes))) return rc;
+    if (h.nF) DSIM_CUDA_TRY(cudaMemcpy(c->fibers, h.fiberPos.data(), (size_t)h.nF * 16, cudaMemcpyHostToDevice));
+    DSIM_CUDA_TRY(cudaMemcpy(c->cc, h.cubeCounter.data(), h.cubeCounter.size() * 4, cudaMemcpyHostToDevice));
+    if (!h.cubes.empty())
+        DSIM_CUDA_TRY(cudaMemcpy(c->cubes, h.cubes.data(), h.cubes.size() * 4, cudaMemcpyHostToDevice));
+    return kOk;
+}
+
+int dsim_cyl_load(const char* path, float spaceScale, dsim_cyl** out) {
+    if (!path || !out || !(spaceScale > 0)) { set_last_error(kErrInvalid, "dsim_cyl_load: bad argument"); return kErrInvalid; }
+    *out = nullptr;
+    dsim_cyl* c = new dsim_cyl();
+    int rc = parse_cyl_file(path, spaceScale, c->host);
+    if (!rc) rc = build_cyl_grid(c->host);
+    if (!rc) rc = cyl_upload(c);
+    if (rc) { cyl_release(c); return rc; }
+    *out = c;
+    return kOk;
+}
+
+int dsim_cyl_create(const float* fiberPos4, uint32_t nFibers, float maxRadius, dsim_cyl** out) {
+    if (!out || (!fiberPos4 && nFibers) || !(maxRadius > 0)) { set_last_error(kErrInvalid, "dsim_cyl_create: bad argument"); return kErrInvalid; }
+    *out = nullptr;
+    dsim_cyl* c = new dsim_cyl();
+    c->host.nF = nFibers;
+    c->host.fiberPos.assign(fiberPos4, fiberPos4 + (size_t)nFibers * 4);
+    c->host.maxR = maxRadius;
+    int rc = build_cyl_grid(c->host);
+    if (!rc) rc = cyl_upload(c);
+    if (rc) { cyl_release(c); return rc; }
+    *out = c;
+    return kOk;
+}
+
+int dsim_cyl_info(const dsim_cyl* c, uint32_t geom[3], float* cubeLength, uint32_t* cubeCounter,
+                  uint32_t* cubes, float* fiberPos4) {
+    if (!c) return kErrInvalid;
+    const CylHost& h = c->host;
+    if (geom) { geom[0] = h.numCubes; geom[1] = h.maxFPC; geom[2] = h.nF; }
+    if (cubeLength) *cubeLength = h.cubeLength;
+    if (cubeCounter) memcpy(cubeCounter, h.cubeCounter.data(), h.cubeCounter.size() * 4);
+    if (cubes && !h.cubes.empty()) memcpy(cubes, h.cubes.data(), h.cubes.size() * 4);
+    if (fiberPos4 && h.nF) memcpy(fiberPos4, h.fiberPos.data(), (size_t)h.nF * 16);
+    return kOk;
+}
+
+void dsim_cyl_free(dsim_cyl* c) { cyl_release(c); }
+
+// ---------------------------------------------------------------------------
+// spins
+// ---------------------------------------------------------------------------
+static void spins_release(dsim_spins* s) {
+    if (!s) return;
+    if (s->st) cudaStreamSynchronize(s->st);
+    cudaFree(s->x); cudaFree(s->y); cudaFree(s->z); cudaFree(s->mag); cudaFree(s->phase);
+    cudaFree(s->meta); cudaFree(s->cpos); cudaFree(s->cseed); cudaFree(s->counts);
+    cudaFree(s->status); cudaFree(s->tested); cudaFree(s->draws); cudaFree(s->grad); cudaFree(s->partials);
+    cudaFree(s->sig); cudaFree(s->flush);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+}
+
+int dsim_spins_create(uint32_t N, dsim_spins** out) {
+    if (!out) return kErrInvalid;
+    *out = nullptr;
+    dsim_spins* s = new dsim_spins();
+    s->N = N;
+    int rc = kOk;
+    do {
+        if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) { rc = kErrCuda; break; }
+        if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess) { rc = kErrCuda; break; }
+        if ((rc = dev_alloc(&s->x, N, &s->bytes)) || (rc = dev_alloc(&s->y, N, &s->bytes)) ||
+            (rc = dev_alloc(&s->z, N, &s->bytes)) || (rc = dev_alloc(&s->mag, N, &s->bytes)) ||
+            (rc = dev_alloc(&s->phase, N, &s->bytes)) || (rc = dev_alloc(&s->meta, N, &s->bytes)) ||
+            (rc = dev_alloc(&s->counts, (size_t)2 * N, &s->bytes)) || (rc = dev_alloc(&s->status, 1, &s->bytes)) ||
+            (rc = dev_alloc(&s->partials, reduce_scratch_doubles(N), &s->bytes)) ||
+            (rc = dev_alloc(&s->sig, 15, &s->bytes)))
+            break;
+        if (cudaMemsetAsync(s->counts, 0, (size_t)8 * N + 4, s->st) != cudaSuccess ||
+            cudaMemsetAsync(s->status, 0, 4, s->st) != cudaSuccess) { rc = kErrCuda; break; }
+    } while (0);
+    if (rc == kErrCuda) set_last_error(kErrCuda, "dsim_spins_create: %s", cudaGetErrorString(cudaGetLastError()));
+    if (rc) { spins_release(s); return rc; }
+    *out = s;
+    return kOk;
+}
+
+uint32_t dsim_spins_count(const dsim_spins* s) { return s ? s->N : 0; }
+uint64_t dsim_spins_bytes(const dsim_spins* s) { return s ? s->bytes : 0; }
+
+int dsim_spins_set(dsim_spins* s, const float* pos3, const float* mag, const float* phase,
+                   const uint8_t* comp, const uint16_t* fiber) {
+    if (!s) return kErrInvalid;
+    uint32_t N = s->N;
+    std::vector<float> a(N), b(N), c(N);
+    if (pos3) {
+        for (uint32_t i = 0; i < N; i++) { a[i] = pos3[3 * i]; b[i] = pos3[3 * i + 1]; c[i] = pos3[3 * i + 2]; }
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->x, a.data(), N * 4, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->y, b.data(), N * 4, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->z, c.data(), N * 4, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    }
+    if (mag) DSIM_CUDA_TRY(cudaMemcpyAsync(s->mag, mag, N * 4, cudaMemcpyHostToDevice, s->st));
+    if (phase) DSIM_CUDA_TRY(cudaMemcpyAsync(s->phase, phase, N * 4, cudaMemcpyHostToDevice, s->st));
+    if (comp || fiber) {
+        std::vector<uint32_t> m(N);
+        for (uint32_t i = 0; i < N; i++)
+            m[i] = (comp ? (uint32_t)comp[i] : 0u) | ((fiber ? (uint32_t)fiber[i] : 0xFFFFu) << 8);
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->meta, m.data(), N * 4, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    }
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+int dsim_spins_get(dsim_spins* s, float* pos3, float* mag, float* phase, uint8_t* comp,
+                   uint16_t* fiber) {
+    if (!s) return kErrInvalid;
+    uint32_t N = s->N;
+    if (pos3) {
+        std::vector<float> a(N), b(N), c(N);
+        DSIM_CUDA_TRY(cudaMemcpyAsync(a.data(), s->x, N * 4, cudaMemcpyDeviceToHost, s->st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(b.data(), s->y, N * 4, cudaMemcpyDeviceToHost, s->st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(c.data(), s->z, N * 4, cudaMemcpyDeviceToHost, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+        for (uint32_t i = 0; i < N; i++) { pos3[3 * i] = a[i]; pos3[3 * i + 1] = b[i]; pos3[3 * i + 2] = c[i]; }
+    }
+    if (mag) DSIM_CUDA_TRY(cudaMemcpyAsync(mag, s->mag, N * 4, cudaMemcpyDeviceToHost, s->st));
+    if (phase) DSIM_CUDA_TRY(cudaMemcpyAsync(phase, s->phase, N * 4, cudaMemcpyDeviceToHost, s->st));
+    if (comp || fiber) {
+        std::vector<uint32_t> m(N);
+        DSIM_CUDA_TRY(cudaMemcpyAsync(m.data(), s->meta, N * 4, cudaMemcpyDeviceToHost, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+        for (uint32_t i = 0; i < N; i++) {
+            if (comp) comp[i] = (uint8_t)(m[i] & 0xFFu);
+            if (fiber) fiber[i] = (uint16_t)(m[i] >> 8);
+        }
+    }
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+static int ensure_cyl(dsim_spins* s) {
+    int rc;
+    if (!s->cpos && (rc = dev_alloc(&s->cpos, s->N, &s->bytes))) return rc;
+    if (!s->cseed && (rc = dev_alloc(&s->cseed, (size_t)4 * s->N, &s->bytes))) return rc;
+    return kOk;
+}
+
+int dsim_spins_set_cyl(dsim_spins* s, const float* pos3, const float* mag, const float* phase,
+                       const uint32_t* imo, const uint32_t* nearest) {
+    if (!s || !pos3) return kErrInvalid;
+    int rc = ensure_cyl(s);
+    if (rc) return rc;
+    uint32_t N = s->N;
+    std::vector<float4> p(N);
+    std::vector<uint32_t> sd((size_t)4 * N, 0u);
+    for (uint32_t i = 0; i < N; i++) {
+        p[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], phase ? phase[i] : 0.0f);
+        sd[4 * i + 2] = (imo ? imo[i] : 2u) + 1u;
+        sd[4 * i + 3] = nearest ? nearest[i] : 0xFFFFFFFFu;
+    }
+    DSIM_CUDA_TRY(cudaMemcpyAsync(s->cpos, p.data(), (size_t)N * 16, cudaMemcpyHostToDevice, s->st));
+    DSIM_CUDA_TRY(cudaMemcpyAsync(s->cseed, sd.data(), (size_t)N * 16, cudaMemcpyHostToDevice, s->st));
+    if (mag) DSIM_CUDA_TRY(cudaMemcpyAsync(s->mag, mag, N * 4, cudaMemcpyHostToDevice, s->st));
+    else {
+        std::vector<float> one(N, 1.0f);
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->mag, one.data(), N * 4, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    }
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+int dsim_spins_get_cyl(dsim_spins* s, float* pos3, float* mag, float* phase, uint32_t* imo,
+                       uint32_t* nearest) {
+    if (!s || !s->cpos) return kErrInvalid;
+    uint32_t N = s->N;
+    std::vector<float4> p(N);
+    std::vector<uint32_t> sd((size_t)4 * N);
+    DSIM_CUDA_TRY(cudaMemcpyAsync(p.data(), s->cpos, (size_t)N * 16, cudaMemcpyDeviceToHost, s->st));
+    DSIM_CUDA_TRY(cudaMemcpyAsync(sd.data(), s->cseed, (size_t)N * 16, cudaMemcpyDeviceToHost, s->st));
+    if (mag) DSIM_CUDA_TRY(cudaMemcpyAsync(mag, s->mag, N * 4, cudaMemcpyDeviceToHost, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    for (uint32_t i = 0; i < N; i++) {
+        if (pos3) { pos3[3 * i] = p[i].x; pos3[3 * i + 1] = p[i].y; pos3[3 * i + 2] = p[i].z; }
+        if (phase) phase[i] = p[i].w;
+        if (imo) imo[i] = sd[4 * i + 2] ? sd[4 * i + 2] - 1u : 2u;
+        if (nearest) nearest[i] = sd[4 * i + 3];
+    }
+    return kOk;
+}
+
+int dsim_spins_counts(dsim_spins* s, uint32_t* counts2N, int reset) {
+    if (!s) return kErrInvalid;
+    if (counts2N) {
+        DSIM_CUDA_TRY(cudaMemcpyAsync(counts2N, s->counts, (size_t)8 * s->N, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (reset) DSIM_CUDA_TRY(cudaMemsetAsync(s->counts, 0, (size_t)8 * s->N, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+int dsim_spins_scanned(dsim_spins* s, uint32_t* scannedN, int reset) {
+    if (!s) return kErrInvalid;
+    if (!s->tested) {
+        if (scannedN) memset(scannedN, 0, (size_t)4 * s->N);
+        return kOk;
+    }
+    if (scannedN) DSIM_CUDA_TRY(cudaMemcpyAsync(scannedN, s->tested, (size_t)4 * s->N, cudaMemcpyDeviceToHost, s->st));
+    if (reset) DSIM_CUDA_TRY(cudaMemsetAsync(s->tested, 0, (size_t)4 * s->N, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+int dsim_spins_status(dsim_spins* s, uint32_t* status, int reset) {
+    if (!s) return kErrInvalid;
+    uint32_t v = 0;
+    DSIM_CUDA_TRY(cudaMemcpyAsync(&v, s->status, 4, cudaMemcpyDeviceToHost, s->st));
+    if (reset) DSIM_CUDA_TRY(cudaMemsetAsync(s->status, 0, 4, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    if (status) *status = v;
+    return kOk;
+}
+
+void dsim_spins_free(dsim_spins* s) { spins_release(s); }
+
+// ---------------------------------------------------------------------------
+// runs
+// ---------------------------------------------------------------------------
+static int upload_grad_draws(dsim_spins* s, const float* gradPerStep, const float* replayDraws,
+                             uint32_t iterations, const float4** gradDev, const float4** drawsDev) {
+    int rc;
+    *gradDev = nullptr;
+    *drawsDev = nullptr;
+    if (gradPerStep) {
+        if (s->gradCap < iterations) {
+            cudaFree(s->grad); s->grad = nullptr; s->gradCap = 0;
+            if ((rc = dev_alloc(&s->grad, iterations))) return rc;
+            s->gradCap = iterations;
+        }
+        std::vector<float4> g(iterations);
+        for (uint32_t k = 0; k < iterations; k++)
+            g[k] = make_float4(gradPerStep[3 * k], gradPerStep[3 * k + 1], gradPerStep[3 * k + 2], 0.0f);
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->grad, g.data(), (size_t)iterations * 16, cudaMemcpyHostToDevice, s->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+        *gradDev = s->grad;
+    }
+    if (replayDraws) {
+        size_t need = (size_t)iterations * s->N;
+        if (s->drawsCap < need) {
+            cudaFree(s->draws); s->draws = nullptr; s->drawsCap = 0;
+            if ((rc = dev_alloc(&s->draws, need))) return rc;
+            s->drawsCap = need;
+        }
+        DSIM_CUDA_TRY(cudaMemcpyAsync(s->draws, replayDraws, need * 16, cudaMemcpyHostToDevice, s->st));
+        *drawsDev = s->draws;
+    }
+    return kOk;
+}
+
+int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const float g[3],
+                  const float* gradPerStep, uint32_t iterations, uint64_t seed, uint64_t step0,
+                  const float* replayDraws, int countCollisions) {
+    if (!m || !s || !p) { set_last_error(kErrInvalid, "dsim_mesh_run: null argument"); return kErrInvalid; }
+    MeshStepArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int k = 0; k < 4; k++) { a.sd[k] = p->stdDevs[k]; a.T2[k] = p->T2[k]; }
+    a.perm = p->permeability;
+    a.reflType = p->reflectionType;
+    a.clampHi = 1.0f - p->spinRadius;
+    a.clampLo = -1.0f + p->spinRadius;
+    a.dt = p->deltaTime;
+    a.pc = p->phaseConstant;
+    if (g) { a.gx = g[0]; a.gy = g[1]; a.gz = g[2]; }
+    a.iterations = iterations;
+    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
+    a.step0 = step0;
+    a.stream = 0;
+    a.maxSub = p->maxSubsegments ? p->maxSubsegments : 4096u;
+    a.status = s->status;
+    a.counts = (countCollisions & 1) ? s->counts : nullptr;
+    if (countCollisions & 2) {
+        if (!s->tested) {
+            int rc0 = dev_alloc(&s->tested, s->N, &s->bytes);
+            if (rc0) return rc0;
+            DSIM_CUDA_TRY(cudaMemsetAsync(s->tested, 0, (size_t)4 * s->N, s->st));
+        }
+        a.tested = s->tested;
+    }
+    int rc = upload_grad_draws(s, gradPerStep, replayDraws, iterations, &a.grad, &a.draws);
+    if (rc) return rc;
+    return launch_mesh_step(m->dev(), a, s->dev(), kLayoutSoA, replayDraws ? kRngReplay : kRngPhilox, s->st);
+}
+
+int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const float g[3],
+                 const float* gradPerStep, uint32_t iterations, uint64_t seed, uint64_t step0,
+                 const float* replayDraws, int countCollisions) {
+    if (!c || !s || !p || !s->cpos) { set_last_error(kErrInvalid, "dsim_cyl_run: bad argument (cylinder state set?)"); return kErrInvalid; }
+    CylStepArgs a;
+    memset(&a, 0, sizeof(a));
+    // SpinSystem::update dSim2/src/spinSystem.cpp:809-913 and cpuIntegrateSystem
+    // dSim2/src/spinKernelCpu.cpp:2-20: ADC scaled by spaceScale^2, sd = sqrt(2 ADC dt)
+    float ss2 = p->spaceScale * p->spaceScale;
+    float intra = p->intraAdc / ss2, extra = p->extraAdc / ss2, myelin = p->myelinAdc / ss2;
+    a.intraSd = sqrtf(2.0f * intra * p->deltaTime);
+    a.extraSd = sqrtf(2.0f * extra * p->deltaTime);
+    a.myelinSd = sqrtf(2.0f * myelin * p->deltaTime);
+    a.T2fiber = p->T2fiber; a.T2myelin = p->T2myelin; a.T2outside = p->T2outside;
+    a.perm = p->permeability;
+    a.inRadPropSq = p->innerRadiusProportion * p->innerRadiusProportion;
+    a.clampHi = 1.0f - p->spinRadius;
+    a.clampLo = -1.0f + p->spinRadius;
+    a.dt = p->deltaTime;
+    a.pc = p->phaseConstant;
+    if (g) { a.gx = g[0]; a.gy = g[1]; a.gz = g[2]; }
+    a.iterations = iterations;
+    a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
+    a.step0 = step0;
+    a.status = s->status;
+    a.counts = countCollisions ? s->counts : nullptr;
+    int rc = upload_grad_draws(s, gradPerStep, replayDraws, iterations, &a.grad, &a.draws);
+    if (rc) return rc;
+    CylSpinsDev S;
+    S.pos = s->cpos; S.seed4 = s->cseed; S.mag = s->mag; S.N = s->N;
+    return launch_cyl_step(c->dev(), a, S, replayDraws ? kRngReplay : kRngPhilox, s->st);
+}
+
+int dsim_signal(dsim_spins* s, double region, double out[15]) {
+    if (!s || !out) return kErrInvalid;
+    SpinsDev S = s->dev();
+    int layout = kLayoutSoA;
+    if (s->cpos) {
+        S.x = reinterpret_cast<float*>(s->cpos);
+        S.meta = s->cseed;
+        layout = 2;
+    }
+    int rc = launch_signal(S, layout, region, s->partials, s->sig, s->st);
+    if (rc) return rc;
+    DSIM_CUDA_TRY(cudaMemcpyAsync(out, s->sig, 15 * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    return kOk;
+}
+
+int dsim_sync(dsim_spins* s) {
+    if (!s) return kErrInvalid;
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+int dsim_timer_start(dsim_spins* s) {
+    if (!s) return kErrInvalid;
+    DSIM_CUDA_TRY(cudaEventRecord(s->ev0, s->st));
+    return kOk;
+}
+
+int dsim_timer_stop(dsim_spins* s, float* ms) {
+    if (!s) return kErrInvalid;
+    DSIM_CUDA_TRY(cudaEventRecord(s->ev1, s->st));
+    DSIM_CUDA_TRY(cudaEventSynchronize(s->ev1));
+    float v = 0;
+    DSIM_CUDA_TRY(cudaEventElapsedTime(&v, s->ev0, s->ev1));
+    if (ms) *ms = v;
+    return kOk;
+}
+
+int dsim_flush_l2(dsim_spins* s, size_t bytes) {
+    if (!s) return kErrInvalid;
+    if (s->flushCap < bytes) {
+        cudaFree(s->flush); s->flush = nullptr; s->flushCap = 0;
+        if (cudaMalloc(&s->flush, bytes) != cudaSuccess) { cudaGetLastError(); set_last_error(kErrNoMem, "flush buffer"); return kErrNoMem; }
+        s->flushCap = bytes;
+    }
+    DSIM_CUDA_TRY(cudaMemsetAsync(s->flush, s->flushCap & 0xFF, bytes, s->st));
+    return kOk;
+}
+
+}  // extern "C"
+
+namespace dsim {
+int launch_rng_draws(uint64_t seed, uint32_t spin0, uint64_t step, uint32_t stream, uint32_t n,
+                     uint32_t* raw, float* out, cudaStream_t st);
+}
+
+extern "C" int dsim_rng_draws(uint64_t seed, uint32_t spin0, uint64_t step, uint32_t stream,
+                              uint32_t n, uint32_t* raw, float* draws4) {
+    if (n == 0) return kOk;
+    uint32_t* dRaw = nullptr;
+    float* dOut = nullptr;
+    int rc = dev_alloc(&dRaw, (size_t)4 * n);
+    if (rc) return rc;
+    if ((rc = dev_alloc(&dOut, (size_t)4 * n))) { cudaFree(dRaw); return rc; }
+    rc = launch_rng_draws(seed, spin0, step, stream, n, dRaw, dOut, 0);
+    if (!rc && raw && cudaMemcpy(raw, dRaw, (size_t)16 * n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
+    if (!rc && draws4 && cudaMemcpy(draws4, dOut, (size_t)16 * n, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
+    if (rc == kErrCuda) set_last_error(kErrCuda, "dsim_rng_draws: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(dRaw);
+    cudaFree(dOut);
+    return rc;
+}

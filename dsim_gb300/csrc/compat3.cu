@@ -1,0 +1,306 @@
+// compat3.cu -- libdsim3.so: the dSim3 plugin boundary (include/dsim3_abi.h),
+// a drop-in for rfdougherty/dSim dSim3/src/spinSystem.cu + spinSystem.cuh.
+//
+// The reference binds its substrate to texture references and __constant__
+// symbols; here the same calls record device pointers and values in one
+// process-wide state block, and integrateSystem launches the GB300 step
+// kernel on the legacy default stream (so it is ordered with the reference's
+// synchronous copies).  Compact per-cell triangle lists and per-triangle
+// records are derived once from the bound arrays and cached until a binding
+// changes.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#pragma GCC visibility push(default)
+#include "../../include/dsim3_abi.h"
+#pragma GCC visibility pop
+#include "common.cuh"
+#include "engine.h"
+
+namespace dsim {
+static thread_local std::string g_last_error;
+void set_last_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = std::string("dsim3 error ") + std::to_string(code) + ": " + buf;
+}
+void set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+    set_last_error(kErrCuda, "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+const char* last_error_message() { return g_last_error.c_str(); }
+}  // namespace dsim
+
+using namespace dsim;
+
+namespace {
+
+struct State {
+    std::mutex mu;
+    int last_status = 0;
+    // constants (names of the reference's __constant__ symbols)
+    uint32_t reflectionType = 1, triSearchMethod = 0, nFibers = 0, nCompartments = 4;
+    float permeability = 0.0f, deltaTime = 0.0f, cubeLength = 0.0f;
+    float T2[4] = {80.0f, 80.0f, 7.5f, 80.0f};
+    float sd[4] = {0, 0, 0, 0};
+    uint32_t numCubes = 0, totalNumCubes = 0, maxTPC = 0;
+    // bound arrays
+    const float* V = nullptr; int nV = 0;
+    const float* H = nullptr; int nH = 0;
+    const uint32_t* triInfo = nullptr; int nTI = 0;
+    const uint32_t* boundCounter = nullptr;
+    const uint32_t* boundTic = nullptr;
+    // replay hook
+    const float4* replay = nullptr;
+    uint32_t* counts = nullptr;
+    // derived (cached) device data
+    struct Key {
+        const void *V, *H, *TI, *tic, *cc;
+        int nH, nTI;
+        uint32_t n, maxTPC;
+        bool operator==(const Key& o) const { return !memcmp(this, &o, sizeof(Key)); }
+    } key;
+    bool have = false;
+    TriPlane* plane = nullptr;
+    TriBary* bary = nullptr;
+    uint32_t* cell_start = nullptr;
+    uint32_t* cell_tri = nullptr;
+    uint32_t* status = nullptr;
+    uint32_t statusHost = 0;
+    void release() {
+        cudaFree(plane); cudaFree(bary); cudaFree(cell_start); cudaFree(cell_tri);
+        plane = nullptr; bary = nullptr; cell_start = nullptr; cell_tri = nullptr;
+        have = false;
+    }
+};
+State& S() {
+    static State s;
+    return s;
+}
+
+int fail(int code) {
+    S().last_status = code;
+    return code;
+}
+
+// Build records and compact lists from the bound arrays and the dense grid.
+int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
+    State::Key k;
+    memset(&k, 0, sizeof(k));
+    k.V = s.V; k.H = s.H; k.TI = s.triInfo; k.tic = tic; k.cc = cc; k.nH = s.nH; k.nTI = s.nTI;
+    k.n = s.numCubes; k.maxTPC = s.maxTPC;
+    if (s.have && k == s.key) return kOk;
+    s.release();
+    if (!s.V || !s.H || !s.triInfo || s.nH % 12 || s.nTI % 3 || s.nH / 12 != s.nTI / 3) {
+        set_last_error(kErrInvalid, "integrateSystem: vertices, triangle helpers and triInfo must be bound (helpers %d, triInfo %d)", s.nH, s.nTI);
+        return kErrInvalid;
+    }
+    if (!tic || !cc || s.numCubes == 0 || s.cubeLength <= 0.0f) {
+        set_last_error(kErrInvalid, "integrateSystem: grid (k_numCubes, k_cubeLength, trianglesInCubes, cubeCounter) not set");
+        return kErrInvalid;
+    }
+    uint32_t nT = (uint32_t)(s.nH / 12);
+    uint32_t ncells = s.numCubes * s.numCubes * s.numCubes;
+    if (!s.status) DSIM_CUDA_TRY(cudaMalloc(&s.status, 4));
+    DSIM_CUDA_TRY(cudaMemset(s.status, 0, 4));
+    DSIM_CUDA_TRY(cudaMalloc(&s.plane, (size_t)(nT ? nT : 1) * sizeof(TriPlane)));
+    DSIM_CUDA_TRY(cudaMalloc(&s.bary, (size_t)(nT ? nT : 1) * sizeof(TriBary)));
+    DSIM_CUDA_TRY(cudaMalloc(&s.cell_start, ((size_t)ncells + 1) * 4));
+    int rc = launch_records_from_helpers(nT, s.V, s.H, s.triInfo, s.plane, s.bary, 0);
+    if (rc) return rc;
+    uint32_t* scratch = nullptr;
+    DSIM_CUDA_TRY(cudaMalloc(&scratch, scan_scratch_words(ncells) * 4));
+    rc = launch_scan_exclusive(cc, s.cell_start, ncells, scratch, 0);
+    uint32_t total = 0;
+    if (!rc && cudaMemcpy(&total, s.cell_start + ncells, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
+    if (!rc && cudaMalloc(&s.cell_tri, (size_t)(total ? total : 1) * 4) != cudaSuccess) rc = kErrNoMem;
+    if (!rc) rc = launch_dense_to_csr(ncells, s.maxTPC, nT, cc, tic, s.cell_start, s.cell_tri, s.status, 0);
+    uint32_t st = 0;
+    if (!rc && cudaMemcpy(&st, s.status, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
+    cudaFree(scratch);
+    if (rc) { set_last_error(rc, "integrateSystem: deriving cell lists failed"); return rc; }
+    if (st) {
+        set_last_error(kErrFormat, "integrateSystem: trianglesInCubes names a triangle >= %u or a cell above k_maxTrianglesPerCube", nT);
+        return kErrFormat;
+    }
+    s.key = k;
+    s.have = true;
+    return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+void checkCUDA(void) {}
+
+void allocateArray(void** devPtr, int size) {
+    if (!devPtr || size < 0) { set_last_error(kErrInvalid, "allocateArray: bad argument"); fail(kErrInvalid); return; }
+    cudaError_t e = cudaMalloc(devPtr, size > 0 ? (size_t)size : 1);
+    if (e != cudaSuccess) {
+        *devPtr = nullptr;
+        cudaGetLastError();
+        set_last_error(kErrNoMem, "allocateArray(%d): %s", size, cudaGetErrorString(e));
+        fail(kErrNoMem);
+    }
+}
+
+void freeArray(void* devPtr) {
+    if (devPtr) cudaFree(devPtr);
+}
+
+void threadSync(void) {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { set_last_cuda_error(e, "threadSync", __FILE__, __LINE__); fail(kErrCuda); }
+}
+
+void copyArrayFromDevice(void* host, const void* device, unsigned int vbo, int size) {
+    if (vbo) { set_last_error(kErrInvalid, "copyArrayFromDevice: OpenGL buffers are unavailable"); fail(kErrInvalid); return; }
+    if (size <= 0) return;
+    cudaError_t e = cudaMemcpy(host, device, (size_t)size, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "copyArrayFromDevice", __FILE__, __LINE__); fail(kErrCuda); }
+}
+
+void copyArrayToDevice(void* device, const void* host, int offset, int size) {
+    if (size <= 0) return;
+    cudaError_t e = cudaMemcpy((char*)device + offset, host, (size_t)size, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "copyArrayToDevice", __FILE__, __LINE__); fail(kErrCuda); }
+}
+
+void registerGLBufferObject(unsigned int) {
+    set_last_error(kErrInvalid, "registerGLBufferObject: OpenGL interop is unavailable");
+    fail(kErrInvalid);
+}
+void unregisterGLBufferObject(unsigned int) {
+    set_last_error(kErrInvalid, "unregisterGLBufferObject: OpenGL interop is unavailable");
+    fail(kErrInvalid);
+}
+
+static void read_table4(const void* host, int size, float out[4]) {
+    // the reference passes &devicePointer with size sizeof(float); a caller may
+    // also pass the four values themselves (size 16)
+    if (size == 4 * (int)sizeof(float)) { memcpy(out, host, 16); return; }
+    const float* dptr = nullptr;
+    memcpy(&dptr, host, sizeof(dptr));
+    if (!dptr) { set_last_error(kErrInvalid, "copyConstantToDevice: null table pointer"); fail(kErrInvalid); return; }
+    cudaError_t e = cudaMemcpy(out, dptr, 16, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "copyConstantToDevice(table)", __FILE__, __LINE__); fail(kErrCuda); }
+}
+
+void copyConstantToDevice(void* device, const void* host, int offset, int size) {
+    (void)offset;
+    State& s = S();
+    std::lock_guard<std::mutex> lk(s.mu);
+    const char* name = (const char*)device;
+    if (!name || !host) { set_last_error(kErrInvalid, "copyConstantToDevice: null argument"); fail(kErrInvalid); return; }
+    uint32_t u = 0;
+    float f = 0.0f;
+    if (size >= 4) { memcpy(&u, host, 4); memcpy(&f, host, 4); }
+    if (!strcmp(name, "k_reflectionType")) s.reflectionType = u;
+    else if (!strcmp(name, "k_triSearchMethod")) s.triSearchMethod = u;
+    else if (!strcmp(name, "k_nFibers")) s.nFibers = u;
+    else if (!strcmp(name, "k_nCompartments")) s.nCompartments = u;
+    else if (!strcmp(name, "k_permeability")) s.permeability = f;
+    else if (!strcmp(name, "k_deltaTime")) s.deltaTime = f;
+    else if (!strcmp(name, "k_T2Values")) read_table4(host, size, s.T2);
+    else if (!strcmp(name, "k_stdDevs")) read_table4(host, size, s.sd);
+    else if (!strcmp(name, "k_numCubes")) s.numCubes = u;
+    else if (!strcmp(name, "k_totalNumCubes")) s.totalNumCubes = u;
+    else if (!strcmp(name, "k_maxTrianglesPerCube")) s.maxTPC = u;
+    else if (!strcmp(name, "k_cubeLength")) s.cubeLength = f;
+    else { set_last_error(kErrInvalid, "copyConstantToDevice: unknown symbol %s", name); fail(kErrInvalid); }
+}
+
+void bindCubeCounter(unsigned int* ptr, int) { std::lock_guard<std::mutex> lk(S().mu); S().boundCounter = ptr; }
+void unbindCubeCounter(void) { std::lock_guard<std::mutex> lk(S().mu); S().boundCounter = nullptr; }
+void bindTrianglesInCubes(unsigned int* ptr, int) { std::lock_guard<std::mutex> lk(S().mu); S().boundTic = ptr; }
+void unbindTrianglesInCubes(void) { std::lock_guard<std::mutex> lk(S().mu); S().boundTic = nullptr; }
+void bindVertices(float* ptr, int size) { std::lock_guard<std::mutex> lk(S().mu); if (size > 0) { S().V = ptr; S().nV = size; } }
+void unbindVertices(void) { std::lock_guard<std::mutex> lk(S().mu); S().V = nullptr; S().nV = 0; }
+void bindTriangleHelpers(float* ptr, int size) { std::lock_guard<std::mutex> lk(S().mu); if (size > 0) { S().H = ptr; S().nH = size; } }
+void unbindTriangleHelpers(void) { std::lock_guard<std::mutex> lk(S().mu); S().H = nullptr; S().nH = 0; }
+// the R-tree search path (triSearchMethod 1) is not used: searchMethod is fixed
+// to 0 in the reference (dSim3/src/spinSystem.cpp:843); the arrays are accepted
+void bindRTreeArray(float*, int) {}
+void unbindRTreeArray(void) {}
+void bindTreeIndexArray(unsigned int*, int) {}
+void unbindTreeIndexArray(void) {}
+void bindTriInfo(unsigned int* ptr, int size) { std::lock_guard<std::mutex> lk(S().mu); if (size > 0) { S().triInfo = ptr; S().nTI = size; } }
+void unbindTriInfo(void) { std::lock_guard<std::mutex> lk(S().mu); S().triInfo = nullptr; S().nTI = 0; }
+
+void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo, float deltaTime,
+                     float permeability, int numBodies, dsim_float3 magneticGradient,
+                     float phaseConstant, unsigned int iterations, unsigned int* trianglesInCubes,
+                     unsigned int* cubeCounter) {
+    State& s = S();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (numBodies <= 0 || iterations == 0) return;
+    if (!pos || !randSeed || !spinInfo) { set_last_error(kErrInvalid, "integrateSystem: null state array"); fail(kErrInvalid); return; }
+    const uint32_t* tic = trianglesInCubes ? trianglesInCubes : s.boundTic;
+    const uint32_t* cc = cubeCounter ? cubeCounter : s.boundCounter;
+    int rc = derive(s, tic, cc);
+    if (rc) { fail(rc); return; }
+    MeshDev g;
+    g.cell_start = s.cell_start; g.cell_tri = s.cell_tri; g.plane = s.plane; g.bary = s.bary;
+    g.n = s.numCubes; g.L = s.cubeLength;
+    MeshStepArgs a;
+    memset(&a, 0, sizeof(a));
+    for (int k = 0; k < 4; k++) { a.sd[k] = s.sd[k]; a.T2[k] = s.T2[k]; }
+    a.perm = permeability;
+    a.reflType = s.reflectionType;
+    // the reference's CPU step clamps to +-(1 - 0.005) (spinKernelCpu.cpp:469-474)
+    a.clampHi = 1.0f - 0.005f;
+    a.clampLo = -1.0f + 0.005f;
+    a.dt = deltaTime;
+    a.pc = phaseConstant;
+    a.gx = magneticGradient.x; a.gy = magneticGradient.y; a.gz = magneticGradient.z;
+    a.iterations = iterations;
+    a.maxSub = 4096;
+    a.status = s.status;
+    a.counts = s.counts;
+    a.draws = s.replay;
+    SpinsDev sp;
+    memset(&sp, 0, sizeof(sp));
+    sp.x = pos;
+    sp.meta = reinterpret_cast<uint32_t*>(spinInfo);
+    sp.seed = randSeed;
+    sp.N = (uint32_t)numBodies;
+    rc = launch_mesh_step(g, a, sp, kLayoutAoS, s.replay ? kRngReplay : kRngPhiloxPerSpinKey, 0);
+    if (rc) fail(rc);
+}
+
+void integrateSystemVBO(unsigned int, unsigned int*, dsim_spinData*, float, float, int, dsim_float3,
+                        float, unsigned int, unsigned int*, unsigned int*) {
+    set_last_error(kErrInvalid, "integrateSystemVBO: OpenGL position buffers are unavailable");
+    fail(kErrInvalid);
+}
+
+const char* dsim3_last_error(void) { return last_error_message(); }
+int dsim3_last_status(void) {
+    int v = S().last_status;
+    S().last_status = 0;
+    return v;
+}
+
+void dsim3_set_replay(const float* draws, unsigned int* counts) {
+    std::lock_guard<std::mutex> lk(S().mu);
+    S().replay = reinterpret_cast<const float4*>(draws);
+    S().counts = counts;
+}
+
+unsigned int dsim3_status(void) {
+    State& s = S();
+    std::lock_guard<std::mutex> lk(s.mu);
+    if (!s.status) return 0;
+    uint32_t v = 0;
+    cudaMemcpy(&v, s.status, 4, cudaMemcpyDeviceToHost);
+    cudaMemset(s.status, 0, 4);
+    return v;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+// engine.h -- internal interfaces shared by the engine's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace dsim {
+
+enum Layout : int { kLayoutSoA = 0, kLayoutAoS = 1 };
+enum Rng : int { kRngPhilox = 0, kRngReplay = 1, kRngPhiloxPerSpinKey = 2 };
+
+// device view of a mesh substrate (CSR cell lists over per-triangle records)
+struct MeshDev {
+    const uint32_t* cell_start;  // ncells + 1
+    const uint32_t* cell_tri;    // triangle index per entry, ascending in a cell
+    const TriPlane* plane;       // per triangle
+    const TriBary* bary;         // per triangle
+    uint32_t n;                  // cells per axis
+    float L;                     // cell edge, normalised units (2 / n)
+};
+
+// device view of spin state.  SoA: x,y,z,mag,phase float[N], meta uint32[N]
+// (compartment | fiber << 8).  AoS (reference arrays): x = float3 positions,
+// meta = spinData records (12 B); y, z, mag, phase unused.
+struct SpinsDev {
+    float *x, *y, *z, *mag, *phase;
+    uint32_t* meta;
+    uint32_t* seed;  // per-spin Philox key (2 words) for kRngPhiloxPerSpinKey
+    uint32_t N;
+};
+
+struct MeshStepArgs {
+    float sd[4];          // per-compartment step standard deviation (normalised)
+    float T2[4];          // per-compartment T2 (ms)
+    float perm;           // permeation probability per hit
+    uint32_t reflType;    // 1 mirror reflection, 0 return to the segment start
+    float clampHi, clampLo;  // 1 - spinRadius, -1 + spinRadius
+    float dt, pc;         // time step (ms), phase constant 2*pi*gamma*dt
+    float gx, gy, gz;     // scaled gradient, constant over the call
+    const float4* grad;   // or one scaled gradient per iteration
+    uint32_t iterations;
+    uint32_t key0, key1;  // Philox key (kRngPhilox)
+    uint64_t step0;       // global index of the first step
+    uint32_t stream;      // Philox counter word 3
+    const float4* draws;  // replay stream [iterations][N] (kRngReplay)
+    uint32_t maxSub;      // cap on collision sub-segments per step
+    uint32_t* status;     // device status word (StatusBits)
+    uint32_t* counts;     // [2N] reflections, permeations (or null)
+    uint32_t* tested;     // [N] grid entries scanned (or null)
+};
+
+// ---- mesh.cu --------------------------------------------------------------
+int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
+                             const uint32_t* membrane, const uint32_t* fiber, TriPlane* plane,
+                             TriBary* bary, cudaStream_t st);
+int launch_records_from_helpers(uint32_t nT, const float* V, const float* H,
+                                const uint32_t* triInfo, TriPlane* plane, TriBary* bary,
+                                cudaStream_t st);
+int launch_tri_cells(bool fill, uint32_t nT, const float* V, const uint32_t* trgls, uint32_t n,
+                     float L, uint32_t* counter, const uint32_t* start, uint32_t* cell_tri,
+                     cudaStream_t st);
+int launch_sort_cells(uint32_t ncells, const uint32_t* start, uint32_t* cell_tri, cudaStream_t st);
+int launch_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT, const uint32_t* counter,
+                        const uint32_t* dense, const uint32_t* start, uint32_t* cell_tri,
+                        uint32_t* status, cudaStream_t st);
+int launch_mesh_step(const MeshDev& g, const MeshStepArgs& a, const SpinsDev& S, int layout,
+                     int rng, cudaStream_t st);
+
+// ---- scan.cu --------------------------------------------------------------
+// exclusive prefix sum: out[0..n] (out[n] = total); scratch >= scan_scratch_words(n)
+size_t scan_scratch_words(uint32_t n);
+int launch_scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,
+                          cudaStream_t st);
+
+// ---- reduce.cu ------------------------------------------------------------
+// Ensemble signal in FP64: out[c] = {sum m cos(phi), sum m sin(phi), count}
+// for c = 0 (all spins) and 1 + compartment.  region > 0 keeps only spins
+// with |x|,|y|,|z| < region (dSim2's getMrSignal).  partials: scratch of
+// reduce_scratch_doubles(N) doubles.
+size_t reduce_scratch_doubles(uint32_t N);
+int launch_signal(const SpinsDev& S, int layout, double region, double* partials, double* out15,
+                  cudaStream_t st);
+
+// ---- cyl.cu ---------------------------------------------------------------
+struct CylDev {
+    const float4* fibers;       // {x, y, z, r^2}; the axis coordinate is 2.0
+    const uint32_t* cube_count; // dense reference grid (dSim2 addEntities)
+    const uint32_t* cubes;
+    uint32_t n, maxFPC;
+    float L;
+    uint32_t nF;                // number of fibers (index bound)
+};
+struct CylSpinsDev {
+    float4* pos;       // x, y, z, phase (dSim2 GPU layout)
+    uint32_t* seed4;   // s0, s1, imo + 1 (0 = derive from w), inside fiber / nearest
+    float* mag;        // or null (no T2 in the dSim2 GPU ABI)
+    uint32_t N;
+};
+struct CylStepArgs {
+    float intraSd, extraSd, myelinSd;
+    float T2fiber, T2myelin, T2outside;
+    float perm, inRadPropSq;
+    float clampHi, clampLo;
+    float dt, pc;
+    float gx, gy, gz;
+    const float4* grad;
+    uint32_t iterations;
+    uint32_t key0, key1;
+    uint64_t step0;
+    uint32_t stream;
+    const float4* draws;
+    uint32_t* status;
+    uint32_t* counts;
+};
+// rng: kRngPhilox (key0/key1), kRngPhiloxPerSpinKey (seed4.x/.y), kRngReplay
+int launch_cyl_step(const CylDev& g, const CylStepArgs& a, const CylSpinsDev& S, int rng,
+                    cudaStream_t st);
+
+// ---- host helpers (engine.cpp) -------------------------------------------
+const char* last_error_message();
+
+}  // namespace dsim

@@ -1,0 +1,287 @@
+"""Python front end of the native engine (include/dsim.h).
+
+MeshSystem and CylinderSystem hold a device-resident substrate and spin state
+and mirror the calls of the reference's SpinSystem (dSim3/src/spinSystem.h:143-310,
+dSim2/src/spinSystem.h:134-222): set the gradient, updateSpins(dt, iterations),
+getMrSignal().  Unit conversions follow the reference exactly (float32
+arithmetic in the same order) so that parameters match bit for bit.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, native
+
+F = np.float32
+TWOPI = F(6.28318530717959)  # dSim3/src/spinSystem.cpp:20
+
+
+def std_devs(extraAdc, intraAdc, myelinAdc, spaceScale, deltaTime):
+    """Per-compartment step sigma, SpinSystem ctor dSim3/src/spinSystem.cpp:52-56:
+    sqrt(2*ADC/(spaceScale^2)*dt) for compartments 0 extra, 1 intra, 2 myelin, 3 glia(intra)."""
+    ss = F(spaceScale)
+    dt = F(deltaTime)
+    out = []
+    for adc in (extraAdc, intraAdc, myelinAdc, intraAdc):
+        out.append(np.sqrt(F(2) * F(adc) / (ss * ss) * dt))
+    return np.array(out, F)
+
+
+def grad_scaled(G, spaceScale):
+    """gradScaled = G[mT/m] * 1e-9f * spaceScale (dSim3/src/spinSystem.cpp:1931)."""
+    g = np.asarray(G, F)
+    return (g * F(1e-9)) * F(spaceScale)
+
+
+def phase_constant(gamma, deltaTime):
+    """2*pi*gamma*dt (dSim3/src/spinSystem.cpp:1938); gamma in kHz/T, dt in ms."""
+    return TWOPI * F(gamma) * F(deltaTime)
+
+
+class DeviceInfo:
+    def __init__(self):
+        name = C.create_string_buffer(256)
+        sm = C.c_int(0)
+        mem = C.c_size_t(0)
+        check(native().dsim_device_info(name, 256, C.byref(sm), C.byref(mem)))
+        self.name = name.value.decode()
+        self.sm_count = sm.value
+        self.total_mem = mem.value
+
+
+class Spins:
+    """Device-resident spin state with its own CUDA stream."""
+
+    def __init__(self, N):
+        self.N = int(N)
+        h = C.c_void_p()
+        check(native().dsim_spins_create(self.N, C.byref(h)))
+        self.h = h
+
+    def free(self):
+        if self.h:
+            native().dsim_spins_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def set(self, pos, mag=None, phase=None, comp=None, fiber=None):
+        c = lambda a, t: None if a is None else np.ascontiguousarray(a, t)
+        check(native().dsim_spins_set(self.h, c(pos, F).reshape(-1) if pos is not None else None,
+                                      c(mag, F), c(phase, F), c(comp, np.uint8), c(fiber, np.uint16)))
+
+    def get(self):
+        N = self.N
+        pos = np.zeros(3 * N, F); mag = np.zeros(N, F); ph = np.zeros(N, F)
+        comp = np.zeros(N, np.uint8); fib = np.zeros(N, np.uint16)
+        check(native().dsim_spins_get(self.h, pos, mag, ph, comp, fib))
+        return pos, mag, ph, comp, fib
+
+    def set_cyl(self, pos, mag=None, phase=None, imo=None, nearest=None):
+        c = lambda a, t: None if a is None else np.ascontiguousarray(a, t)
+        check(native().dsim_spins_set_cyl(self.h, c(pos, F).reshape(-1), c(mag, F), c(phase, F),
+                                          c(imo, np.uint32), c(nearest, np.uint32)))
+
+    def get_cyl(self):
+        N = self.N
+        pos = np.zeros(3 * N, F); mag = np.zeros(N, F); ph = np.zeros(N, F)
+        imo = np.zeros(N, np.uint32); near = np.zeros(N, np.uint32)
+        check(native().dsim_spins_get_cyl(self.h, pos, mag, ph, imo, near))
+        return pos, mag, ph, imo, near
+
+    def counts(self, reset=False):
+        out = np.zeros(2 * self.N, np.uint32)
+        check(native().dsim_spins_counts(self.h, out, 1 if reset else 0))
+        return out.reshape(-1, 2)
+
+    def scanned(self, reset=False):
+        out = np.zeros(self.N, np.uint32)
+        check(native().dsim_spins_scanned(self.h, out, 1 if reset else 0))
+        return out
+
+    def status(self, reset=True):
+        v = C.c_uint32(0)
+        check(native().dsim_spins_status(self.h, C.byref(v), 1 if reset else 0))
+        return v.value
+
+    def signal(self, region=0.0):
+        """FP64 sums per (all, compartment 0..3): array (5, 3) of X, Y, n."""
+        out = np.zeros(15, np.float64)
+        check(native().dsim_signal(self.h, float(region), out))
+        return out.reshape(5, 3)
+
+    def sync(self):
+        check(native().dsim_sync(self.h))
+
+    def timer_start(self):
+        check(native().dsim_timer_start(self.h))
+
+    def timer_stop(self):
+        ms = C.c_float(0)
+        check(native().dsim_timer_stop(self.h, C.byref(ms)))
+        return ms.value
+
+    def flush_l2(self, nbytes=512 << 20):
+        check(native().dsim_flush_l2(self.h, int(nbytes)))
+
+    @property
+    def nbytes(self):
+        return int(native().dsim_spins_bytes(self.h))
+
+
+def signal_from_sums(sums):
+    """S = |X + iY| / n per row (0 when n = 0), as getMrSignal does."""
+    s = np.asarray(sums, np.float64).reshape(-1, 3)
+    out = np.zeros(len(s))
+    nz = s[:, 2] > 0
+    out[nz] = np.sqrt(s[nz, 0] ** 2 + s[nz, 1] ** 2) / s[nz, 2]
+    return out
+
+
+class Mesh:
+    """Triangle-mesh substrate on the device with its GPU-built grid."""
+
+    def __init__(self, handle):
+        self.h = handle
+        info = np.zeros(8, np.uint64)
+        check(native().dsim_mesh_info(self.h, info))
+        (self.nV, self.nT, self.nFibers, self.numCubes, self.entries, self.max_per_cell,
+         self.nbytes, self.nonempty) = [int(x) for x in info]
+
+    @classmethod
+    def load(cls, path, spaceScale, numCubes=50):
+        h = C.c_void_p()
+        check(native().dsim_mesh_load(str(path).encode(), float(spaceScale), int(numCubes), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, vertices_um, trgls, membrane, fiber, spaceScale, numCubes=50):
+        v = np.ascontiguousarray(vertices_um, F).reshape(-1)
+        t = np.ascontiguousarray(trgls, np.uint32).reshape(-1)
+        m = None if membrane is None else np.ascontiguousarray(membrane, np.uint32)
+        f = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
+        h = C.c_void_p()
+        check(native().dsim_mesh_create(v, len(v) // 3, t, m, f, len(t) // 3, float(spaceScale),
+                                        int(numCubes), C.byref(h)))
+        return cls(h)
+
+    def grid(self):
+        n3 = self.numCubes ** 3
+        start = np.zeros(n3 + 1, np.uint32)
+        tri = np.zeros(max(1, self.entries), np.uint32)
+        check(native().dsim_mesh_grid(self.h, start, tri))
+        return start, tri[:self.entries]
+
+    def arrays(self):
+        v = np.zeros(3 * self.nV, F)
+        ti = np.zeros(3 * self.nT, np.uint32)
+        check(native().dsim_mesh_arrays(self.h, v, ti))
+        return v, ti
+
+    def free(self):
+        if self.h:
+            native().dsim_mesh_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def mesh_params(stdDevs, T2, permeability, deltaTime, phaseConstant, reflectionType=1,
+                spinRadius=0.005, maxSubsegments=0):
+    p = _lib.MeshParams()
+    p.stdDevs[:] = [float(x) for x in stdDevs]
+    p.T2[:] = [float(x) for x in T2]
+    p.permeability = float(permeability)
+    p.reflectionType = int(reflectionType)
+    p.spinRadius = float(spinRadius)
+    p.deltaTime = float(deltaTime)
+    p.phaseConstant = float(phaseConstant)
+    p.maxSubsegments = int(maxSubsegments)
+    return p
+
+
+def mesh_run(mesh, spins, params, g=(0, 0, 0), iterations=1, seed=1, step0=0, draws=None,
+             grad_per_step=None, count=False, scanned=False):
+    gg = np.ascontiguousarray(g, F)
+    d = None if draws is None else np.ascontiguousarray(draws, F).reshape(-1)
+    gp = None if grad_per_step is None else np.ascontiguousarray(grad_per_step, F).reshape(-1)
+    check(native().dsim_mesh_run(mesh.h, spins.h, C.byref(params), gg, gp, int(iterations),
+                                 int(seed), int(step0), d, (1 if count else 0) | (2 if scanned else 0)))
+
+
+class Cylinders:
+    """Cylinder substrate (dSim2 fibers) with the reference's grid."""
+
+    def __init__(self, handle):
+        self.h = handle
+        geom = np.zeros(3, np.uint32)
+        L = C.c_float(0)
+        check(native().dsim_cyl_info(self.h, geom, C.byref(L), None, None, None))
+        self.numCubes, self.maxFPC, self.nF = [int(x) for x in geom]
+        self.cubeLength = F(L.value)
+
+    @classmethod
+    def load(cls, path, spaceScale):
+        h = C.c_void_p()
+        check(native().dsim_cyl_load(str(path).encode(), float(spaceScale), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, fiberPos4, maxRadius):
+        fp = np.ascontiguousarray(fiberPos4, F).reshape(-1)
+        h = C.c_void_p()
+        check(native().dsim_cyl_create(fp, len(fp) // 4, float(maxRadius), C.byref(h)))
+        return cls(h)
+
+    def grid(self):
+        geom = np.zeros(3, np.uint32)
+        L = C.c_float(0)
+        n3 = self.numCubes ** 3
+        cc = np.zeros(n3, np.uint32)
+        cubes = np.zeros(max(1, n3 * self.maxFPC), np.uint32)
+        fp = np.zeros(max(1, 4 * self.nF), F)
+        check(native().dsim_cyl_info(self.h, geom, C.byref(L), cc, cubes, fp))
+        return cc, cubes, fp[:4 * self.nF]
+
+    def free(self):
+        if self.h:
+            native().dsim_cyl_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def cyl_params(intraAdc, extraAdc, myelinAdc, spaceScale, T2fiber, T2myelin, T2outside,
+               permeability, innerRadiusProportion, deltaTime, phaseConstant, spinRadius=0.005):
+    p = _lib.CylParams()
+    p.intraAdc, p.extraAdc, p.myelinAdc = float(intraAdc), float(extraAdc), float(myelinAdc)
+    p.spaceScale = float(spaceScale)
+    p.T2fiber, p.T2myelin, p.T2outside = float(T2fiber), float(T2myelin), float(T2outside)
+    p.permeability = float(permeability)
+    p.innerRadiusProportion = float(innerRadiusProportion)
+    p.spinRadius = float(spinRadius)
+    p.deltaTime = float(deltaTime)
+    p.phaseConstant = float(phaseConstant)
+    return p
+
+
+def cyl_run(cyl, spins, params, g=(0, 0, 0), iterations=1, seed=1, step0=0, draws=None,
+            grad_per_step=None, count=False):
+    gg = np.ascontiguousarray(g, F)
+    d = None if draws is None else np.ascontiguousarray(draws, F).reshape(-1)
+    gp = None if grad_per_step is None else np.ascontiguousarray(grad_per_step, F).reshape(-1)
+    check(native().dsim_cyl_run(cyl.h, spins.h, C.byref(params), gg, gp, int(iterations),
+                                int(seed), int(step0), d, 1 if count else 0))

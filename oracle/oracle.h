@@ -76,6 +76,14 @@ uint32_t or3_integrate(const or3_params* p, uint32_t N, float* pos, uint32_t* se
                        float phaseConstant, uint32_t iterations, const float* draws,
                        float* drawsOut, uint32_t* counts);
 
+/* or3_integrate with the spin loop over nthreads OpenMP threads (MWC draws) */
+uint32_t or3_integrate_mt(const or3_params* p, uint32_t N, float* pos, uint32_t* seed,
+                          float* mag, float* phase, uint8_t* comp, uint16_t* fiber,
+                          const float* vertices, const float* helpers,
+                          const uint32_t* triInfo, const uint32_t* cubeCounter,
+                          const uint32_t* trianglesInCubes, float gx, float gy, float gz,
+                          float phaseConstant, uint32_t iterations, int nthreads);
+
 /* FP64 restatement of the same step (precision oracle): same algorithm,
  * doubles throughout, triangle helpers recomputed in double from vertices
  * (double[3V]); draws are the same float stream.  Grid as in the FP32 path. */

@@ -29,7 +29,7 @@ def build(force=False):
             return LIB_PATH
     import subprocess
     cc = os.environ.get("CC", "gcc")
-    cmd = [cc, "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+    cmd = [cc, "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
            "-o", LIB_PATH + ".tmp"] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     os.replace(LIB_PATH + ".tmp", LIB_PATH)
@@ -97,6 +97,10 @@ def _declare(L):
                                 C.c_float, C.c_float, C.c_uint32, _opt(P_F32), _opt(P_F32),
                                 _opt(P_U32)]
     L.or3_integrate.restype = C.c_uint32
+    L.or3_integrate_mt.argtypes = [C.POINTER(Params3), C.c_uint32, P_F32, P_U32, P_F32, P_F32, P_U8,
+                                   P_U16, P_F32, P_F32, P_U32, P_U32, P_U32, C.c_float, C.c_float,
+                                   C.c_float, C.c_float, C.c_uint32, C.c_int]
+    L.or3_integrate_mt.restype = C.c_uint32
     L.or3_integrate_f64.argtypes = [C.POINTER(Params3), C.c_uint32, P_F64, P_F64, P_F64, P_U8,
                                     P_U16, C.c_uint32, P_F64, P_U32, P_U32, P_U32, P_U32, P_F64,
                                     C.c_double, C.c_uint32, P_F32, _opt(P_U32)]

@@ -339,6 +339,29 @@ uint32_t or3_integrate(const or3_params* p, uint32_t N, float* pos, uint32_t* se
     return capped;
 }
 
+/* The same loop with the spin loop of each iteration spread over threads, as
+ * the reference's OpenMP patch does (dSim3/parallelization_cpu.diff:38);
+ * MWC draws only (each spin owns its seeds).  Used to time the CPU path. */
+uint32_t or3_integrate_mt(const or3_params* p, uint32_t N, float* pos, uint32_t* seed,
+                          float* mag, float* phase, uint8_t* comp, uint16_t* fiber,
+                          const float* vertices, const float* helpers,
+                          const uint32_t* triInfo, const uint32_t* cubeCounter,
+                          const uint32_t* trianglesInCubes, float gx, float gy, float gz,
+                          float phaseConstant, uint32_t iterations, int nthreads) {
+    uint32_t capped = 0;
+    for (uint32_t it = 0; it < iterations; it++) {
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads) reduction(+ : capped)
+        for (uint32_t i = 0; i < N; i++) {
+            float d[4];
+            or_myrandn(seed + 2 * (size_t)i, d);
+            capped += step_f32(p, pos + 3 * (size_t)i, mag + i, phase + i, comp + i, fiber + i,
+                               vertices, helpers, triInfo, cubeCounter, trianglesInCubes,
+                               gx, gy, gz, phaseConstant, d, NULL);
+        }
+    }
+    return capped;
+}
+
 uint32_t or3_integrate_f64(const or3_params* p, uint32_t N, double* pos, double* mag,
                            double* phase, uint8_t* comp, uint16_t* fiber,
                            uint32_t nT, const double* vertices, const uint32_t* trgls,

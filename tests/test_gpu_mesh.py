@@ -1,0 +1,162 @@
+"""GPU parity of the triangle-mesh hot path against the CPU oracle.
+
+Replay mode feeds the same step stream to the GPU kernel and to the oracle
+(the C restatement of dSim3's cpuIntegrate, pinned to the reference by the
+golden fixtures): per-spin collision counts, positions, magnitude and phase
+must agree bit for bit, compartments and fibers exactly.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from scenarios import MeshCase, draws
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_run(case, mesh_o, cc, tic, maxtpc, iters, d, perm=None):
+    p = O.params3(case.stdDevs, case.T2, case.permeability if perm is None else perm, case.dt, 50,
+                  maxtpc)
+    pos = case.pos.copy(); seed = np.zeros(2 * case.N, np.uint32)
+    mag = case.mag.copy(); ph = case.phase.copy(); comp = case.comp.copy(); fib = case.fiber.copy()
+    cnt = np.zeros(2 * case.N, np.uint32)
+    capped, _ = O.integrate3(p, pos, seed, mag, ph, comp, fib, mesh_o.vertices, mesh_o.helpers,
+                             mesh_o.triInfo, cc, tic, case.g, case.pc, iters, draws=d, counts=cnt)
+    assert capped == 0
+    return pos, mag, ph, comp, fib, cnt.reshape(-1, 2)
+
+
+@pytest.mark.parametrize("membranes", ["AM", "G"])
+def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
+    from dsim_gb300.engine import Mesh
+    case = MeshCase(tmp_path, membranes=membranes)
+    m = Mesh.load(case.path, case.spaceScale)
+    mo = O.Mesh(case.path, case.spaceScale)
+    v, ti = m.arrays()
+    assert np.array_equal(v.view(np.uint32), mo.vertices.view(np.uint32))
+    assert np.array_equal(ti, mo.triInfo)
+    cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, 50)
+    start, tri = m.grid()
+    counts = np.diff(start.astype(np.int64))
+    assert np.array_equal(counts, cc.astype(np.int64))
+    assert m.max_per_cell == maxtpc
+    dense = tic.reshape(-1, maxtpc)
+    for c in np.nonzero(cc)[0]:
+        assert np.array_equal(tri[start[c]:start[c + 1]], dense[c, :cc[c]])
+
+
+@pytest.mark.parametrize("membranes,perm", [("AM", 0.05), ("G", 0.0), ("G", 0.3)])
+def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm):
+    from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
+    case = MeshCase(tmp_path, membranes=membranes, permeability=perm, N=1500)
+    iters = 60
+    d = draws(iters, case.N, seed=11)
+    mo = O.Mesh(case.path, case.spaceScale)
+    cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, 50)
+    ref = _oracle_run(case, mo, cc, tic, maxtpc, iters, d)
+
+    m = Mesh.load(case.path, case.spaceScale)
+    s = Spins(case.N)
+    s.set(case.pos, case.mag, case.phase, case.comp, case.fiber)
+    p = mesh_params(case.stdDevs, case.T2, case.permeability, case.dt, case.pc)
+    # two launches of 30 steps: state round-trips through HBM between calls
+    mesh_run(m, s, p, g=case.g, iterations=30, draws=d[:30], count=True)
+    mesh_run(m, s, p, g=case.g, iterations=30, draws=d[30:], count=True)
+    pos, mag, ph, comp, fib = s.get()
+    cnt = s.counts()
+    assert s.status() == 0
+    assert cnt.sum() > 0, "scenario produced no collisions"
+    assert np.array_equal(cnt, ref[5]), "collision counts differ"
+    assert np.array_equal(pos.view(np.uint32), ref[0].view(np.uint32))
+    assert np.array_equal(mag.view(np.uint32), ref[1].view(np.uint32))
+    assert np.array_equal(ph.view(np.uint32), ref[2].view(np.uint32))
+    assert np.array_equal(comp, ref[3])
+    assert np.array_equal(fib, ref[4])
+    if perm > 0:
+        assert cnt[:, 1].sum() > 0, "no permeation exercised"
+
+
+def test_mesh_replay_bit_parity_dsim3_abi(engine, tmp_path):
+    """Same replay through the reference-facing C-ABI (libdsim3.so), driven
+    the way SpinSystem drives spinSystem.cuh: allocateArray / copy / bind /
+    copyConstantToDevice by symbol name / integrateSystem."""
+    from dsim_gb300 import _lib
+    L = _lib.abi3()
+    case = MeshCase(tmp_path, membranes="AM", permeability=0.05, N=1200)
+    iters = 40
+    d = draws(iters, case.N, seed=3)
+    mo = O.Mesh(case.path, case.spaceScale)
+    cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, 50)
+    ref = _oracle_run(case, mo, cc, tic, maxtpc, iters, d)
+
+    def dev(arr):
+        p = C.c_void_p()
+        L.allocateArray(C.byref(p), arr.nbytes)
+        L.copyArrayToDevice(p, arr.ctypes.data, 0, arr.nbytes)
+        return p
+
+    dV, dH, dTI = dev(mo.vertices), dev(mo.helpers), dev(mo.triInfo)
+    L.bindVertices(dV, len(mo.vertices))
+    L.bindTriangleHelpers(dH, len(mo.helpers))
+    L.bindTriInfo(dTI, len(mo.triInfo))
+    dTic, dCc = dev(np.ascontiguousarray(tic)), dev(cc)
+    for name, val, ty in (("k_numCubes", 50, np.uint32), ("k_totalNumCubes", 50 ** 3, np.uint32),
+                          ("k_maxTrianglesPerCube", maxtpc, np.uint32),
+                          ("k_cubeLength", np.float32(2.0) / np.float32(50), np.float32),
+                          ("k_reflectionType", 1, np.uint32), ("k_permeability", case.permeability, np.float32),
+                          ("k_deltaTime", case.dt, np.float32)):
+        a = np.array([val], ty)
+        L.copyConstantToDevice(name.encode(), a.ctypes.data, 0, 4)
+    # T2 and sigma tables: the reference passes the address of a device pointer
+    for name, tab in (("k_T2Values", case.T2), ("k_stdDevs", case.stdDevs)):
+        dp = dev(np.ascontiguousarray(tab, np.float32))
+        holder = C.c_void_p(dp.value)
+        L.copyConstantToDevice(name.encode(), C.addressof(holder), 0, 4)
+    spins = np.zeros(case.N, np.dtype([("mag", "<f4"), ("phase", "<f4"), ("comp", "u1"),
+                                        ("pad", "u1"), ("fiber", "<u2")]))
+    spins["mag"], spins["phase"], spins["comp"], spins["fiber"] = case.mag, case.phase, case.comp, case.fiber
+    dPos, dSeed, dSpins = dev(case.pos.copy()), dev(np.zeros(2 * case.N, np.uint32)), dev(spins)
+    dDraws = dev(d.reshape(-1))
+    dCnt = dev(np.zeros(2 * case.N, np.uint32))
+    L.dsim3_set_replay(dDraws, dCnt)
+    g = _lib.Float3(*[float(x) for x in case.g])
+    L.integrateSystem(dPos, dSeed, dSpins, float(case.dt), float(case.permeability), case.N, g,
+                      float(case.pc), iters, dTic, dCc)
+    L.dsim3_set_replay(None, None)
+    assert L.dsim3_last_status() == 0, L.dsim3_last_error()
+    pos = np.zeros_like(case.pos)
+    out = np.zeros_like(spins)
+    cnt = np.zeros(2 * case.N, np.uint32)
+    L.copyArrayFromDevice(pos.ctypes.data, dPos, 0, pos.nbytes)
+    L.copyArrayFromDevice(out.ctypes.data, dSpins, 0, out.nbytes)
+    L.copyArrayFromDevice(cnt.ctypes.data, dCnt, 0, cnt.nbytes)
+    assert L.dsim3_status() == 0
+    assert np.array_equal(cnt.reshape(-1, 2), ref[5])
+    assert np.array_equal(pos.view(np.uint32), ref[0].view(np.uint32))
+    assert np.array_equal(out["mag"].view(np.uint32), ref[1].view(np.uint32))
+    assert np.array_equal(out["phase"].view(np.uint32), ref[2].view(np.uint32))
+    assert np.array_equal(out["comp"], ref[3])
+    assert np.array_equal(out["fiber"], ref[4])
+    for p in (dV, dH, dTI, dTic, dCc, dPos, dSeed, dSpins, dDraws, dCnt):
+        L.freeArray(p)
+
+
+def test_mesh_philox_run_is_deterministic_and_in_box(engine, tmp_path):
+    from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
+    case = MeshCase(tmp_path, membranes="AM", permeability=0.01, N=4096)
+    m = Mesh.load(case.path, case.spaceScale)
+    p = mesh_params(case.stdDevs, case.T2, case.permeability, case.dt, case.pc)
+    outs = []
+    for _ in range(2):
+        s = Spins(case.N)
+        s.set(case.pos, case.mag, case.phase, case.comp, case.fiber)
+        mesh_run(m, s, p, g=case.g, iterations=200, seed=1234, step0=0, count=True)
+        outs.append(s.get())
+        assert s.status() == 0
+        assert s.counts().sum() > 0
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    pos = outs[0][0]
+    assert np.all(np.abs(pos) <= np.float32(0.995))
