@@ -380,7 +380,7 @@ int dsim_spins_create(uint32_t N, dsim_spins** out) {
             (rc = dev_alloc(&s->partials, reduce_scratch_doubles(N), &s->bytes)) ||
             (rc = dev_alloc(&s->sig, 15, &s->bytes)))
             break;
-        if (cudaMemsetAsync(s->counts, 0, (size_t)8 * N + 4, s->st) != cudaSuccess ||
+        if (cudaMemsetAsync(s->counts, 0, (size_t)8 * N, s->st) != cudaSuccess ||
             cudaMemsetAsync(s->status, 0, 4, s->st) != cudaSuccess) { rc = kErrCuda; break; }
     } while (0);
     if (rc == kErrCuda) set_last_error(kErrCuda, "dsim_spins_create: %s", cudaGetErrorString(cudaGetLastError()));
