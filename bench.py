@@ -335,6 +335,7 @@ def run_ours(args, rank, world):
     from dsim_gb300.engine import DeviceInfo, Spins, mesh_run
     dev = DeviceInfo()
     W = Workload(axons=args.axons, spins=args.spins, seed=1 + rank)
+    W.steps_per_launch = args.steps_per_launch
     m = make_mesh(W)
     p = mesh_params_of(W)
     s = Spins(W.N)
@@ -461,6 +462,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--axons", type=int, default=400)
     ap.add_argument("--spins", type=int, default=1 << 20)
+    ap.add_argument("--steps-per-launch", type=int, default=1000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -85,6 +85,9 @@ def _declare_native(L):
         "dsim_mesh_grid": (i32, [VP, OU32, OU32]),
         "dsim_mesh_arrays": (i32, [VP, OF32, OU32]),
         "dsim_mesh_free": (None, [VP]),
+        "dsim_mesh_set_accel": (i32, [VP, u32]),
+        "dsim_mesh_accel_info": (i32, [VP, _nd(np.uint64, flags="C_CONTIGUOUS")]),
+        "dsim_spins_set_sort_interval": (i32, [VP, u32]),
         "dsim_cyl_load": (i32, [C.c_char_p, f32, C.POINTER(VP)]),
         "dsim_cyl_create": (i32, [F32, u32, f32, C.POINTER(VP)]),
         "dsim_cyl_info": (i32, [VP, U32, C.POINTER(f32), OU32, OU32, OF32]),

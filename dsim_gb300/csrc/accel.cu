@@ -1,0 +1,431 @@
+// accel.cu -- the fast mesh path: a fine acceleration grid, spin sorting by
+// cell, and the step kernel that uses them while keeping the reference's
+// collision semantics bit for bit.
+//
+// Semantics (rfdougherty/dSim dSim3/src/spinKernelCpu.cpp:198-395): for one
+// sub-segment the reference visits the cells of its 50^3 grid in the box
+// between the start and end cells (x outer, z inner) and stops at the first
+// cell whose triangle list holds a hit; the result is the nearest hit in that
+// list (lowest index on ties, the last-hit triangle excluded).
+//
+// Here every triangle the sub-segment hits is first collected from a finer
+// grid whose lists hold each triangle in every fine cell its bounding box
+// (widened by kAccelEps) overlaps: a triangle that the float test reports as
+// hit lies within rounding of the segment, so it is always found.  With no
+// hit (the common case) the step is done.  Otherwise the reference's
+// traversal is replayed over the found hits only: a hit counts for a
+// reference cell when the triangle is in that cell's (sorted) list, found by
+// binary search.  The hit tests use the same float expressions as the
+// reference grid path in mesh.cu, so results are identical.
+//
+// Spins are reordered by the Morton code of their fine cell every few steps
+// so that the threads of a warp read the same cell records (broadcast loads)
+// and the records of a block's cells stay in L1.  Each spin keeps a stable id
+// that keys its Philox counter, its replay draws and its counters.
+#include "common.cuh"
+#include "engine.h"
+
+namespace dsim {
+
+__device__ __forceinline__ uint32_t fine_coord(float p, float invLf, uint32_t nf) {
+    float f = floorf((p + 1.0f) * invLf);
+    f = fminf(fmaxf(f, 0.0f), (float)(nf - 1));
+    return (uint32_t)f;
+}
+
+__host__ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    // 10 bits -> every third bit
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+// ---- build --------------------------------------------------------------
+__device__ __forceinline__ void tri_fine_range(const TriPlane& P, const TriBary& B, float invLf,
+                                               uint32_t nf, uint32_t lo[3], uint32_t hi[3]) {
+    float p1[3] = {P.p1x, P.p1y, P.p1z};
+    float u[3] = {B.ux, B.uy, B.uz};
+    float v[3] = {B.vx, B.vy, B.vz};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float a = p1[k], b = p1[k] + v[k], c = p1[k] + u[k];
+        float mn = fminf(a, fminf(b, c)) - kAccelEps;
+        float mx = fmaxf(a, fmaxf(b, c)) + kAccelEps;
+        lo[k] = fine_coord(mn, invLf, nf);
+        hi[k] = fine_coord(mx, invLf, nf);
+    }
+}
+
+template <bool FILL>
+__global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
+                              const TriBary* __restrict__ bary, uint32_t nf, float invLf,
+                              uint32_t* counter, const uint32_t* __restrict__ start, AccelRec* rec) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nT) return;
+    TriPlane P = plane[t];
+    TriBary B = bary[t];
+    uint32_t lo[3], hi[3];
+    tri_fine_range(P, B, invLf, nf, lo, hi);
+    for (uint32_t x = lo[0]; x <= hi[0]; x++)
+        for (uint32_t y = lo[1]; y <= hi[1]; y++)
+            for (uint32_t z = lo[2]; z <= hi[2]; z++) {
+                uint32_t key = morton3(x, y, z);
+                uint32_t slot = atomicAdd(counter + key, 1u);
+                if (FILL) {
+                    AccelRec r;
+                    r.a = make_float4(P.nx, P.ny, P.nz, P.p1x);
+                    r.b = make_float4(P.p1y, P.p1z, P.vv, __uint_as_float(t));
+                    rec[start[key] + slot] = r;
+                }
+            }
+}
+
+int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
+                       uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
+                       cudaStream_t st) {
+    if (nT == 0) return kOk;
+    float invLf = (float)nf / 2.0f;
+    if (fill)
+        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec);
+    else
+        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+// ---- spin sorting (counting sort on a coarse Morton key) -----------------
+__global__ void k_sort_keys(SpinsSorted S, uint32_t nb, float invLb, uint32_t* keys, uint32_t* hist) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    uint32_t key = morton3(fine_coord(S.x[i], invLb, nb), fine_coord(S.y[i], invLb, nb),
+                           fine_coord(S.z[i], invLb, nb));
+    keys[i] = key;
+    atomicAdd(hist + key, 1u);
+}
+
+__global__ void k_sort_scatter(SpinsSorted S, SpinsSorted D, const uint32_t* __restrict__ keys,
+                               const uint32_t* __restrict__ start, uint32_t* cursor) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    uint32_t key = keys[i];
+    uint32_t j = start[key] + atomicAdd(cursor + key, 1u);
+    D.x[j] = S.x[i]; D.y[j] = S.y[i]; D.z[j] = S.z[i];
+    D.mag[j] = S.mag[i]; D.phase[j] = S.phase[i];
+    D.meta[j] = S.meta[i]; D.id[j] = S.id[i];
+}
+
+int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
+                      uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st) {
+    if (S.N == 0) return kOk;
+    uint32_t nkeys = morton3(nb - 1, nb - 1, nb - 1) + 1;
+    DSIM_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)nkeys * 4, st));
+    float invLb = (float)nb / 2.0f;
+    k_sort_keys<<<(S.N + 255) / 256, 256, 0, st>>>(S, nb, invLb, keys, hist);
+    int rc = launch_scan_exclusive(hist, start, nkeys, scratch, st);
+    if (rc) return rc;
+    DSIM_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)nkeys * 4, st));
+    k_sort_scatter<<<(S.N + 255) / 256, 256, 0, st>>>(S, D, keys, start, hist);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+// ---- the step ------------------------------------------------------------
+struct FastHit {
+    uint32_t t;
+    float x, y, z, d2;
+    uint32_t type;
+};
+static constexpr int kMaxHits = 4;
+
+// reference-grid membership of triangle t in cell c: binary search of the
+// ascending list
+__device__ __forceinline__ bool in_ref_cell(const MeshDev& g, uint32_t c, uint32_t t) {
+    uint32_t lo = __ldg(g.cell_start + c), hi = __ldg(g.cell_start + c + 1);
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t v = __ldg(g.cell_tri + mid);
+        if (v == t) return true;
+        if (v < t) lo = mid + 1; else hi = mid;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t ref_coord(float p, float L, uint32_t n) {
+    float f = floorf((p + 1.0f) / L);
+    float hi = (float)(n - 1);
+    float mn = (hi < f) ? hi : f;
+    float mx = (0.0f < mn) ? mn : 0.0f;
+    return (uint32_t)mx;
+}
+
+// full test of one accel record against the sub-segment (same float
+// expressions as triCollDetect); returns true and fills h on a hit
+__device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, float ox, float oy,
+                                         float oz, float dx, float dy, float dz, FastHit& h) {
+    float num = a.x * (a.w - ox) + a.y * (b.x - oy) + a.z * (b.y - oz);
+    float den = a.x * dx + a.y * dy + a.z * dz;
+    if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
+        ((__float_as_uint(num) ^ __float_as_uint(den)) & 0x80000000u))
+        return false;
+    float r = num / den;
+    if (!((0.0f < r) & (r < 1.0f))) return false;
+    uint32_t t = __float_as_uint(b.w);
+    const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
+    float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);
+    float wx = ox + r * dx - a.w;
+    float wy = oy + r * dy - b.x;
+    float wz = oz + r * dz - b.y;
+    float wu = wx * u4.x + wy * u4.y + wz * u4.z;
+    float wv = wx * u4.w + wy * v4.x + wz * v4.y;
+    float uv = v4.z, uu = v4.w, vv = b.z;
+    float s = (uv * wv - vv * wu) / (uv * uv - uu * vv);
+    float tt = (uv * wu - uu * wv) / (uv * uv - uu * vv);
+    if (!((s >= 0.0f) & (tt >= 0.0f) & (s + tt <= 1.0f))) return false;
+    h.t = t;
+    h.x = ox + dx * r; h.y = oy + dy * r; h.z = oz + dz * r;
+    h.d2 = (ox - h.x) * (ox - h.x) + (oy - h.y) * (oy - h.y) + (oz - h.z) * (oz - h.z);
+    uint32_t type = 1;
+    if ((s == 0.0f) | (tt == 0.0f) | (s + tt == 1.0f)) {
+        type = 2;
+        if (((s == 0.0f) & (tt == 0.0f)) | ((s == 0.0f) & (tt == 1.0f)) | ((s == 1.0f) & (tt == 0.0f)))
+            type = 3;
+    }
+    h.type = type;
+    return true;
+}
+
+// the reference grid scan of mesh.cu for one sub-segment (fallback when more
+// distinct triangles are hit than kMaxHits)
+__device__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py, float pz,
+                         uint32_t excluded, FastHit& best, bool& found);
+
+template <bool STATS>
+__global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc, MeshStepArgs a,
+                                                         SpinsSorted S, int rng) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    float x = S.x[i], y = S.y[i], z = S.z[i], mag = S.mag[i], phase = S.phase[i];
+    uint32_t meta = S.meta[i];
+    uint32_t comp = meta & 0xFFu, fiber = meta >> 8;
+    const uint32_t id = S.id[i];
+    uint32_t nrefl = 0, nperm = 0, ntested = 0, status = 0;
+    const float invLf = acc.invLf;
+    const uint32_t nf = acc.nf;
+    for (uint32_t it = 0; it < a.iterations; it++) {
+        Draw d;
+        if (rng == kRngReplay) {
+            float4 q = __ldg(a.draws + (size_t)it * S.N + id);
+            d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
+        } else {
+            d = philox_draw(id, a.step0 + it, a.stream, a.key0, a.key1);
+        }
+        float ox = x, oy = y, oz = z;
+        float sd = a.sd[comp & 3u];
+        float px = x + d.nx * sd, py = y + d.ny * sd, pz = z + d.nz * sd;
+        float ex = px, ey = py, ez = pz;
+        uint32_t excluded = 0xFFFFFFFFu;
+        float umax = 1.0f, umin = 0.0f;
+        if (STATS) {
+            // reference-grid entries in the step segment's cell box
+            uint32_t sx = ref_coord(ox, g.L, g.n), sy = ref_coord(oy, g.L, g.n), sz = ref_coord(oz, g.L, g.n);
+            uint32_t tx = ref_coord(px, g.L, g.n), ty = ref_coord(py, g.L, g.n), tz = ref_coord(pz, g.L, g.n);
+            for (uint32_t cx = min(sx, tx); cx <= max(sx, tx); cx++)
+                for (uint32_t cy = min(sy, ty); cy <= max(sy, ty); cy++)
+                    for (uint32_t cz = min(sz, tz); cz <= max(sz, tz); cz++) {
+                        uint32_t c = g.n * g.n * cz + g.n * cy + cx;
+                        ntested += __ldg(g.cell_start + c + 1) - __ldg(g.cell_start + c);
+                    }
+        }
+        for (uint32_t sub = 0;; sub++) {
+            if (sub >= a.maxSub) { status |= kStatusSubsegCap; ex = ox; ey = oy; ez = oz; break; }
+            float dx = px - ox, dy = py - oy, dz = pz - oz;
+            // 1. every hit triangle, from the fine grid
+            uint32_t lo0 = fine_coord(fminf(ox, px) - kAccelEps, invLf, nf);
+            uint32_t lo1 = fine_coord(fminf(oy, py) - kAccelEps, invLf, nf);
+            uint32_t lo2 = fine_coord(fminf(oz, pz) - kAccelEps, invLf, nf);
+            uint32_t hi0 = fine_coord(fmaxf(ox, px) + kAccelEps, invLf, nf);
+            uint32_t hi1 = fine_coord(fmaxf(oy, py) + kAccelEps, invLf, nf);
+            uint32_t hi2 = fine_coord(fmaxf(oz, pz) + kAccelEps, invLf, nf);
+            FastHit hits[kMaxHits];
+            int nh = 0;
+            bool overflow = false;
+            for (uint32_t cx = lo0; cx <= hi0; cx++)
+                for (uint32_t cy = lo1; cy <= hi1; cy++)
+                    for (uint32_t cz = lo2; cz <= hi2; cz++) {
+                        uint32_t key = morton3(cx, cy, cz);
+                        uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
+                        for (uint32_t k = b0; k < b1; k++) {
+                            const float4* rp = reinterpret_cast<const float4*>(acc.rec + k);
+                            float4 ra = __ldg(rp), rb = __ldg(rp + 1);
+                            if (__float_as_uint(rb.w) == excluded) continue;
+                            FastHit h;
+                            if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) continue;
+                            bool dup = false;
+                            for (int q = 0; q < nh; q++) dup |= (hits[q].t == h.t);
+                            if (dup) continue;
+                            if (nh < kMaxHits) hits[nh++] = h; else overflow = true;
+                        }
+                    }
+            if (nh == 0) break;
+            // 2. the reference's traversal over the hits
+            FastHit best;
+            bool found = false;
+            if (overflow) {
+                ref_scan(g, ox, oy, oz, px, py, pz, excluded, best, found);
+            } else {
+                const uint32_t n = g.n;
+                const float L = g.L;
+                uint32_t sx = ref_coord(ox, L, n), sy = ref_coord(oy, L, n), sz = ref_coord(oz, L, n);
+                uint32_t tx = ref_coord(px, L, n), ty = ref_coord(py, L, n), tz = ref_coord(pz, L, n);
+                uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
+                uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
+                uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
+                uint32_t cx = sx;
+                do {
+                    uint32_t cy = sy;
+                    do {
+                        uint32_t cz = sz;
+                        do {
+                            uint32_t c = n * n * cz + n * cy + cx;
+                            for (int q = 0; q < nh; q++) {
+                                if (!in_ref_cell(g, c, hits[q].t)) continue;
+                                if (!found || hits[q].d2 < best.d2 ||
+                                    (hits[q].d2 == best.d2 && hits[q].t < best.t)) {
+                                    best = hits[q];
+                                    found = true;
+                                }
+                            }
+                            cz += iz;
+                        } while ((cz != tz + iz) && !found);
+                        cy += iy;
+                    } while ((cy != ty + iy) && !found);
+                    cx += ix;
+                } while ((cx != tx + ix) && !found);
+            }
+            if (!found) break;
+            float thr = umax - (umax - umin) * a.perm;
+            if (d.u <= thr) {
+                if ((a.reflType == 0) | (best.type > 1)) {
+                    ex = ox; ey = oy; ez = oz;
+                } else {
+                    const float4 nn = __ldg(reinterpret_cast<const float4*>(g.plane + best.t));
+                    float nx = nn.x, ny = nn.y, nz = nn.z;
+                    float sx2 = px - best.x, sy2 = py - best.y, sz2 = pz - best.z;
+                    ex = (1.0f - 2.0f * nx * nx) * sx2 - 2.0f * nx * ny * sy2 - 2.0f * nx * nz * sz2 + best.x;
+                    ey = -2.0f * nx * ny * sx2 + (1.0f - 2.0f * ny * ny) * sy2 - 2.0f * ny * nz * sz2 + best.y;
+                    ez = -2.0f * nx * nz * sx2 - 2.0f * ny * nz * sy2 + (1.0f - 2.0f * nz * nz) * sz2 + best.z;
+                }
+                umax = thr;
+                nrefl++;
+            } else {
+                umin = thr;
+                nperm++;
+                uint32_t info = __ldg(&g.plane[best.t].info);
+                uint32_t membrane = info & 3u;
+                if (comp == 2) {
+                    if (membrane == 0) comp = 1;
+                    else { comp = 0; fiber = 0xFFFFu; }
+                } else if (comp == 1) {
+                    comp = 2;
+                } else if (comp == 3) {
+                    comp = 0; fiber = 0xFFFFu;
+                } else {
+                    fiber = (info >> 2) & 0xFFFFu;
+                    comp = (membrane == 1) ? 2u : 3u;
+                }
+            }
+            ox = best.x; oy = best.y; oz = best.z;
+            px = ex; py = ey; pz = ez;
+            excluded = best.t;
+        }
+        if (ex > a.clampHi) ex = a.clampHi; else if (ex < a.clampLo) ex = a.clampLo;
+        if (ey > a.clampHi) ey = a.clampHi; else if (ey < a.clampLo) ey = a.clampLo;
+        if (ez > a.clampHi) ez = a.clampHi; else if (ez < a.clampLo) ez = a.clampLo;
+        x = ex; y = ey; z = ez;
+        mag += -mag / a.T2[comp & 3u] * a.dt;
+        float gx = a.gx, gy = a.gy, gz = a.gz;
+        if (a.grad) { float4 G = __ldg(a.grad + it); gx = G.x; gy = G.y; gz = G.z; }
+        phase += (gx * x + gy * y + gz * z) * a.pc;
+    }
+    S.x[i] = x; S.y[i] = y; S.z[i] = z; S.mag[i] = mag; S.phase[i] = phase;
+    S.meta[i] = (comp & 0xFFu) | (fiber << 8);
+    if (a.counts) { a.counts[2 * id] += nrefl; a.counts[2 * id + 1] += nperm; }
+    if (STATS && a.tested) a.tested[id] += ntested;
+    if (status) atomicOr(a.status, status);
+}
+
+// cubeCollDetect over the reference grid (dSim3/src/spinKernelCpu.cpp:311-337)
+__device__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py, float pz,
+                         uint32_t excluded, FastHit& best, bool& found) {
+    const uint32_t n = g.n;
+    const float L = g.L;
+    float dx = px - ox, dy = py - oy, dz = pz - oz;
+    uint32_t sx = ref_coord(ox, L, n), sy = ref_coord(oy, L, n), sz = ref_coord(oz, L, n);
+    uint32_t tx = ref_coord(px, L, n), ty = ref_coord(py, L, n), tz = ref_coord(pz, L, n);
+    uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
+    uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
+    uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
+    found = false;
+    uint32_t cx = sx;
+    do {
+        uint32_t cy = sy;
+        do {
+            uint32_t cz = sz;
+            do {
+                uint32_t c = n * n * cz + n * cy + cx;
+                uint32_t b0 = __ldg(g.cell_start + c), b1 = __ldg(g.cell_start + c + 1);
+                float bd2 = 400000000.0f;
+                for (uint32_t k = b0; k < b1; k++) {
+                    uint32_t t = __ldg(g.cell_tri + k);
+                    if (t == excluded) continue;
+                    const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
+                    float4 ra = __ldg(pp), rc = __ldg(pp + 1);
+                    float4 rb = make_float4(rc.x, rc.y, rc.z, __uint_as_float(t));
+                    FastHit h;
+                    if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) continue;
+                    if (h.d2 < bd2) { bd2 = h.d2; best = h; found = true; }
+                }
+                cz += iz;
+            } while ((cz != tz + iz) && !found);
+            cy += iy;
+        } while ((cy != ty + iy) && !found);
+        cx += ix;
+    } while ((cx != tx + ix) && !found);
+}
+
+int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
+                          const SpinsSorted& S, int rng, cudaStream_t st) {
+    if (S.N == 0 || a.iterations == 0) return kOk;
+    dim3 block(128), grid((S.N + 127) / 128);
+    if (a.tested) k_mesh_step_fast<true><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    else k_mesh_step_fast<false><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+}  // namespace dsim
+
+namespace dsim {
+// slot order back to spin order: D[id[i]] = S[i]
+__global__ void k_unpermute(SpinsSorted S, SpinsSorted D) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    uint32_t j = S.id[i];
+    if (j >= S.N) return;
+    D.x[j] = S.x[i]; D.y[j] = S.y[i]; D.z[j] = S.z[i];
+    D.mag[j] = S.mag[i]; D.phase[j] = S.phase[i]; D.meta[j] = S.meta[i]; D.id[j] = j;
+}
+
+int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st) {
+    if (S.N == 0) return kOk;
+    k_unpermute<<<(S.N + 255) / 256, 256, 0, st>>>(S, D);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+}  // namespace dsim

@@ -63,13 +63,59 @@ struct dsim_mesh {
     TriBary* bary = nullptr;
     uint32_t* cell_start = nullptr;
     uint32_t* cell_tri = nullptr;
+    // fine acceleration grid (nf = 0: none; steps scan the reference grid)
+    uint32_t nf = 0;
+    uint64_t accEntries = 0, accBytes = 0;
+    uint32_t* acc_start = nullptr;
+    AccelRec* acc_rec = nullptr;
     MeshDev dev() const {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
         g.n = n; g.L = L;
         return g;
     }
+    AccelDev acc() const {
+        AccelDev a;
+        a.start = acc_start; a.rec = acc_rec; a.nf = nf; a.invLf = (float)nf / 2.0f;
+        return a;
+    }
 };
+
+// (Re)build the fine acceleration grid with nf cells per axis (0 removes it).
+static int accel_build(dsim_mesh* m, uint32_t nf) {
+    cudaFree(m->acc_start); cudaFree(m->acc_rec);
+    m->acc_start = nullptr; m->acc_rec = nullptr;
+    m->nf = 0; m->accEntries = 0; m->accBytes = 0;
+    if (nf == 0) return kOk;
+    if (nf > 1024) { set_last_error(kErrTooLarge, "accel grid: %u cells per axis > 1024", nf); return kErrTooLarge; }
+    uint32_t nkeys = accel_keys(nf);
+    int rc;
+    uint32_t* counter = nullptr;
+    uint32_t* scratch = nullptr;
+    cudaStream_t st = 0;
+    if ((rc = dev_alloc(&counter, nkeys))) return rc;
+    if ((rc = dev_alloc(&scratch, scan_scratch_words(nkeys)))) { cudaFree(counter); return rc; }
+    do {
+        if ((rc = dev_alloc(&m->acc_start, (size_t)nkeys + 1, &m->accBytes))) break;
+        if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
+        if ((rc = launch_accel_cells(false, m->nT, m->plane, m->bary, nf, counter, nullptr, nullptr, st))) break;
+        if ((rc = launch_scan_exclusive(counter, m->acc_start, nkeys, scratch, st))) break;
+        uint32_t total = 0;
+        if (cudaMemcpyAsync(&total, m->acc_start + nkeys, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
+        m->accEntries = total;
+        if ((rc = dev_alloc(&m->acc_rec, total, &m->accBytes))) break;
+        if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
+        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, st))) break;
+        if (cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
+        m->nf = nf;
+    } while (0);
+    if (rc == kErrCuda) set_last_error(kErrCuda, "accel grid build: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaFree(counter);
+    cudaFree(scratch);
+    if (rc) { cudaFree(m->acc_start); cudaFree(m->acc_rec); m->acc_start = nullptr; m->acc_rec = nullptr; m->nf = 0; }
+    return rc;
+}
 
 struct dsim_cyl {
     CylHost host;
@@ -91,6 +137,14 @@ struct dsim_spins {
     cudaStream_t st = nullptr;
     float *x = nullptr, *y = nullptr, *z = nullptr, *mag = nullptr, *phase = nullptr;
     uint32_t* meta = nullptr;
+    // reordering by cell (fast mesh path): stable ids, second buffer set
+    uint32_t* id = nullptr;
+    float *x2 = nullptr, *y2 = nullptr, *z2 = nullptr, *mag2 = nullptr, *phase2 = nullptr;
+    uint32_t *meta2 = nullptr, *id2 = nullptr, *keys = nullptr, *hist = nullptr, *hstart = nullptr,
+             *hscratch = nullptr;
+    uint32_t sortNb = 0;        // key grid of the allocated sort buffers
+    uint32_t sortEvery = 20;    // steps between reorderings (0 = never)
+    bool permuted = false;      // slot i does not hold spin i
     float4* cpos = nullptr;     // cylinder layout (lazy)
     uint32_t* cseed = nullptr;  // cylinder layout (lazy)
     uint32_t* counts = nullptr;
@@ -112,6 +166,20 @@ struct dsim_spins {
         S.N = N;
         return S;
     }
+    SpinsSorted sorted() const {
+        SpinsSorted S;
+        S.x = x; S.y = y; S.z = z; S.mag = mag; S.phase = phase; S.meta = meta; S.id = id; S.N = N;
+        return S;
+    }
+    SpinsSorted sorted2() const {
+        SpinsSorted S;
+        S.x = x2; S.y = y2; S.z = z2; S.mag = mag2; S.phase = phase2; S.meta = meta2; S.id = id2; S.N = N;
+        return S;
+    }
+    void swap_buffers() {
+        std::swap(x, x2); std::swap(y, y2); std::swap(z, z2); std::swap(mag, mag2);
+        std::swap(phase, phase2); std::swap(meta, meta2); std::swap(id, id2);
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -121,6 +189,7 @@ static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
     cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
+    cudaFree(m->acc_start); cudaFree(m->acc_rec);
     delete m;
 }
 
@@ -186,7 +255,9 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     if (rc == kErrCuda) set_last_error(kErrCuda, "grid build: %s", cudaGetErrorString(cudaGetLastError()));
     cudaFree(counter);
     cudaFree(scratch);
-    return rc;
+    if (rc) return rc;
+    // default fine grid: half the reference cell edge
+    return accel_build(m, 2 * m->n <= 1024 ? 2 * m->n : 1024);
 }
 
 extern "C" {
@@ -251,6 +322,12 @@ int dsim_mesh_create(const float* vertices_um, uint32_t nVertices, const uint32_
     int rc = mesh_build(m, Vn, T, mem, fib);
     if (rc) { mesh_release(m); return rc; }
     *out = m;
+    return kOk;
+}
+
+int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]) {
+    if (!m || !info) return kErrInvalid;
+    info[0] = m->nf; info[1] = m->accEntries; info[2] = m->accBytes;
     return kOk;
 }
 
@@ -358,6 +435,9 @@ static void spins_release(dsim_spins* s) {
     cudaFree(s->meta); cudaFree(s->cpos); cudaFree(s->cseed); cudaFree(s->counts);
     cudaFree(s->status); cudaFree(s->tested); cudaFree(s->draws); cudaFree(s->grad); cudaFree(s->partials);
     cudaFree(s->sig); cudaFree(s->flush);
+    cudaFree(s->id); cudaFree(s->x2); cudaFree(s->y2); cudaFree(s->z2); cudaFree(s->mag2);
+    cudaFree(s->phase2); cudaFree(s->meta2); cudaFree(s->id2); cudaFree(s->keys); cudaFree(s->hist);
+    cudaFree(s->hstart); cudaFree(s->hscratch);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->st) cudaStreamDestroy(s->st);
@@ -378,10 +458,14 @@ int dsim_spins_create(uint32_t N, dsim_spins** out) {
             (rc = dev_alloc(&s->phase, N, &s->bytes)) || (rc = dev_alloc(&s->meta, N, &s->bytes)) ||
             (rc = dev_alloc(&s->counts, (size_t)2 * N, &s->bytes)) || (rc = dev_alloc(&s->status, 1, &s->bytes)) ||
             (rc = dev_alloc(&s->partials, reduce_scratch_doubles(N), &s->bytes)) ||
-            (rc = dev_alloc(&s->sig, 15, &s->bytes)))
+            (rc = dev_alloc(&s->sig, 15, &s->bytes)) || (rc = dev_alloc(&s->id, N, &s->bytes)))
             break;
         if (cudaMemsetAsync(s->counts, 0, (size_t)8 * N, s->st) != cudaSuccess ||
             cudaMemsetAsync(s->status, 0, 4, s->st) != cudaSuccess) { rc = kErrCuda; break; }
+        std::vector<uint32_t> iota(N);
+        for (uint32_t i = 0; i < N; i++) iota[i] = i;
+        if (cudaMemcpyAsync(s->id, iota.data(), (size_t)4 * N, cudaMemcpyHostToDevice, s->st) != cudaSuccess ||
+            cudaStreamSynchronize(s->st) != cudaSuccess) { rc = kErrCuda; break; }
     } while (0);
     if (rc == kErrCuda) set_last_error(kErrCuda, "dsim_spins_create: %s", cudaGetErrorString(cudaGetLastError()));
     if (rc) { spins_release(s); return rc; }
@@ -392,10 +476,52 @@ int dsim_spins_create(uint32_t N, dsim_spins** out) {
 uint32_t dsim_spins_count(const dsim_spins* s) { return s ? s->N : 0; }
 uint64_t dsim_spins_bytes(const dsim_spins* s) { return s ? s->bytes : 0; }
 
+static int spins_identity(dsim_spins* s) {
+    std::vector<uint32_t> iota(s->N);
+    for (uint32_t i = 0; i < s->N; i++) iota[i] = i;
+    DSIM_CUDA_TRY(cudaMemcpyAsync(s->id, iota.data(), (size_t)4 * s->N, cudaMemcpyHostToDevice, s->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(s->st));
+    s->permuted = false;
+    return kOk;
+}
+
+// bring slot order back to spin order (slot i holds spin i)
+static int spins_unpermute(dsim_spins* s) {
+    if (!s->permuted) return kOk;
+    int rc = launch_unpermute(s->sorted(), s->sorted2(), s->st);
+    if (rc) return rc;
+    s->swap_buffers();
+    s->permuted = false;
+    return kOk;
+}
+
+static int ensure_sort_buffers(dsim_spins* s, uint32_t nb) {
+    int rc;
+    if (!s->x2) {
+        if ((rc = dev_alloc(&s->x2, s->N, &s->bytes)) || (rc = dev_alloc(&s->y2, s->N, &s->bytes)) ||
+            (rc = dev_alloc(&s->z2, s->N, &s->bytes)) || (rc = dev_alloc(&s->mag2, s->N, &s->bytes)) ||
+            (rc = dev_alloc(&s->phase2, s->N, &s->bytes)) || (rc = dev_alloc(&s->meta2, s->N, &s->bytes)) ||
+            (rc = dev_alloc(&s->id2, s->N, &s->bytes)) || (rc = dev_alloc(&s->keys, s->N, &s->bytes)))
+            return rc;
+    }
+    if (s->sortNb != nb) {
+        cudaFree(s->hist); cudaFree(s->hstart); cudaFree(s->hscratch);
+        s->hist = s->hstart = s->hscratch = nullptr;
+        uint32_t nkeys = accel_keys(nb);
+        if ((rc = dev_alloc(&s->hist, nkeys, &s->bytes)) || (rc = dev_alloc(&s->hstart, (size_t)nkeys + 1, &s->bytes)) ||
+            (rc = dev_alloc(&s->hscratch, scan_scratch_words(nkeys), &s->bytes)))
+            return rc;
+        s->sortNb = nb;
+    }
+    return kOk;
+}
+
 int dsim_spins_set(dsim_spins* s, const float* pos3, const float* mag, const float* phase,
                    const uint8_t* comp, const uint16_t* fiber) {
     if (!s) return kErrInvalid;
     uint32_t N = s->N;
+    int rc0 = spins_unpermute(s);
+    if (rc0) return rc0;
     std::vector<float> a(N), b(N), c(N);
     if (pos3) {
         for (uint32_t i = 0; i < N; i++) { a[i] = pos3[3 * i]; b[i] = pos3[3 * i + 1]; c[i] = pos3[3 * i + 2]; }
@@ -421,6 +547,8 @@ int dsim_spins_get(dsim_spins* s, float* pos3, float* mag, float* phase, uint8_t
                    uint16_t* fiber) {
     if (!s) return kErrInvalid;
     uint32_t N = s->N;
+    int rc0 = spins_unpermute(s);
+    if (rc0) return rc0;
     if (pos3) {
         std::vector<float> a(N), b(N), c(N);
         DSIM_CUDA_TRY(cudaMemcpyAsync(a.data(), s->x, N * 4, cudaMemcpyDeviceToHost, s->st));
@@ -594,7 +722,46 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
     }
     int rc = upload_grad_draws(s, gradPerStep, replayDraws, iterations, &a.grad, &a.draws);
     if (rc) return rc;
-    return launch_mesh_step(m->dev(), a, s->dev(), kLayoutSoA, replayDraws ? kRngReplay : kRngPhilox, s->st);
+    int rng = replayDraws ? kRngReplay : kRngPhilox;
+    if (m->nf == 0) {
+        // reference-grid scan: slot order = spin order
+        if ((rc = spins_unpermute(s))) return rc;
+        if (a.tested) { set_last_error(kErrInvalid, "entry counting needs the fine grid"); return kErrInvalid; }
+        return launch_mesh_step(m->dev(), a, s->dev(), kLayoutSoA, rng, s->st);
+    }
+    // fast path: reorder by fine cell every sortEvery steps
+    uint32_t chunk = s->sortEvery ? s->sortEvery : iterations;
+    if (s->sortEvery && (rc = ensure_sort_buffers(s, m->nf))) return rc;
+    const float4* grad0 = a.grad;
+    const float4* draws0 = a.draws;
+    for (uint32_t done = 0; done < iterations; done += chunk) {
+        uint32_t n = iterations - done < chunk ? iterations - done : chunk;
+        if (s->sortEvery) {
+            if ((rc = launch_sort_spins(s->sorted(), s->sorted2(), s->sortNb, s->keys, s->hist,
+                                        s->hstart, s->hscratch, s->st)))
+                return rc;
+            s->swap_buffers();
+            s->permuted = true;
+        }
+        MeshStepArgs b = a;
+        b.iterations = n;
+        b.step0 = a.step0 + done;
+        b.grad = grad0 ? grad0 + done : nullptr;
+        b.draws = draws0 ? draws0 + (size_t)done * s->N : nullptr;
+        if ((rc = launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st))) return rc;
+    }
+    return kOk;
+}
+
+int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis) {
+    if (!m) return kErrInvalid;
+    return accel_build(m, cellsPerAxis);
+}
+
+int dsim_spins_set_sort_interval(dsim_spins* s, uint32_t steps) {
+    if (!s) return kErrInvalid;
+    s->sortEvery = steps;
+    return kOk;
 }
 
 int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const float g[3],

@@ -52,6 +52,40 @@ struct MeshStepArgs {
     uint32_t* tested;     // [N] grid entries scanned (or null)
 };
 
+// ---- accel.cu -------------------------------------------------------------
+// Fine acceleration grid: every triangle is listed in each fine cell its
+// bounding box (widened by kAccelEps) overlaps; cells are stored in Morton
+// order; one 32-byte record per entry {n.x, n.y, n.z, p1.x}, {p1.y, p1.z, vv, t}.
+static constexpr float kAccelEps = 1e-5f;
+struct __align__(16) AccelRec {
+    float4 a, b;
+};
+struct AccelDev {
+    const uint32_t* start;  // Morton key -> first record (keys + 1 entries)
+    const AccelRec* rec;
+    uint32_t nf;            // fine cells per axis
+    float invLf;            // nf / 2
+};
+// spin state reordered by cell; id = the spin's stable index
+struct SpinsSorted {
+    float *x, *y, *z, *mag, *phase;
+    uint32_t *meta, *id;
+    uint32_t N;
+};
+__host__ __device__ inline uint32_t accel_keys(uint32_t nf) {
+    uint32_t v = nf - 1, s = 0;
+    for (uint32_t b = 0; b < 10; b++) s |= ((v >> b) & 1u) << (3 * b);
+    return (s | (s << 1) | (s << 2)) + 1;
+}
+int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
+                       uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
+                       cudaStream_t st);
+int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
+                      uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st);
+int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
+                          const SpinsSorted& S, int rng, cudaStream_t st);
+int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st);
+
 // ---- mesh.cu --------------------------------------------------------------
 int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
                              const uint32_t* membrane, const uint32_t* fiber, TriPlane* plane,

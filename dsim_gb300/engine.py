@@ -99,6 +99,9 @@ class Spins:
         check(native().dsim_spins_counts(self.h, out, 1 if reset else 0))
         return out.reshape(-1, 2)
 
+    def set_sort_interval(self, steps):
+        check(native().dsim_spins_set_sort_interval(self.h, int(steps)))
+
     def scanned(self, reset=False):
         out = np.zeros(self.N, np.uint32)
         check(native().dsim_spins_scanned(self.h, out, 1 if reset else 0))
@@ -169,6 +172,14 @@ class Mesh:
         check(native().dsim_mesh_create(v, len(v) // 3, t, m, f, len(t) // 3, float(spaceScale),
                                         int(numCubes), C.byref(h)))
         return cls(h)
+
+    def set_accel(self, cells_per_axis):
+        check(native().dsim_mesh_set_accel(self.h, int(cells_per_axis)))
+
+    def accel_info(self):
+        info = np.zeros(3, np.uint64)
+        check(native().dsim_mesh_accel_info(self.h, info))
+        return dict(cells=int(info[0]), entries=int(info[1]), nbytes=int(info[2]))
 
     def grid(self):
         n3 = self.numCubes ** 3

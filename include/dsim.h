@@ -60,6 +60,14 @@ int dsim_mesh_create(const float* vertices_um, uint32_t nVertices, const uint32_
 /* info[0..7] = nVertices, nTriangles, nFibers, numCubes, grid entries,
  *              max entries in one cell, device bytes, nonempty cells */
 int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
+/* The step kernels find candidate triangles in a finer acceleration grid
+ * (each triangle listed in every fine cell its bounding box overlaps) and
+ * apply the reference grid's first-cell-with-hit rule only to the hits, which
+ * gives the same results.  Built with 2 * numCubes cells per axis by default;
+ * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
+ * info = {cells per axis, entries, device bytes}. */
+int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
+int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]);
 /* copies the CSR grid: cellStart[numCubes^3 + 1], cellTri[entries] */
 int dsim_mesh_grid(const dsim_mesh* m, uint32_t* cellStart, uint32_t* cellTri);
 /* copies normalised vertices[3V] and triInfo[3T] = {fiber, membrane, first vertex} */
@@ -98,6 +106,10 @@ int dsim_spins_counts(dsim_spins* s, uint32_t* counts2N, int reset);
  * accumulated by dsim_mesh_run when countCollisions has bit 2 set */
 int dsim_spins_scanned(dsim_spins* s, uint32_t* scannedN, int reset);
 int dsim_spins_status(dsim_spins* s, uint32_t* status, int reset);
+/* Spins are reordered by fine-grid cell every `steps` steps of a mesh run
+ * (default 20; 0 = never) so that neighbouring threads read the same cell
+ * records.  Each spin keeps its identity (random stream, counters, getters). */
+int dsim_spins_set_sort_interval(dsim_spins* s, uint32_t steps);
 /* bytes of device memory held by the object */
 uint64_t dsim_spins_bytes(const dsim_spins* s);
 void dsim_spins_free(dsim_spins* s);

@@ -47,8 +47,13 @@ def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
         assert np.array_equal(tri[start[c]:start[c + 1]], dense[c, :cc[c]])
 
 
-@pytest.mark.parametrize("membranes,perm", [("AM", 0.05), ("G", 0.0), ("G", 0.3)])
-def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm):
+@pytest.mark.parametrize("membranes,perm,accel,sort", [
+    ("AM", 0.05, None, 20), ("G", 0.0, None, 20), ("G", 0.3, None, 7),
+    ("AM", 0.05, 0, 0), ("AM", 0.05, 37, 7), ("AM", 0.05, 300, 0), ("G", 0.3, 13, 1)])
+def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort):
+    """accel None: default fine grid; 0: reference-grid scan; other: fine
+    cells per axis (coarser and finer than the reference grid).  sort: steps
+    between spin reorderings (0 = never)."""
     from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
     case = MeshCase(tmp_path, membranes=membranes, permeability=perm, N=1500)
     iters = 60
@@ -58,7 +63,10 @@ def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm):
     ref = _oracle_run(case, mo, cc, tic, maxtpc, iters, d)
 
     m = Mesh.load(case.path, case.spaceScale)
+    if accel is not None:
+        m.set_accel(accel)
     s = Spins(case.N)
+    s.set_sort_interval(sort)
     s.set(case.pos, case.mag, case.phase, case.comp, case.fiber)
     p = mesh_params(case.stdDevs, case.T2, case.permeability, case.dt, case.pc)
     # two launches of 30 steps: state round-trips through HBM between calls
