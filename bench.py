@@ -337,8 +337,14 @@ def run_ours(args, rank, world):
     W = Workload(axons=args.axons, spins=args.spins, seed=1 + rank)
     W.steps_per_launch = args.steps_per_launch
     m = make_mesh(W)
+    if args.accel >= 0:
+        m.set_accel(args.accel)
+    acc_info = m.accel_info()
+    log("accel grid: %s" % acc_info)
     p = mesh_params_of(W)
     s = Spins(W.N)
+    if args.sort_every >= 0:
+        s.set_sort_interval(args.sort_every)
     it = W.steps_per_launch
 
     def reset():
@@ -395,7 +401,8 @@ def run_ours(args, rank, world):
                                % (W.axons, len(W.tube["trgls"]), W.N),
                    "spins": W.N, "triangles": int(len(W.tube["trgls"])), "steps_per_launch": it,
                    "form": "plain", "rng": "philox4x32-10", "l2": "flushed between launches (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "accel_cells_per_axis": acc_info["cells"], "sort_every": args.sort_every},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "peak_kind": kind,
                      "bytes_per_spin_step": B_step, "T_bar": Tbar,
@@ -463,6 +470,8 @@ def main():
     ap.add_argument("--axons", type=int, default=400)
     ap.add_argument("--spins", type=int, default=1 << 20)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
+    ap.add_argument("--accel", type=int, default=-1, help="fine grid cells per axis (-1 default, 0 reference grid)")
+    ap.add_argument("--sort-every", type=int, default=-1, help="steps between spin reorderings (-1 default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
