@@ -27,7 +27,7 @@ UNITS = ["mesh.cu", "accel.cu", "cyl.cu", "scan.cu", "reduce.cu", "api.cu", "com
          "host_formats.cpp"]
 LIBS = {
     "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "cyl", "scan", "reduce"],
-    "libdsim3.so": ["compat3", "mesh", "scan"],
+    "libdsim3.so": ["compat3", "mesh", "accel", "scan"],
     "libdsim2.so": ["compat2", "cyl"],
 }
 

@@ -215,6 +215,8 @@ __global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc,
     uint32_t comp = meta & 0xFFu, fiber = meta >> 8;
     const uint32_t id = S.id[i];
     uint32_t nrefl = 0, nperm = 0, ntested = 0, status = 0;
+    uint32_t k0 = a.key0, k1 = a.key1;
+    if (rng == kRngPhiloxPerSpinKey) { k0 = a.spinKeys[2 * id]; k1 = a.spinKeys[2 * id + 1]; }
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
     for (uint32_t it = 0; it < a.iterations; it++) {
@@ -223,7 +225,7 @@ __global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc,
             float4 q = __ldg(a.draws + (size_t)it * S.N + id);
             d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
         } else {
-            d = philox_draw(id, a.step0 + it, a.stream, a.key0, a.key1);
+            d = philox_draw(id, a.step0 + it, a.stream, k0, k1);
         }
         float ox = x, oy = y, oz = z;
         float sd = a.sd[comp & 3u];
@@ -425,6 +427,58 @@ __global__ void k_unpermute(SpinsSorted S, SpinsSorted D) {
 int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st) {
     if (S.N == 0) return kOk;
     k_unpermute<<<(S.N + 255) / 256, 256, 0, st>>>(S, D);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+}  // namespace dsim
+
+namespace dsim {
+// the reference's AoS arrays (float3 positions, 12-byte spinData) -> SoA
+// work buffers in spin order (id = index)
+__global__ void k_aos_to_soa(const float* __restrict__ pos, const unsigned char* __restrict__ spin,
+                             SpinsSorted D) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= D.N) return;
+    D.x[i] = pos[3 * i]; D.y[i] = pos[3 * i + 1]; D.z[i] = pos[3 * i + 2];
+    const unsigned char* rec = spin + 12 * (size_t)i;
+    D.mag[i] = *reinterpret_cast<const float*>(rec);
+    D.phase[i] = *reinterpret_cast<const float*>(rec + 4);
+    D.meta[i] = (uint32_t)rec[8] | ((uint32_t)(*reinterpret_cast<const uint16_t*>(rec + 10)) << 8);
+    D.id[i] = i;
+}
+
+// SoA work buffers (any slot order) -> the reference's AoS arrays by id; with
+// spinKeys, each spin's key is advanced for the next call
+__global__ void k_soa_to_aos(SpinsSorted S, float* pos, unsigned char* spin, uint32_t* spinKeys,
+                             uint32_t iterations) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    uint32_t j = S.id[i];
+    if (j >= S.N) return;
+    pos[3 * j] = S.x[i]; pos[3 * j + 1] = S.y[i]; pos[3 * j + 2] = S.z[i];
+    unsigned char* rec = spin + 12 * (size_t)j;
+    *reinterpret_cast<float*>(rec) = S.mag[i];
+    *reinterpret_cast<float*>(rec + 4) = S.phase[i];
+    rec[8] = (unsigned char)(S.meta[i] & 0xFFu);
+    *reinterpret_cast<uint16_t*>(rec + 10) = (uint16_t)(S.meta[i] >> 8);
+    if (spinKeys) {
+        uint32_t k0 = spinKeys[2 * j], k1 = spinKeys[2 * j + 1];
+        u32x4 nk = philox4x32_10({j, iterations, 0xFFFFFFFFu, 0x5EEDu}, k0, k1);
+        spinKeys[2 * j] = nk.x; spinKeys[2 * j + 1] = nk.y;
+    }
+}
+
+int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st) {
+    if (D.N == 0) return kOk;
+    k_aos_to_soa<<<(D.N + 255) / 256, 256, 0, st>>>(pos, (const unsigned char*)spin, D);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
+                      uint32_t iterations, cudaStream_t st) {
+    if (S.N == 0) return kOk;
+    k_soa_to_aos<<<(S.N + 255) / 256, 256, 0, st>>>(S, pos, (unsigned char*)spin, spinKeys, iterations);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

@@ -256,8 +256,8 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     cudaFree(counter);
     cudaFree(scratch);
     if (rc) return rc;
-    // default fine grid: half the reference cell edge
-    return accel_build(m, 2 * m->n <= 1024 ? 2 * m->n : 1024);
+    // default fine grid: a third of the reference cell edge
+    return accel_build(m, 3 * m->n <= 1024 ? 3 * m->n : 1024);
 }
 
 extern "C" {

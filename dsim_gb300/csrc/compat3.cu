@@ -72,10 +72,30 @@ struct State {
     uint32_t* cell_tri = nullptr;
     uint32_t* status = nullptr;
     uint32_t statusHost = 0;
+    // fine acceleration grid (cells per axis = accelFactor x k_numCubes)
+    uint32_t nf = 0;
+    uint32_t* acc_start = nullptr;
+    AccelRec* acc_rec = nullptr;
+    // spin work buffers for the reordered fast path (grow with N)
+    uint32_t cap = 0;
+    float* w[10] = {nullptr};       // x, y, z, mag, phase  (two sets)
+    uint32_t* wu[4] = {nullptr};    // meta, id (two sets)
+    uint32_t* keys = nullptr;
+    uint32_t *hist = nullptr, *hstart = nullptr, *hscratch = nullptr;
+    uint32_t histNf = 0;
+    uint32_t sortEvery = 20;
     void release() {
         cudaFree(plane); cudaFree(bary); cudaFree(cell_start); cudaFree(cell_tri);
+        cudaFree(acc_start); cudaFree(acc_rec);
         plane = nullptr; bary = nullptr; cell_start = nullptr; cell_tri = nullptr;
+        acc_start = nullptr; acc_rec = nullptr; nf = 0;
         have = false;
+    }
+    SpinsSorted set(int k, uint32_t N) const {
+        SpinsSorted S;
+        S.x = w[5 * k]; S.y = w[5 * k + 1]; S.z = w[5 * k + 2]; S.mag = w[5 * k + 3];
+        S.phase = w[5 * k + 4]; S.meta = wu[2 * k]; S.id = wu[2 * k + 1]; S.N = N;
+        return S;
     }
 };
 State& S() {
@@ -128,8 +148,51 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
         set_last_error(kErrFormat, "integrateSystem: trianglesInCubes names a triangle >= %u or a cell above k_maxTrianglesPerCube", nT);
         return kErrFormat;
     }
+    // fine acceleration grid from the records (triangle corners p1, p1 + v, p1 + u)
+    uint32_t nf = s.numCubes * 3 <= 1024 ? s.numCubes * 3 : 1024;
+    uint32_t nkeys = accel_keys(nf);
+    uint32_t* counter = nullptr;
+    uint32_t* scr = nullptr;
+    DSIM_CUDA_TRY(cudaMalloc(&counter, (size_t)nkeys * 4));
+    DSIM_CUDA_TRY(cudaMalloc(&scr, scan_scratch_words(nkeys) * 4));
+    DSIM_CUDA_TRY(cudaMalloc(&s.acc_start, ((size_t)nkeys + 1) * 4));
+    DSIM_CUDA_TRY(cudaMemset(counter, 0, (size_t)nkeys * 4));
+    rc = launch_accel_cells(false, nT, s.plane, s.bary, nf, counter, nullptr, nullptr, 0);
+    if (!rc) rc = launch_scan_exclusive(counter, s.acc_start, nkeys, scr, 0);
+    uint32_t accTotal = 0;
+    if (!rc && cudaMemcpy(&accTotal, s.acc_start + nkeys, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
+    if (!rc && cudaMalloc(&s.acc_rec, (size_t)(accTotal ? accTotal : 1) * sizeof(AccelRec)) != cudaSuccess) rc = kErrNoMem;
+    if (!rc && cudaMemset(counter, 0, (size_t)nkeys * 4) != cudaSuccess) rc = kErrCuda;
+    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, 0);
+    cudaFree(counter);
+    cudaFree(scr);
+    if (rc) { set_last_error(rc, "integrateSystem: building the fine grid failed"); return rc; }
+    s.nf = nf;
     s.key = k;
     s.have = true;
+    return kOk;
+}
+
+int ensure_work(State& s, uint32_t N) {
+    if (s.cap < N) {
+        for (auto& p : s.w) { cudaFree(p); p = nullptr; }
+        for (auto& p : s.wu) { cudaFree(p); p = nullptr; }
+        cudaFree(s.keys); s.keys = nullptr;
+        s.cap = 0;
+        for (auto& p : s.w) DSIM_CUDA_TRY(cudaMalloc(&p, (size_t)N * 4));
+        for (auto& p : s.wu) DSIM_CUDA_TRY(cudaMalloc(&p, (size_t)N * 4));
+        DSIM_CUDA_TRY(cudaMalloc(&s.keys, (size_t)N * 4));
+        s.cap = N;
+    }
+    if (s.histNf != s.nf) {
+        cudaFree(s.hist); cudaFree(s.hstart); cudaFree(s.hscratch);
+        s.hist = s.hstart = s.hscratch = nullptr;
+        uint32_t nkeys = accel_keys(s.nf);
+        DSIM_CUDA_TRY(cudaMalloc(&s.hist, (size_t)nkeys * 4));
+        DSIM_CUDA_TRY(cudaMalloc(&s.hstart, ((size_t)nkeys + 1) * 4));
+        DSIM_CUDA_TRY(cudaMalloc(&s.hscratch, scan_scratch_words(nkeys) * 4));
+        s.histNf = s.nf;
+    }
     return kOk;
 }
 
@@ -264,13 +327,32 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
     a.status = s.status;
     a.counts = s.counts;
     a.draws = s.replay;
-    SpinsDev sp;
-    memset(&sp, 0, sizeof(sp));
-    sp.x = pos;
-    sp.meta = reinterpret_cast<uint32_t*>(spinInfo);
-    sp.seed = randSeed;
-    sp.N = (uint32_t)numBodies;
-    rc = launch_mesh_step(g, a, sp, kLayoutAoS, s.replay ? kRngReplay : kRngPhiloxPerSpinKey, 0);
+    const uint32_t N = (uint32_t)numBodies;
+    if ((rc = ensure_work(s, N))) { fail(rc); return; }
+    // the reference's arrays -> SoA work buffers; steps in chunks with the
+    // spins reordered by fine cell before each chunk; back to the arrays
+    int cur = 0;
+    if ((rc = launch_aos_to_soa(pos, spinInfo, s.set(cur, N), 0))) { fail(rc); return; }
+    AccelDev acc;
+    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.nf = s.nf; acc.invLf = (float)s.nf / 2.0f;
+    a.spinKeys = randSeed;
+    int rng = s.replay ? kRngReplay : kRngPhiloxPerSpinKey;
+    uint32_t chunk = s.sortEvery ? s.sortEvery : iterations;
+    for (uint32_t done = 0; done < iterations; done += chunk) {
+        uint32_t n = iterations - done < chunk ? iterations - done : chunk;
+        if (s.sortEvery) {
+            rc = launch_sort_spins(s.set(cur, N), s.set(1 - cur, N), s.nf, s.keys, s.hist, s.hstart,
+                                   s.hscratch, 0);
+            if (rc) { fail(rc); return; }
+            cur = 1 - cur;
+        }
+        MeshStepArgs b = a;
+        b.iterations = n;
+        b.step0 = done;
+        b.draws = s.replay ? s.replay + (size_t)done * N : nullptr;
+        if ((rc = launch_mesh_step_fast(g, acc, b, s.set(cur, N), rng, 0))) { fail(rc); return; }
+    }
+    rc = launch_soa_to_aos(s.set(cur, N), pos, spinInfo, s.replay ? nullptr : randSeed, iterations, 0);
     if (rc) fail(rc);
 }
 

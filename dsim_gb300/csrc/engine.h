@@ -50,6 +50,7 @@ struct MeshStepArgs {
     uint32_t* status;     // device status word (StatusBits)
     uint32_t* counts;     // [2N] reflections, permeations (or null)
     uint32_t* tested;     // [N] grid entries scanned (or null)
+    const uint32_t* spinKeys;  // per-spin Philox keys [2N] by id (kRngPhiloxPerSpinKey, fast path)
 };
 
 // ---- accel.cu -------------------------------------------------------------
@@ -85,6 +86,9 @@ int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, u
 int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
                           const SpinsSorted& S, int rng, cudaStream_t st);
 int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st);
+int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st);
+int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
+                      uint32_t iterations, cudaStream_t st);
 
 // ---- mesh.cu --------------------------------------------------------------
 int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
