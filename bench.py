@@ -337,6 +337,8 @@ def run_ours(args, rank, world):
     W = Workload(axons=args.axons, spins=args.spins, seed=1 + rank)
     W.steps_per_launch = args.steps_per_launch
     m = make_mesh(W)
+    if args.kernel > 0:
+        m.set_kernel(args.kernel)
     if args.accel >= 0:
         m.set_accel(args.accel)
     acc_info = m.accel_info()
@@ -472,6 +474,7 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=1000)
     ap.add_argument("--accel", type=int, default=-1, help="fine grid cells per axis (-1 default, 0 reference grid)")
     ap.add_argument("--sort-every", type=int, default=-1, help="steps between spin reorderings (-1 default)")
+    ap.add_argument("--kernel", type=int, default=0, help="step kernel variant (0 default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

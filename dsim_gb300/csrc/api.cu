@@ -65,6 +65,7 @@ struct dsim_mesh {
     uint32_t* cell_tri = nullptr;
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
+    uint32_t kernel = 2;  // 1 per-thread candidate lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM)
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
@@ -748,8 +749,17 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
         b.step0 = a.step0 + done;
         b.grad = grad0 ? grad0 + done : nullptr;
         b.draws = draws0 ? draws0 + (size_t)done * s->N : nullptr;
-        if ((rc = launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st))) return rc;
+        rc = m->kernel == 1 ? launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st)
+                            : launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
+                                                    m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
+        if (rc) return rc;
     }
+    return kOk;
+}
+
+int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant) {
+    if (!m || variant < 1 || variant > 4) { set_last_error(kErrInvalid, "kernel variant must be 1..4"); return kErrInvalid; }
+    m->kernel = variant;
     return kOk;
 }
 

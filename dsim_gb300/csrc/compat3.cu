@@ -350,7 +350,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
         b.iterations = n;
         b.step0 = done;
         b.draws = s.replay ? s.replay + (size_t)done * N : nullptr;
-        if ((rc = launch_mesh_step_fast(g, acc, b, s.set(cur, N), rng, 0))) { fail(rc); return; }
+        if ((rc = launch_mesh_step_coop(g, acc, b, s.set(cur, N), rng, 0))) { fail(rc); return; }
     }
     rc = launch_soa_to_aos(s.set(cur, N), pos, spinInfo, s.replay ? nullptr : randSeed, iterations, 0);
     if (rc) fail(rc);

@@ -86,6 +86,11 @@ int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, u
 int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
                           const SpinsSorted& S, int rng, cudaStream_t st);
 int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st);
+// coop.cu: warp-cooperative variant of the fast step (same results)
+// occupancy: minimum resident blocks of 128 threads per SM the kernel is
+// compiled for (4, 6 or 8: register budget 128, 85 or 64)
+int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
+                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 6);
 int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st);
 int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
                       uint32_t iterations, cudaStream_t st);

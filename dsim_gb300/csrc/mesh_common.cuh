@@ -1,0 +1,136 @@
+// mesh_common.cuh -- device helpers shared by the fast mesh step kernels
+// (accel.cu, coop.cu): fine-grid coordinates and Morton keys, the exact
+// triangle test on a fine-grid record, membership in a reference-grid cell,
+// and the reference grid scan used as the exact fallback.
+#pragma once
+#include "common.cuh"
+#include "engine.h"
+
+namespace dsim {
+
+__device__ __forceinline__ uint32_t fine_coord(float p, float invLf, uint32_t nf) {
+    float f = floorf((p + 1.0f) * invLf);
+    f = fminf(fmaxf(f, 0.0f), (float)(nf - 1));
+    return (uint32_t)f;
+}
+
+__host__ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    // 10 bits -> every third bit
+    v &= 0x3FFu;
+    v = (v | (v << 16)) & 0x030000FFu;
+    v = (v | (v << 8)) & 0x0300F00Fu;
+    v = (v | (v << 4)) & 0x030C30C3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+// ---- the step ------------------------------------------------------------
+struct FastHit {
+    uint32_t t;
+    float x, y, z, d2;
+    uint32_t type;
+};
+static constexpr int kMaxHits = 4;
+
+// reference-grid membership of triangle t in cell c: binary search of the
+// ascending list
+__device__ __forceinline__ bool in_ref_cell(const MeshDev& g, uint32_t c, uint32_t t) {
+    uint32_t lo = __ldg(g.cell_start + c), hi = __ldg(g.cell_start + c + 1);
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        uint32_t v = __ldg(g.cell_tri + mid);
+        if (v == t) return true;
+        if (v < t) lo = mid + 1; else hi = mid;
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t ref_coord(float p, float L, uint32_t n) {
+    float f = floorf((p + 1.0f) / L);
+    float hi = (float)(n - 1);
+    float mn = (hi < f) ? hi : f;
+    float mx = (0.0f < mn) ? mn : 0.0f;
+    return (uint32_t)mx;
+}
+
+// full test of one accel record against the sub-segment (same float
+// expressions as triCollDetect); returns true and fills h on a hit
+__device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, float ox, float oy,
+                                         float oz, float dx, float dy, float dz, FastHit& h) {
+    float num = a.x * (a.w - ox) + a.y * (b.x - oy) + a.z * (b.y - oz);
+    float den = a.x * dx + a.y * dy + a.z * dz;
+    if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
+        ((__float_as_uint(num) ^ __float_as_uint(den)) & 0x80000000u))
+        return false;
+    float r = num / den;
+    if (!((0.0f < r) & (r < 1.0f))) return false;
+    uint32_t t = __float_as_uint(b.w);
+    const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
+    float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);
+    float wx = ox + r * dx - a.w;
+    float wy = oy + r * dy - b.x;
+    float wz = oz + r * dz - b.y;
+    float wu = wx * u4.x + wy * u4.y + wz * u4.z;
+    float wv = wx * u4.w + wy * v4.x + wz * v4.y;
+    float uv = v4.z, uu = v4.w, vv = b.z;
+    float s = (uv * wv - vv * wu) / (uv * uv - uu * vv);
+    float tt = (uv * wu - uu * wv) / (uv * uv - uu * vv);
+    if (!((s >= 0.0f) & (tt >= 0.0f) & (s + tt <= 1.0f))) return false;
+    h.t = t;
+    h.x = ox + dx * r; h.y = oy + dy * r; h.z = oz + dz * r;
+    h.d2 = (ox - h.x) * (ox - h.x) + (oy - h.y) * (oy - h.y) + (oz - h.z) * (oz - h.z);
+    uint32_t type = 1;
+    if ((s == 0.0f) | (tt == 0.0f) | (s + tt == 1.0f)) {
+        type = 2;
+        if (((s == 0.0f) & (tt == 0.0f)) | ((s == 0.0f) & (tt == 1.0f)) | ((s == 1.0f) & (tt == 0.0f)))
+            type = 3;
+    }
+    h.type = type;
+    return true;
+}
+
+
+// cubeCollDetect over the reference grid (dSim3/src/spinKernelCpu.cpp:311-337)
+static __device__ __noinline__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py, float pz,
+                         uint32_t excluded, FastHit& best, bool& found) {
+    const uint32_t n = g.n;
+    const float L = g.L;
+    float dx = px - ox, dy = py - oy, dz = pz - oz;
+    uint32_t sx = ref_coord(ox, L, n), sy = ref_coord(oy, L, n), sz = ref_coord(oz, L, n);
+    uint32_t tx = ref_coord(px, L, n), ty = ref_coord(py, L, n), tz = ref_coord(pz, L, n);
+    uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
+    uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
+    uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
+    found = false;
+    uint32_t cx = sx;
+    do {
+        uint32_t cy = sy;
+        do {
+            uint32_t cz = sz;
+            do {
+                uint32_t c = n * n * cz + n * cy + cx;
+                uint32_t b0 = __ldg(g.cell_start + c), b1 = __ldg(g.cell_start + c + 1);
+                float bd2 = 400000000.0f;
+                for (uint32_t k = b0; k < b1; k++) {
+                    uint32_t t = __ldg(g.cell_tri + k);
+                    if (t == excluded) continue;
+                    const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
+                    float4 ra = __ldg(pp), rc = __ldg(pp + 1);
+                    float4 rb = make_float4(rc.x, rc.y, rc.z, __uint_as_float(t));
+                    FastHit h;
+                    if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) continue;
+                    if (h.d2 < bd2) { bd2 = h.d2; best = h; found = true; }
+                }
+                cz += iz;
+            } while ((cz != tz + iz) && !found);
+            cy += iy;
+        } while ((cy != ty + iy) && !found);
+        cx += ix;
+    } while ((cx != tx + ix) && !found);
+}
+
+
+}  // namespace dsim

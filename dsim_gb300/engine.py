@@ -176,6 +176,9 @@ class Mesh:
     def set_accel(self, cells_per_axis):
         check(native().dsim_mesh_set_accel(self.h, int(cells_per_axis)))
 
+    def set_kernel(self, variant):
+        check(native().dsim_mesh_set_kernel(self.h, int(variant)))
+
     def accel_info(self):
         info = np.zeros(3, np.uint64)
         check(native().dsim_mesh_accel_info(self.h, info))

@@ -67,6 +67,10 @@ int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
  * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
  * info = {cells per axis, entries, device bytes}. */
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
+/* step kernel on the fine grid (all give the same results): 1 one thread per
+ * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
+ * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM */
+int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]);
 /* copies the CSR grid: cellStart[numCubes^3 + 1], cellTri[entries] */
 int dsim_mesh_grid(const dsim_mesh* m, uint32_t* cellStart, uint32_t* cellTri);
