@@ -65,7 +65,7 @@ struct dsim_mesh {
     uint32_t* cell_tri = nullptr;
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
-    uint32_t kernel = 2;  // 1 per-thread candidate lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM)
+    uint32_t kernel = 4;  // 1 per-thread candidate lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM)
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
@@ -257,8 +257,8 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     cudaFree(counter);
     cudaFree(scratch);
     if (rc) return rc;
-    // default fine grid: a third of the reference cell edge
-    return accel_build(m, 3 * m->n <= 1024 ? 3 * m->n : 1024);
+    // default fine grid: half the reference cell edge
+    return accel_build(m, 2 * m->n <= 1024 ? 2 * m->n : 1024);
 }
 
 extern "C" {

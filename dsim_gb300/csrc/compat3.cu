@@ -149,7 +149,7 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
         return kErrFormat;
     }
     // fine acceleration grid from the records (triangle corners p1, p1 + v, p1 + u)
-    uint32_t nf = s.numCubes * 3 <= 1024 ? s.numCubes * 3 : 1024;
+    uint32_t nf = s.numCubes * 2 <= 1024 ? s.numCubes * 2 : 1024;
     uint32_t nkeys = accel_keys(nf);
     uint32_t* counter = nullptr;
     uint32_t* scr = nullptr;
@@ -350,7 +350,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
         b.iterations = n;
         b.step0 = done;
         b.draws = s.replay ? s.replay + (size_t)done * N : nullptr;
-        if ((rc = launch_mesh_step_coop(g, acc, b, s.set(cur, N), rng, 0))) { fail(rc); return; }
+        if ((rc = launch_mesh_step_coop(g, acc, b, s.set(cur, N), rng, 0, 8))) { fail(rc); return; }
     }
     rc = launch_soa_to_aos(s.set(cur, N), pos, spinInfo, s.replay ? nullptr : randSeed, iterations, 0);
     if (rc) fail(rc);
