@@ -47,7 +47,8 @@ __device__ __forceinline__ void tri_fine_range(const TriPlane& P, const TriBary&
 template <bool FILL>
 __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                               const TriBary* __restrict__ bary, uint32_t nf, float invLf,
-                              uint32_t* counter, const uint32_t* __restrict__ start, AccelRec* rec) {
+                              uint32_t* counter, const uint32_t* __restrict__ start, AccelRec* rec,
+                              uint32_t* tri) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nT) return;
     TriPlane P = plane[t];
@@ -61,22 +62,22 @@ __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                 uint32_t slot = atomicAdd(counter + key, 1u);
                 if (FILL) {
                     AccelRec r;
-                    r.a = make_float4(P.nx, P.ny, P.nz, P.p1x);
-                    r.b = make_float4(P.p1y, P.p1z, P.vv, __uint_as_float(t));
+                    r.q = make_float4(P.nx, P.ny, P.nz, P.nx * P.p1x + P.ny * P.p1y + P.nz * P.p1z);
                     rec[start[key] + slot] = r;
+                    tri[start[key] + slot] = t;
                 }
             }
 }
 
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       cudaStream_t st) {
+                       uint32_t* tri, cudaStream_t st) {
     if (nT == 0) return kOk;
     float invLf = (float)nf / 2.0f;
     if (fill)
-        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec);
+        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri);
     else
-        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec);
+        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }
@@ -175,11 +176,12 @@ __global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc,
                         uint32_t key = morton3(cx, cy, cz);
                         uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                         for (uint32_t k = b0; k < b1; k++) {
-                            const float4* rp = reinterpret_cast<const float4*>(acc.rec + k);
-                            float4 ra = __ldg(rp), rb = __ldg(rp + 1);
-                            if (__float_as_uint(rb.w) == excluded) continue;
+                            const float4 rq = __ldg(&acc.rec[k].q);
+                            if (!plane_may_cross(rq, ox, oy, oz, dx, dy, dz)) continue;
+                            const uint32_t t = __ldg(acc.tri + k);
+                            if (t == excluded) continue;
                             FastHit h;
-                            if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) continue;
+                            if (!test_tri(g, t, ox, oy, oz, dx, dy, dz, h)) continue;
                             bool dup = false;
                             for (int q = 0; q < nh; q++) dup |= (hits[q].t == h.t);
                             if (dup) continue;

@@ -69,6 +69,7 @@ struct dsim_mesh {
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
+    uint32_t* acc_tri = nullptr;
     MeshDev dev() const {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
@@ -77,15 +78,15 @@ struct dsim_mesh {
     }
     AccelDev acc() const {
         AccelDev a;
-        a.start = acc_start; a.rec = acc_rec; a.nf = nf; a.invLf = (float)nf / 2.0f;
+        a.start = acc_start; a.rec = acc_rec; a.tri = acc_tri; a.nf = nf; a.invLf = (float)nf / 2.0f;
         return a;
     }
 };
 
 // (Re)build the fine acceleration grid with nf cells per axis (0 removes it).
 static int accel_build(dsim_mesh* m, uint32_t nf) {
-    cudaFree(m->acc_start); cudaFree(m->acc_rec);
-    m->acc_start = nullptr; m->acc_rec = nullptr;
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri);
+    m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr;
     m->nf = 0; m->accEntries = 0; m->accBytes = 0;
     if (nf == 0) return kOk;
     if (nf > 1024) { set_last_error(kErrTooLarge, "accel grid: %u cells per axis > 1024", nf); return kErrTooLarge; }
@@ -99,22 +100,23 @@ static int accel_build(dsim_mesh* m, uint32_t nf) {
     do {
         if ((rc = dev_alloc(&m->acc_start, (size_t)nkeys + 1, &m->accBytes))) break;
         if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
-        if ((rc = launch_accel_cells(false, m->nT, m->plane, m->bary, nf, counter, nullptr, nullptr, st))) break;
+        if ((rc = launch_accel_cells(false, m->nT, m->plane, m->bary, nf, counter, nullptr, nullptr, nullptr, st))) break;
         if ((rc = launch_scan_exclusive(counter, m->acc_start, nkeys, scratch, st))) break;
         uint32_t total = 0;
         if (cudaMemcpyAsync(&total, m->acc_start + nkeys, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->accEntries = total;
         if ((rc = dev_alloc(&m->acc_rec, total, &m->accBytes))) break;
+        if ((rc = dev_alloc(&m->acc_tri, total, &m->accBytes))) break;
         if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
-        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, st))) break;
+        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, m->acc_tri, st))) break;
         if (cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->nf = nf;
     } while (0);
     if (rc == kErrCuda) set_last_error(kErrCuda, "accel grid build: %s", cudaGetErrorString(cudaGetLastError()));
     cudaFree(counter);
     cudaFree(scratch);
-    if (rc) { cudaFree(m->acc_start); cudaFree(m->acc_rec); m->acc_start = nullptr; m->acc_rec = nullptr; m->nf = 0; }
+    if (rc) { cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->nf = 0; }
     return rc;
 }
 
@@ -190,7 +192,7 @@ static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
     cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
-    cudaFree(m->acc_start); cudaFree(m->acc_rec);
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri);
     delete m;
 }
 

@@ -76,6 +76,7 @@ struct State {
     uint32_t nf = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
+    uint32_t* acc_tri = nullptr;
     // spin work buffers for the reordered fast path (grow with N)
     uint32_t cap = 0;
     float* w[10] = {nullptr};       // x, y, z, mag, phase  (two sets)
@@ -86,9 +87,9 @@ struct State {
     uint32_t sortEvery = 20;
     void release() {
         cudaFree(plane); cudaFree(bary); cudaFree(cell_start); cudaFree(cell_tri);
-        cudaFree(acc_start); cudaFree(acc_rec);
+        cudaFree(acc_start); cudaFree(acc_rec); cudaFree(acc_tri);
         plane = nullptr; bary = nullptr; cell_start = nullptr; cell_tri = nullptr;
-        acc_start = nullptr; acc_rec = nullptr; nf = 0;
+        acc_start = nullptr; acc_rec = nullptr; acc_tri = nullptr; nf = 0;
         have = false;
     }
     SpinsSorted set(int k, uint32_t N) const {
@@ -157,13 +158,14 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
     DSIM_CUDA_TRY(cudaMalloc(&scr, scan_scratch_words(nkeys) * 4));
     DSIM_CUDA_TRY(cudaMalloc(&s.acc_start, ((size_t)nkeys + 1) * 4));
     DSIM_CUDA_TRY(cudaMemset(counter, 0, (size_t)nkeys * 4));
-    rc = launch_accel_cells(false, nT, s.plane, s.bary, nf, counter, nullptr, nullptr, 0);
+    rc = launch_accel_cells(false, nT, s.plane, s.bary, nf, counter, nullptr, nullptr, nullptr, 0);
     if (!rc) rc = launch_scan_exclusive(counter, s.acc_start, nkeys, scr, 0);
     uint32_t accTotal = 0;
     if (!rc && cudaMemcpy(&accTotal, s.acc_start + nkeys, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
     if (!rc && cudaMalloc(&s.acc_rec, (size_t)(accTotal ? accTotal : 1) * sizeof(AccelRec)) != cudaSuccess) rc = kErrNoMem;
+    if (!rc && cudaMalloc(&s.acc_tri, (size_t)(accTotal ? accTotal : 1) * 4) != cudaSuccess) rc = kErrNoMem;
     if (!rc && cudaMemset(counter, 0, (size_t)nkeys * 4) != cudaSuccess) rc = kErrCuda;
-    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, 0);
+    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, s.acc_tri, 0);
     cudaFree(counter);
     cudaFree(scr);
     if (rc) { set_last_error(rc, "integrateSystem: building the fine grid failed"); return rc; }
@@ -334,7 +336,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
     int cur = 0;
     if ((rc = launch_aos_to_soa(pos, spinInfo, s.set(cur, N), 0))) { fail(rc); return; }
     AccelDev acc;
-    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.nf = s.nf; acc.invLf = (float)s.nf / 2.0f;
+    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.tri = s.acc_tri; acc.nf = s.nf; acc.invLf = (float)s.nf / 2.0f;
     a.spinKeys = randSeed;
     int rng = s.replay ? kRngReplay : kRngPhiloxPerSpinKey;
     uint32_t chunk = s.sortEvery ? s.sortEvery : iterations;

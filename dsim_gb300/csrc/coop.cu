@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
         float ox = x, oy = y, oz = z;
         float sd = a.sd[comp & 3u];
         float px = x + d.nx * sd, py = y + d.ny * sd, pz = z + d.nz * sd;
-        float ex = px, ey = py, ez = pz;
+        // (the reference's endPos equals the sub-segment target p at the top of
+        // every collision round, so p doubles as endPos)
         uint32_t excluded = 0xFFFFFFFFu;
         float umax = 1.0f, umin = 0.0f;
         if (STATS && valid) {
@@ -130,11 +131,12 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     const uint32_t excl = __shfl_sync(FULL, excluded, l);
                     const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                     for (uint32_t k = b0 + lane; k < b1; k += 32) {
-                        const float4* rp = reinterpret_cast<const float4*>(acc.rec + k);
-                        const float4 ra = __ldg(rp), rb = __ldg(rp + 1);
-                        if (__float_as_uint(rb.w) == excl) continue;
+                        const float4 rq = __ldg(&acc.rec[k].q);
+                        if (!plane_may_cross(rq, sox, soy, soz, sdx, sdy, sdz)) continue;
+                        const uint32_t t = __ldg(acc.tri + k);
+                        if (t == excl) continue;
                         FastHit h;
-                        if (test_rec(g, ra, rb, sox, soy, soz, sdx, sdy, sdz, h)) file_hit(H, l, h);
+                        if (test_tri(g, t, sox, soy, soz, sdx, sdy, sdz, h)) file_hit(H, l, h);
                     }
                 }
             }
@@ -145,11 +147,12 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     uint32_t key = morton3(lo0 + ix, lo1 + iy, lo2 + iz);
                     uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                     for (uint32_t k = b0; k < b1; k++) {
-                        const float4* rp = reinterpret_cast<const float4*>(acc.rec + k);
-                        const float4 ra = __ldg(rp), rb = __ldg(rp + 1);
-                        if (__float_as_uint(rb.w) == excluded) continue;
+                        const float4 rq = __ldg(&acc.rec[k].q);
+                        if (!plane_may_cross(rq, ox, oy, oz, dx, dy, dz)) continue;
+                        const uint32_t t = __ldg(acc.tri + k);
+                        if (t == excluded) continue;
                         FastHit h;
-                        if (test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) file_hit(H, lane, h);
+                        if (test_tri(g, t, ox, oy, oz, dx, dy, dz, h)) file_hit(H, lane, h);
                     }
                 }
             }
@@ -161,19 +164,9 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                 if (n > (uint32_t)kSlots) {
                     ref_scan(g, ox, oy, oz, px, py, pz, excluded, best, found);
                 } else if (n > 0) {
-                    // distinct hits
-                    FastHit hits[kSlots];
-                    int nh = 0;
-                    for (uint32_t q = 0; q < n; q++) {
-                        uint32_t t = H.t[q][lane];
-                        bool dup = false;
-                        for (int r = 0; r < nh; r++) dup |= (hits[r].t == t);
-                        if (dup) continue;
-                        hits[nh].t = t; hits[nh].type = H.type[q][lane]; hits[nh].d2 = H.d2[q][lane];
-                        hits[nh].x = H.x[q][lane]; hits[nh].y = H.y[q][lane]; hits[nh].z = H.z[q][lane];
-                        nh++;
-                    }
-                    // the reference's traversal of its grid over these hits
+                    // the reference's traversal of its grid over the hits filed in
+                    // this lane's slots (read in place; a triangle filed twice from
+                    // two fine cells is the same hit)
                     const uint32_t gn = g.n;
                     const float L = g.L;
                     uint32_t sx = ref_coord(ox, L, gn), sy = ref_coord(oy, L, gn), sz = ref_coord(oz, L, gn);
@@ -181,6 +174,7 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
                     uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
                     uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
+                    uint32_t bq = 0;
                     uint32_t cx = sx;
                     do {
                         uint32_t cy = sy;
@@ -188,11 +182,12 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                             uint32_t cz = sz;
                             do {
                                 uint32_t c = gn * gn * cz + gn * cy + cx;
-                                for (int q = 0; q < nh; q++) {
-                                    if (!in_ref_cell(g, c, hits[q].t)) continue;
-                                    if (!found || hits[q].d2 < best.d2 ||
-                                        (hits[q].d2 == best.d2 && hits[q].t < best.t)) {
-                                        best = hits[q];
+                                for (uint32_t q = 0; q < n; q++) {
+                                    const uint32_t t = H.t[q][lane];
+                                    if (!in_ref_cell(g, c, t)) continue;
+                                    const float d2 = H.d2[q][lane];
+                                    if (!found || d2 < H.d2[bq][lane] || (d2 == H.d2[bq][lane] && t < H.t[bq][lane])) {
+                                        bq = q;
                                         found = true;
                                     }
                                 }
@@ -202,6 +197,10 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                         } while ((cy != ty + iy) && !found);
                         cx += ix;
                     } while ((cx != tx + ix) && !found);
+                    if (found) {
+                        best.t = H.t[bq][lane]; best.type = H.type[bq][lane]; best.d2 = H.d2[bq][lane];
+                        best.x = H.x[bq][lane]; best.y = H.y[bq][lane]; best.z = H.z[bq][lane];
+                    }
                 }
                 if (!found) {
                     open = false;
@@ -209,14 +208,14 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     float thr = umax - (umax - umin) * a.perm;
                     if (d.u <= thr) {
                         if ((a.reflType == 0) | (best.type > 1)) {
-                            ex = ox; ey = oy; ez = oz;
+                            px = ox; py = oy; pz = oz;
                         } else {
                             const float4 nn = __ldg(reinterpret_cast<const float4*>(g.plane + best.t));
                             float nx = nn.x, ny = nn.y, nz = nn.z;
                             float sx2 = px - best.x, sy2 = py - best.y, sz2 = pz - best.z;
-                            ex = (1.0f - 2.0f * nx * nx) * sx2 - 2.0f * nx * ny * sy2 - 2.0f * nx * nz * sz2 + best.x;
-                            ey = -2.0f * nx * ny * sx2 + (1.0f - 2.0f * ny * ny) * sy2 - 2.0f * ny * nz * sz2 + best.y;
-                            ez = -2.0f * nx * nz * sx2 - 2.0f * ny * nz * sy2 + (1.0f - 2.0f * nz * nz) * sz2 + best.z;
+                            px = (1.0f - 2.0f * nx * nx) * sx2 - 2.0f * nx * ny * sy2 - 2.0f * nx * nz * sz2 + best.x;
+                            py = -2.0f * nx * ny * sx2 + (1.0f - 2.0f * ny * ny) * sy2 - 2.0f * ny * nz * sz2 + best.y;
+                            pz = -2.0f * nx * nz * sx2 - 2.0f * ny * nz * sy2 + (1.0f - 2.0f * nz * nz) * sz2 + best.z;
                         }
                         umax = thr;
                         nrefl++;
@@ -238,17 +237,17 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                         }
                     }
                     ox = best.x; oy = best.y; oz = best.z;
-                    px = ex; py = ey; pz = ez;
                     excluded = best.t;
                     if (++sub >= a.maxSub) {
                         status |= kStatusSubsegCap;
-                        ex = ox; ey = oy; ez = oz;
+                        px = ox; py = oy; pz = oz;
                         open = false;
                     }
                 }
             }
             __syncwarp();
         }
+        float ex = px, ey = py, ez = pz;
         if (valid) {
             if (ex > a.clampHi) ex = a.clampHi; else if (ex < a.clampLo) ex = a.clampLo;
             if (ey > a.clampHi) ey = a.clampHi; else if (ey < a.clampLo) ey = a.clampLo;
@@ -274,6 +273,7 @@ int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepA
     dim3 block(kCoopThreads), grid((S.N + kCoopThreads - 1) / kCoopThreads);
     if (a.tested) k_mesh_step_coop<true, 4><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     else if (occupancy >= 8) k_mesh_step_coop<false, 8><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    else if (occupancy >= 7) k_mesh_step_coop<false, 7><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     else if (occupancy >= 6) k_mesh_step_coop<false, 6><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     else k_mesh_step_coop<false, 4><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     DSIM_CUDA_TRY(cudaGetLastError());

@@ -56,14 +56,16 @@ struct MeshStepArgs {
 // ---- accel.cu -------------------------------------------------------------
 // Fine acceleration grid: every triangle is listed in each fine cell its
 // bounding box (widened by kAccelEps) overlaps; cells are stored in Morton
-// order; one 32-byte record per entry {n.x, n.y, n.z, p1.x}, {p1.y, p1.z, vv, t}.
+// order.  Per entry a 16-byte plane record {n.x, n.y, n.z, n.p1} for a
+// conservative plane-crossing prefilter, and the triangle index beside it.
 static constexpr float kAccelEps = 1e-5f;
 struct __align__(16) AccelRec {
-    float4 a, b;
+    float4 q;
 };
 struct AccelDev {
     const uint32_t* start;  // Morton key -> first record (keys + 1 entries)
     const AccelRec* rec;
+    const uint32_t* tri;    // triangle of each record
     uint32_t nf;            // fine cells per axis
     float invLf;            // nf / 2
 };
@@ -80,7 +82,7 @@ __host__ __device__ inline uint32_t accel_keys(uint32_t nf) {
 }
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       cudaStream_t st);
+                       uint32_t* tri, cudaStream_t st);
 int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
                       uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st);
 int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,

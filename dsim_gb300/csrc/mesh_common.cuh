@@ -93,6 +93,28 @@ __device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, f
 }
 
 
+// Conservative plane test on a fine-grid record q = {n, n.p1}: with den the
+// exact denominator of triCollDetect and na = n.p1 - n.o, the exact numerator
+// differs from na by at most ~2.5e-6 for points in the box (a few float
+// roundings of terms of size <= 3.5), so a margin of 1e-5 keeps every record
+// whose exact test can pass (0 < num/den < 1).
+static constexpr float kPlaneMargin = 1e-5f;
+__device__ __forceinline__ bool plane_may_cross(float4 q, float ox, float oy, float oz, float dx,
+                                                float dy, float dz) {
+    float den = q.x * dx + q.y * dy + q.z * dz;
+    float na = q.w - (q.x * ox + q.y * oy + q.z * oz);
+    return (den > 0.0f) ? ((na > -kPlaneMargin) & (na < den + kPlaneMargin))
+                        : ((den < 0.0f) & (na < kPlaneMargin) & (na > den - kPlaneMargin));
+}
+
+// exact test against triangle t from its per-triangle records
+__device__ __forceinline__ bool test_tri(const MeshDev& g, uint32_t t, float ox, float oy, float oz,
+                                         float dx, float dy, float dz, FastHit& h) {
+    const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
+    const float4 a = __ldg(pp), c = __ldg(pp + 1);
+    return test_rec(g, a, make_float4(c.x, c.y, c.z, __uint_as_float(t)), ox, oy, oz, dx, dy, dz, h);
+}
+
 // cubeCollDetect over the reference grid (dSim3/src/spinKernelCpu.cpp:311-337)
 static __device__ __noinline__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py, float pz,
                          uint32_t excluded, FastHit& best, bool& found) {
