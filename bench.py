@@ -339,6 +339,8 @@ def run_ours(args, rank, world):
     m = make_mesh(W)
     if args.kernel > 0:
         m.set_kernel(args.kernel)
+    if args.records > 0:
+        m.set_records(args.records)
     if args.accel >= 0:
         m.set_accel(args.accel)
     acc_info = m.accel_info()
@@ -410,6 +412,7 @@ def run_ours(args, rank, world):
                      "bytes_per_spin_step": B_step, "T_bar": Tbar,
                      "note": "B_step = 2*S + 40*T_bar, S = 20 B, T_bar = grid entries scanned per step (kernel counter)"},
         "gpu_launches": args.steps,
+        "launch_ms": times,
         "clocks": clk.summary(),
         "device": dev.name,
         "signal_after_run": S,
@@ -475,6 +478,7 @@ def main():
     ap.add_argument("--accel", type=int, default=-1, help="fine grid cells per axis (-1 default, 0 reference grid)")
     ap.add_argument("--sort-every", type=int, default=-1, help="steps between spin reorderings (-1 default)")
     ap.add_argument("--kernel", type=int, default=0, help="step kernel variant (0 default)")
+    ap.add_argument("--records", type=int, default=0, help="fine-grid record bytes (0 default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -87,6 +87,7 @@ def _declare_native(L):
         "dsim_mesh_free": (None, [VP]),
         "dsim_mesh_set_accel": (i32, [VP, u32]),
         "dsim_mesh_set_kernel": (i32, [VP, u32]),
+        "dsim_mesh_set_records": (i32, [VP, u32]),
         "dsim_mesh_accel_info": (i32, [VP, _nd(np.uint64, flags="C_CONTIGUOUS")]),
         "dsim_spins_set_sort_interval": (i32, [VP, u32]),
         "dsim_cyl_load": (i32, [C.c_char_p, f32, C.POINTER(VP)]),

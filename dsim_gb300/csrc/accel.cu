@@ -48,7 +48,7 @@ template <bool FILL>
 __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                               const TriBary* __restrict__ bary, uint32_t nf, float invLf,
                               uint32_t* counter, const uint32_t* __restrict__ start, AccelRec* rec,
-                              uint32_t* tri) {
+                              uint32_t* tri, AccelRecWide* recw) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nT) return;
     TriPlane P = plane[t];
@@ -61,23 +61,31 @@ __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                 uint32_t key = morton3(x, y, z);
                 uint32_t slot = atomicAdd(counter + key, 1u);
                 if (FILL) {
-                    AccelRec r;
-                    r.q = make_float4(P.nx, P.ny, P.nz, P.nx * P.p1x + P.ny * P.p1y + P.nz * P.p1z);
-                    rec[start[key] + slot] = r;
-                    tri[start[key] + slot] = t;
+                    const float4 q = make_float4(P.nx, P.ny, P.nz, P.nx * P.p1x + P.ny * P.p1y + P.nz * P.p1z);
+                    if (recw) {
+                        AccelRecWide r;
+                        r.q = q;
+                        r.pt = make_float4(P.p1x, P.p1y, P.p1z, __uint_as_float(t));
+                        recw[start[key] + slot] = r;
+                    } else {
+                        AccelRec r;
+                        r.q = q;
+                        rec[start[key] + slot] = r;
+                        tri[start[key] + slot] = t;
+                    }
                 }
             }
 }
 
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       uint32_t* tri, cudaStream_t st) {
+                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st) {
     if (nT == 0) return kOk;
     float invLf = (float)nf / 2.0f;
     if (fill)
-        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri);
+        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw);
     else
-        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri);
+        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }
@@ -176,12 +184,8 @@ __global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc,
                         uint32_t key = morton3(cx, cy, cz);
                         uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                         for (uint32_t k = b0; k < b1; k++) {
-                            const float4 rq = __ldg(&acc.rec[k].q);
-                            if (!plane_may_cross(rq, ox, oy, oz, dx, dy, dz)) continue;
-                            const uint32_t t = __ldg(acc.tri + k);
-                            if (t == excluded) continue;
                             FastHit h;
-                            if (!test_tri(g, t, ox, oy, oz, dx, dy, dz, h)) continue;
+                            if (!test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h)) continue;
                             bool dup = false;
                             for (int q = 0; q < nh; q++) dup |= (hits[q].t == h.t);
                             if (dup) continue;

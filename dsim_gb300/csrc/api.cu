@@ -70,6 +70,8 @@ struct dsim_mesh {
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
     uint32_t* acc_tri = nullptr;
+    AccelRecWide* acc_recw = nullptr;
+    uint32_t accWide = 1;  // 32-byte fine-grid records (0: 16-byte)
     MeshDev dev() const {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
@@ -78,15 +80,16 @@ struct dsim_mesh {
     }
     AccelDev acc() const {
         AccelDev a;
-        a.start = acc_start; a.rec = acc_rec; a.tri = acc_tri; a.nf = nf; a.invLf = (float)nf / 2.0f;
+        a.start = acc_start; a.rec = acc_rec; a.tri = acc_tri; a.recw = acc_recw; a.nf = nf;
+        a.invLf = (float)nf / 2.0f; a.wide = acc_recw ? 1u : 0u;
         return a;
     }
 };
 
 // (Re)build the fine acceleration grid with nf cells per axis (0 removes it).
 static int accel_build(dsim_mesh* m, uint32_t nf) {
-    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri);
-    m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr;
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
+    m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr;
     m->nf = 0; m->accEntries = 0; m->accBytes = 0;
     if (nf == 0) return kOk;
     if (nf > 1024) { set_last_error(kErrTooLarge, "accel grid: %u cells per axis > 1024", nf); return kErrTooLarge; }
@@ -100,23 +103,30 @@ static int accel_build(dsim_mesh* m, uint32_t nf) {
     do {
         if ((rc = dev_alloc(&m->acc_start, (size_t)nkeys + 1, &m->accBytes))) break;
         if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
-        if ((rc = launch_accel_cells(false, m->nT, m->plane, m->bary, nf, counter, nullptr, nullptr, nullptr, st))) break;
+        if ((rc = launch_accel_cells(false, m->nT, m->plane, m->bary, nf, counter, nullptr, nullptr, nullptr, nullptr, st))) break;
         if ((rc = launch_scan_exclusive(counter, m->acc_start, nkeys, scratch, st))) break;
         uint32_t total = 0;
         if (cudaMemcpyAsync(&total, m->acc_start + nkeys, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->accEntries = total;
-        if ((rc = dev_alloc(&m->acc_rec, total, &m->accBytes))) break;
-        if ((rc = dev_alloc(&m->acc_tri, total, &m->accBytes))) break;
+        if (m->accWide) {
+            if ((rc = dev_alloc(&m->acc_recw, total, &m->accBytes))) break;
+        } else {
+            if ((rc = dev_alloc(&m->acc_rec, total, &m->accBytes))) break;
+            if ((rc = dev_alloc(&m->acc_tri, total, &m->accBytes))) break;
+        }
         if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
-        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, m->acc_tri, st))) break;
+        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, m->acc_tri, m->acc_recw, st))) break;
         if (cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->nf = nf;
     } while (0);
     if (rc == kErrCuda) set_last_error(kErrCuda, "accel grid build: %s", cudaGetErrorString(cudaGetLastError()));
     cudaFree(counter);
     cudaFree(scratch);
-    if (rc) { cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->nf = 0; }
+    if (rc) {
+        cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
+        m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr; m->nf = 0;
+    }
     return rc;
 }
 
@@ -192,7 +202,7 @@ static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
     cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
-    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri);
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
     delete m;
 }
 
@@ -768,6 +778,15 @@ int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant) {
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis) {
     if (!m) return kErrInvalid;
     return accel_build(m, cellsPerAxis);
+}
+
+int dsim_mesh_set_records(dsim_mesh* m, uint32_t bytesPerRecord) {
+    if (!m || (bytesPerRecord != 16 && bytesPerRecord != 32)) {
+        set_last_error(kErrInvalid, "record size must be 16 or 32 bytes");
+        return kErrInvalid;
+    }
+    m->accWide = bytesPerRecord == 32 ? 1u : 0u;
+    return accel_build(m, m->nf);
 }
 
 int dsim_spins_set_sort_interval(dsim_spins* s, uint32_t steps) {

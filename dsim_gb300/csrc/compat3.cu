@@ -158,14 +158,14 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
     DSIM_CUDA_TRY(cudaMalloc(&scr, scan_scratch_words(nkeys) * 4));
     DSIM_CUDA_TRY(cudaMalloc(&s.acc_start, ((size_t)nkeys + 1) * 4));
     DSIM_CUDA_TRY(cudaMemset(counter, 0, (size_t)nkeys * 4));
-    rc = launch_accel_cells(false, nT, s.plane, s.bary, nf, counter, nullptr, nullptr, nullptr, 0);
+    rc = launch_accel_cells(false, nT, s.plane, s.bary, nf, counter, nullptr, nullptr, nullptr, nullptr, 0);
     if (!rc) rc = launch_scan_exclusive(counter, s.acc_start, nkeys, scr, 0);
     uint32_t accTotal = 0;
     if (!rc && cudaMemcpy(&accTotal, s.acc_start + nkeys, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
     if (!rc && cudaMalloc(&s.acc_rec, (size_t)(accTotal ? accTotal : 1) * sizeof(AccelRec)) != cudaSuccess) rc = kErrNoMem;
     if (!rc && cudaMalloc(&s.acc_tri, (size_t)(accTotal ? accTotal : 1) * 4) != cudaSuccess) rc = kErrNoMem;
     if (!rc && cudaMemset(counter, 0, (size_t)nkeys * 4) != cudaSuccess) rc = kErrCuda;
-    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, s.acc_tri, 0);
+    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, s.acc_tri, nullptr, 0);
     cudaFree(counter);
     cudaFree(scr);
     if (rc) { set_last_error(rc, "integrateSystem: building the fine grid failed"); return rc; }
@@ -336,7 +336,8 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
     int cur = 0;
     if ((rc = launch_aos_to_soa(pos, spinInfo, s.set(cur, N), 0))) { fail(rc); return; }
     AccelDev acc;
-    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.tri = s.acc_tri; acc.nf = s.nf; acc.invLf = (float)s.nf / 2.0f;
+    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.tri = s.acc_tri; acc.recw = nullptr; acc.nf = s.nf;
+    acc.invLf = (float)s.nf / 2.0f; acc.wide = 0;
     a.spinKeys = randSeed;
     int rng = s.replay ? kRngReplay : kRngPhiloxPerSpinKey;
     uint32_t chunk = s.sortEvery ? s.sortEvery : iterations;

@@ -131,12 +131,8 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     const uint32_t excl = __shfl_sync(FULL, excluded, l);
                     const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                     for (uint32_t k = b0 + lane; k < b1; k += 32) {
-                        const float4 rq = __ldg(&acc.rec[k].q);
-                        if (!plane_may_cross(rq, sox, soy, soz, sdx, sdy, sdz)) continue;
-                        const uint32_t t = __ldg(acc.tri + k);
-                        if (t == excl) continue;
                         FastHit h;
-                        if (test_tri(g, t, sox, soy, soz, sdx, sdy, sdz, h)) file_hit(H, l, h);
+                        if (test_entry(g, acc, k, excl, sox, soy, soz, sdx, sdy, sdz, h)) file_hit(H, l, h);
                     }
                 }
             }
@@ -147,12 +143,8 @@ __global__ void __launch_bounds__(kCoopThreads, MINB) k_mesh_step_coop(MeshDev g
                     uint32_t key = morton3(lo0 + ix, lo1 + iy, lo2 + iz);
                     uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                     for (uint32_t k = b0; k < b1; k++) {
-                        const float4 rq = __ldg(&acc.rec[k].q);
-                        if (!plane_may_cross(rq, ox, oy, oz, dx, dy, dz)) continue;
-                        const uint32_t t = __ldg(acc.tri + k);
-                        if (t == excluded) continue;
                         FastHit h;
-                        if (test_tri(g, t, ox, oy, oz, dx, dy, dz, h)) file_hit(H, lane, h);
+                        if (test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h)) file_hit(H, lane, h);
                     }
                 }
             }

@@ -62,12 +62,19 @@ static constexpr float kAccelEps = 1e-5f;
 struct __align__(16) AccelRec {
     float4 q;
 };
+// 32-byte record: the plane record and {p1.x, p1.y, p1.z, t} in one sector,
+// so the exact plane test needs no dependent load
+struct __align__(32) AccelRecWide {
+    float4 q, pt;
+};
 struct AccelDev {
     const uint32_t* start;  // Morton key -> first record (keys + 1 entries)
-    const AccelRec* rec;
-    const uint32_t* tri;    // triangle of each record
+    const AccelRec* rec;    // 16-byte records (wide == 0)
+    const uint32_t* tri;    // triangle of each record (wide == 0)
+    const AccelRecWide* recw;  // 32-byte records (wide == 1)
     uint32_t nf;            // fine cells per axis
     float invLf;            // nf / 2
+    uint32_t wide;
 };
 // spin state reordered by cell; id = the spin's stable index
 struct SpinsSorted {
@@ -82,7 +89,7 @@ __host__ __device__ inline uint32_t accel_keys(uint32_t nf) {
 }
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       uint32_t* tri, cudaStream_t st);
+                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st);
 int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
                       uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st);
 int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,

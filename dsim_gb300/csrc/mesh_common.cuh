@@ -115,6 +115,41 @@ __device__ __forceinline__ bool test_tri(const MeshDev& g, uint32_t t, float ox,
     return test_rec(g, a, make_float4(c.x, c.y, c.z, __uint_as_float(t)), ox, oy, oz, dx, dy, dz, h);
 }
 
+// exact test with the plane data from a 32-byte record (p1, t) and the rest
+// (vv, u, v, uv, uu) from the triangle's records, loaded only past the plane
+__device__ __forceinline__ bool test_split(const MeshDev& g, float4 q, float4 pt, float ox, float oy,
+                                           float oz, float dx, float dy, float dz, FastHit& h) {
+    float num = q.x * (pt.x - ox) + q.y * (pt.y - oy) + q.z * (pt.z - oz);
+    float den = q.x * dx + q.y * dy + q.z * dz;
+    if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
+        ((__float_as_uint(num) ^ __float_as_uint(den)) & 0x80000000u))
+        return false;
+    float r = num / den;
+    if (!((0.0f < r) & (r < 1.0f))) return false;
+    const uint32_t t = __float_as_uint(pt.w);
+    const float vv = __ldg(&g.plane[t].vv);
+    return test_rec(g, make_float4(q.x, q.y, q.z, pt.x), make_float4(pt.y, pt.z, vv, pt.w), ox, oy, oz,
+                    dx, dy, dz, h);
+}
+
+// one fine-grid entry k against a sub-segment (either record layout)
+__device__ __forceinline__ bool test_entry(const MeshDev& g, const AccelDev& acc, uint32_t k,
+                                           uint32_t excl, float ox, float oy, float oz, float dx,
+                                           float dy, float dz, FastHit& h) {
+    if (acc.wide) {
+        const float4 q = __ldg(&acc.recw[k].q);
+        if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
+        const float4 pt = __ldg(&acc.recw[k].pt);
+        if (__float_as_uint(pt.w) == excl) return false;
+        return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
+    }
+    const float4 q = __ldg(&acc.rec[k].q);
+    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
+    const uint32_t t = __ldg(acc.tri + k);
+    if (t == excl) return false;
+    return test_tri(g, t, ox, oy, oz, dx, dy, dz, h);
+}
+
 // cubeCollDetect over the reference grid (dSim3/src/spinKernelCpu.cpp:311-337)
 static __device__ __noinline__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py, float pz,
                          uint32_t excluded, FastHit& best, bool& found) {

@@ -176,6 +176,9 @@ class Mesh:
     def set_accel(self, cells_per_axis):
         check(native().dsim_mesh_set_accel(self.h, int(cells_per_axis)))
 
+    def set_records(self, nbytes):
+        check(native().dsim_mesh_set_records(self.h, int(nbytes)))
+
     def set_kernel(self, variant):
         check(native().dsim_mesh_set_kernel(self.h, int(variant)))
 

@@ -71,6 +71,10 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
  * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
  * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM */
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
+/* fine-grid record size: 32 (default) holds the plane data for the exact
+ * plane test; 16 holds a prefilter record only (half the bytes, one more
+ * dependent load for records that pass) */
+int dsim_mesh_set_records(dsim_mesh* m, uint32_t bytesPerRecord);
 int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]);
 /* copies the CSR grid: cellStart[numCubes^3 + 1], cellTri[entries] */
 int dsim_mesh_grid(const dsim_mesh* m, uint32_t* cellStart, uint32_t* cellTri);

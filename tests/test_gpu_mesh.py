@@ -47,13 +47,16 @@ def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
         assert np.array_equal(tri[start[c]:start[c + 1]], dense[c, :cc[c]])
 
 
-@pytest.mark.parametrize("membranes,perm,accel,sort", [
-    ("AM", 0.05, None, 20), ("G", 0.0, None, 20), ("G", 0.3, None, 7),
-    ("AM", 0.05, 0, 0), ("AM", 0.05, 37, 7), ("AM", 0.05, 300, 0), ("G", 0.3, 13, 1)])
-def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort):
+@pytest.mark.parametrize("membranes,perm,accel,sort,kernel,records", [
+    ("AM", 0.05, None, 20, None, None), ("G", 0.0, None, 20, None, None),
+    ("G", 0.3, None, 7, None, None), ("AM", 0.05, 0, 0, None, None),
+    ("AM", 0.05, 37, 7, None, 16), ("AM", 0.05, 300, 0, None, None), ("G", 0.3, 13, 1, None, 16),
+    ("AM", 0.05, None, 20, 1, None), ("AM", 0.05, None, 20, 2, 16), ("AM", 0.05, 75, 20, 3, None)])
+def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort, kernel, records):
     """accel None: default fine grid; 0: reference-grid scan; other: fine
     cells per axis (coarser and finer than the reference grid).  sort: steps
-    between spin reorderings (0 = never)."""
+    between spin reorderings (0 = never).  kernel: step kernel variant;
+    records: fine-grid record bytes."""
     from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
     case = MeshCase(tmp_path, membranes=membranes, permeability=perm, N=1500)
     iters = 60
@@ -65,6 +68,10 @@ def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel,
     m = Mesh.load(case.path, case.spaceScale)
     if accel is not None:
         m.set_accel(accel)
+    if records is not None:
+        m.set_records(records)
+    if kernel is not None:
+        m.set_kernel(kernel)
     s = Spins(case.N)
     s.set_sort_interval(sort)
     s.set(case.pos, case.mag, case.phase, case.comp, case.fiber)
