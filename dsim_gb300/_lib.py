@@ -108,6 +108,7 @@ def _declare_native(L):
         "dsim_mesh_run": (i32, [VP, VP, C.POINTER(MeshParams), OF32, OF32, u32, u64, u64, OF32, i32]),
         "dsim_cyl_run": (i32, [VP, VP, C.POINTER(CylParams), OF32, OF32, u32, u64, u64, OF32, i32]),
         "dsim_signal": (i32, [VP, C.c_double, F64]),
+        "dsim_signal_noalloc": (i32, [VP, VP, u32, i32, C.c_double, VP, VP]),
         "dsim_sync": (i32, [VP]),
         "dsim_timer_start": (i32, [VP]),
         "dsim_timer_stop": (i32, [VP, C.POINTER(f32)]),

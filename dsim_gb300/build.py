@@ -24,9 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EXACT = {"mesh.cu", "cyl.cu", "accel.cu", "coop.cu"}
 
 UNITS = ["mesh.cu", "accel.cu", "coop.cu", "cyl.cu", "scan.cu", "reduce.cu", "api.cu", "compat3.cu", "compat2.cu",
-         "host_formats.cpp"]
+         "host_formats.cpp", "noalloc.cu"]
 LIBS = {
-    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "cyl", "scan", "reduce"],
+    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "cyl", "scan", "reduce", "noalloc"],
     "libdsim3.so": ["compat3", "mesh", "accel", "coop", "scan"],
     "libdsim2.so": ["compat2", "cyl"],
 }

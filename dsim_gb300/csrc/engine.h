@@ -135,6 +135,10 @@ int launch_scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_
 size_t reduce_scratch_doubles(uint32_t N);
 int launch_signal(const SpinsDev& S, int layout, double region, double* partials, double* out15,
                   cudaStream_t st);
+// same partial pass over nb blocks (partials: nb * 15 doubles), then a
+// warp-per-field final pass
+int launch_signal_blocks(const SpinsDev& S, int layout, double region, double* partials, int nb,
+                         double* out15, cudaStream_t st);
 
 // ---- cyl.cu ---------------------------------------------------------------
 struct CylDev {

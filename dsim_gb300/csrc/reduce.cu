@@ -91,6 +91,29 @@ __global__ void k_signal_final(const double* __restrict__ partials, int nblocks,
     out[k] = v;
 }
 
+// final pass over nb partial records: warp k adds field k with lane-strided
+// partial sums and a shuffle tree (fixed order, deterministic)
+__global__ void k_signal_final_warps(const double* __restrict__ partials, int nb, double* out) {
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (k >= kRedVals) return;
+    double v = 0.0;
+    for (int b = lane; b < nb; b += 32) v += partials[(size_t)b * kRedVals + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+    if (lane == 0) out[k] = v;
+}
+
+int launch_signal_blocks(const SpinsDev& S, int layout, double region, double* partials, int nb,
+                         double* out15, cudaStream_t st) {
+    if (nb < 1) nb = 1;
+    if (layout == kLayoutSoA) k_signal_partial<kLayoutSoA><<<nb, kRedThreads, 0, st>>>(S, region, partials);
+    else if (layout == kLayoutAoS) k_signal_partial<kLayoutAoS><<<nb, kRedThreads, 0, st>>>(S, region, partials);
+    else k_signal_partial<2><<<nb, kRedThreads, 0, st>>>(S, region, partials);
+    k_signal_final_warps<<<1, 32 * kRedVals, 0, st>>>(partials, nb, out15);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
 int launch_signal(const SpinsDev& S, int layout, double region, double* partials, double* out15,
                   cudaStream_t st) {
     int nb = kRedBlocks;

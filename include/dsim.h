@@ -167,6 +167,27 @@ int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const flo
  * region > 0 keeps spins with |x|,|y|,|z| < region (dSim2 uses 0.8). */
 int dsim_signal(dsim_spins* s, double region, double out[15]);
 
+/* dsim_signal over the reference's own device spin arrays, allocating
+ * nothing (no counterpart in the reference, whose getMrSignal copies every
+ * spin to the host: dSim3/src/spinSystem.cpp:1452-1500,
+ * dSim2/src/spinSystem.cpp:944-978).  For callers that cannot allocate device
+ * memory when they need the signal.
+ *   layout DSIM_SIGNAL_DSIM3: pos = float3[N], spinRecords = spinData[N]
+ *          (12 B: mag, phase, compartment byte, pad, fiber u16)
+ *   layout DSIM_SIGNAL_DSIM2: pos = float4[N] {x, y, z, phase},
+ *          spinRecords = uint4 seeds[N] (imo + 1 in word 2) or NULL; mag = 1
+ * out: DEVICE pointer to 15 doubles, same meaning as dsim_signal; written
+ * asynchronously on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Scratch is a fixed array inside the library (983,040 bytes): N above
+ * 16,777,216 returns DSIM_ETOOLARGE.  Nothing must start at zero.  The first
+ * call on a device looks up the scratch address; make it before any stream
+ * capture.  Calls that may overlap in time race on the one scratch array:
+ * serialise them (e.g. issue them on one stream). */
+#define DSIM_SIGNAL_DSIM3 1
+#define DSIM_SIGNAL_DSIM2 2
+int dsim_signal_noalloc(const float* pos, const void* spinRecords, uint32_t N, int layout,
+                        double region, double* out, void* stream);
+
 /* The draws the step kernels use: for spins [spin0, spin0 + n) at global
  * step `step` with key `seed` and counter word `stream`, writes the Philox
  * words (raw, 4 per spin, may be NULL) and (n.x, n.y, n.z, u) (draws4). */
