@@ -65,7 +65,7 @@ struct dsim_mesh {
     uint32_t* cell_tri = nullptr;
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
-    uint32_t kernel = 4;  // 1 per-thread candidate lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM)
+    uint32_t kernel = 6;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened (8, 6, 4)
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
@@ -269,8 +269,9 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     cudaFree(counter);
     cudaFree(scratch);
     if (rc) return rc;
-    // default fine grid: half the reference cell edge
-    return accel_build(m, 2 * m->n <= 1024 ? 2 * m->n : 1024);
+    // default fine grid: 2.5 fine cells per reference cell edge
+    const uint32_t nf = 5 * m->n / 2;
+    return accel_build(m, nf < 1 ? 1 : (nf <= 1024 ? nf : 1024));
 }
 
 extern "C" {
@@ -761,16 +762,19 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
         b.step0 = a.step0 + done;
         b.grad = grad0 ? grad0 + done : nullptr;
         b.draws = draws0 ? draws0 + (size_t)done * s->N : nullptr;
-        rc = m->kernel == 1 ? launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st)
-                            : launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
-                                                    m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
+        if (m->kernel == 1) rc = launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st);
+        else if (m->kernel >= 5)
+            rc = launch_mesh_step_flat(m->dev(), m->acc(), b, s->sorted(), rng, s->st, m->kernel == 5 ? 8 : (m->kernel == 6 ? 6 : 4));
+        else
+            rc = launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
+                                       m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
         if (rc) return rc;
     }
     return kOk;
 }
 
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant) {
-    if (!m || variant < 1 || variant > 4) { set_last_error(kErrInvalid, "kernel variant must be 1..4"); return kErrInvalid; }
+    if (!m || variant < 1 || variant > 7) { set_last_error(kErrInvalid, "kernel variant must be 1..7"); return kErrInvalid; }
     m->kernel = variant;
     return kOk;
 }

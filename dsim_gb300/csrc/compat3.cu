@@ -75,8 +75,7 @@ struct State {
     // fine acceleration grid (cells per axis = accelFactor x k_numCubes)
     uint32_t nf = 0;
     uint32_t* acc_start = nullptr;
-    AccelRec* acc_rec = nullptr;
-    uint32_t* acc_tri = nullptr;
+    AccelRecWide* acc_recw = nullptr;
     // spin work buffers for the reordered fast path (grow with N)
     uint32_t cap = 0;
     float* w[10] = {nullptr};       // x, y, z, mag, phase  (two sets)
@@ -87,9 +86,9 @@ struct State {
     uint32_t sortEvery = 20;
     void release() {
         cudaFree(plane); cudaFree(bary); cudaFree(cell_start); cudaFree(cell_tri);
-        cudaFree(acc_start); cudaFree(acc_rec); cudaFree(acc_tri);
+        cudaFree(acc_start); cudaFree(acc_recw);
         plane = nullptr; bary = nullptr; cell_start = nullptr; cell_tri = nullptr;
-        acc_start = nullptr; acc_rec = nullptr; acc_tri = nullptr; nf = 0;
+        acc_start = nullptr; acc_recw = nullptr; nf = 0;
         have = false;
     }
     SpinsSorted set(int k, uint32_t N) const {
@@ -149,8 +148,10 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
         set_last_error(kErrFormat, "integrateSystem: trianglesInCubes names a triangle >= %u or a cell above k_maxTrianglesPerCube", nT);
         return kErrFormat;
     }
-    // fine acceleration grid from the records (triangle corners p1, p1 + v, p1 + u)
-    uint32_t nf = s.numCubes * 2 <= 1024 ? s.numCubes * 2 : 1024;
+    // fine acceleration grid from the records (triangle corners p1, p1 + v, p1 + u),
+    // 2.5 fine cells per reference cell edge, 32-byte records
+    uint32_t nf = s.numCubes * 5 / 2 <= 1024 ? s.numCubes * 5 / 2 : 1024;
+    if (nf < 1) nf = 1;
     uint32_t nkeys = accel_keys(nf);
     uint32_t* counter = nullptr;
     uint32_t* scr = nullptr;
@@ -162,10 +163,9 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
     if (!rc) rc = launch_scan_exclusive(counter, s.acc_start, nkeys, scr, 0);
     uint32_t accTotal = 0;
     if (!rc && cudaMemcpy(&accTotal, s.acc_start + nkeys, 4, cudaMemcpyDeviceToHost) != cudaSuccess) rc = kErrCuda;
-    if (!rc && cudaMalloc(&s.acc_rec, (size_t)(accTotal ? accTotal : 1) * sizeof(AccelRec)) != cudaSuccess) rc = kErrNoMem;
-    if (!rc && cudaMalloc(&s.acc_tri, (size_t)(accTotal ? accTotal : 1) * 4) != cudaSuccess) rc = kErrNoMem;
+    if (!rc && cudaMalloc(&s.acc_recw, (size_t)(accTotal ? accTotal : 1) * sizeof(AccelRecWide)) != cudaSuccess) rc = kErrNoMem;
     if (!rc && cudaMemset(counter, 0, (size_t)nkeys * 4) != cudaSuccess) rc = kErrCuda;
-    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, s.acc_rec, s.acc_tri, nullptr, 0);
+    if (!rc) rc = launch_accel_cells(true, nT, s.plane, s.bary, nf, counter, s.acc_start, nullptr, nullptr, s.acc_recw, 0);
     cudaFree(counter);
     cudaFree(scr);
     if (rc) { set_last_error(rc, "integrateSystem: building the fine grid failed"); return rc; }
@@ -336,8 +336,8 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
     int cur = 0;
     if ((rc = launch_aos_to_soa(pos, spinInfo, s.set(cur, N), 0))) { fail(rc); return; }
     AccelDev acc;
-    acc.start = s.acc_start; acc.rec = s.acc_rec; acc.tri = s.acc_tri; acc.recw = nullptr; acc.nf = s.nf;
-    acc.invLf = (float)s.nf / 2.0f; acc.wide = 0;
+    acc.start = s.acc_start; acc.rec = nullptr; acc.tri = nullptr; acc.recw = s.acc_recw; acc.nf = s.nf;
+    acc.invLf = (float)s.nf / 2.0f; acc.wide = 1;
     a.spinKeys = randSeed;
     int rng = s.replay ? kRngReplay : kRngPhiloxPerSpinKey;
     uint32_t chunk = s.sortEvery ? s.sortEvery : iterations;
@@ -353,7 +353,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
         b.iterations = n;
         b.step0 = done;
         b.draws = s.replay ? s.replay + (size_t)done * N : nullptr;
-        if ((rc = launch_mesh_step_coop(g, acc, b, s.set(cur, N), rng, 0, 8))) { fail(rc); return; }
+        if ((rc = launch_mesh_step_flat(g, acc, b, s.set(cur, N), rng, 0, 6))) { fail(rc); return; }
     }
     rc = launch_soa_to_aos(s.set(cur, N), pos, spinInfo, s.replay ? nullptr : randSeed, iterations, 0);
     if (rc) fail(rc);

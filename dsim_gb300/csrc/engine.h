@@ -100,6 +100,9 @@ int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st
 // compiled for (4, 6 or 8: register budget 128, 85 or 64)
 int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
                           const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 6);
+// flat.cu: warp-flattened candidate lists (same results); occupancy 6 or 8
+int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
+                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 8);
 int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st);
 int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
                       uint32_t iterations, cudaStream_t st);

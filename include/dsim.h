@@ -63,13 +63,15 @@ int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
 /* The step kernels find candidate triangles in a finer acceleration grid
  * (each triangle listed in every fine cell its bounding box overlaps) and
  * apply the reference grid's first-cell-with-hit rule only to the hits, which
- * gives the same results.  Built with 2 * numCubes cells per axis by default;
+ * gives the same results.  Built with 2.5 * numCubes cells per axis by default;
  * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
  * info = {cells per axis, entries, device bytes}. */
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
-/* step kernel on the fine grid (all give the same results; default 4): 1 one thread per
+/* step kernel on the fine grid (all give the same results; default 6): 1 one thread per
  * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
- * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM */
+ * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM; 5, 6, 7 the
+ * warp's candidate records flattened into one list, lanes stepping
+ * independently (8, 6, 4 blocks per SM) */
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 /* fine-grid record size: 32 (default) holds the plane data for the exact
  * plane test; 16 holds a prefilter record only (half the bytes, one more
