@@ -38,7 +38,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 F = np.float32
-METRIC = "spin-steps/s"
+DRAM_BYTES_PER_SPIN_STEP = 1.542e9 / (262144 * 20)
+METRIC = "spin-steps/s on 1 GB300, served vs plain, at \u22641e-3 signal err; p50/p99 latency"
 UNIT = "spin-steps/s"
 
 
@@ -370,6 +371,7 @@ def run_ours(args, rank, world):
                  step0=k * it)
     s.sync()
     reset()
+    s.launches(reset=True)
     times = []
     barrier(world)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
@@ -381,6 +383,7 @@ def run_ours(args, rank, world):
             times.append(s.timer_stop())
         s.sync()
     barrier(world)
+    launches = s.launches(reset=True)
     assert s.status() == 0
     total_ms = sum(times)
     total_ms = max_over_ranks(total_ms, world)
@@ -392,6 +395,14 @@ def run_ours(args, rank, world):
     S = signal_from_sums(sums)[0]
 
     hbm, kind = peaks()
+    # DRAM bytes of the step kernel per spin-step, from one ncu capture of
+    # k_mesh_step_flat<0,6> (default kernel, 125^3 fine grid, 32-byte records)
+    # on 262,144 spins x 20 steps of this mesh: 1.487 GB read + 0.055 GB
+    # written per launch = 294 B per spin-step; scaled to this call's spin-steps
+    default_cfg = args.kernel <= 0 and args.accel < 0 and args.records <= 0 and args.sort_every < 0
+    traffic = DRAM_BYTES_PER_SPIN_STEP * it * W.N if default_cfg else None
+    traffic_note = ("bytes per launch (one %d-step call) = 294.2 B per spin-step from an ncu capture of "
+                    "the default step kernel, scaled by spin-steps" % it) if default_cfg else "no capture for this configuration"
     S_bytes = 12 + 4 + 4
     B_step = 2 * S_bytes + 40 * Tbar
     mean_launch_ms = (sum(times) / len(times))
@@ -401,17 +412,18 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "mesh: %d beaded tubes, %d triangles, 50 um cube, 1 um cells, %d spins, "
-                               "dt 5 us, PGSE delta 15 Delta 40 ms, b 3000 s/mm2, 1000 steps per launch"
-                               % (W.axons, len(W.tube["trgls"]), W.N),
+                               "dt 5 us, PGSE delta 15 Delta 40 ms, b 3000 s/mm2, %d steps per launch"
+                               % (W.axons, len(W.tube["trgls"]), W.N, it),
                    "spins": W.N, "triangles": int(len(W.tube["trgls"])), "steps_per_launch": it,
                    "form": "plain", "rng": "philox4x32-10", "l2": "flushed between launches (512 MB write)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "accel_cells_per_axis": acc_info["cells"], "sort_every": args.sort_every},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_kind": kind,
+                     "frac": achieved / hbm, "traffic": traffic, "peak_kind": kind,
+                     "traffic_note": traffic_note,
                      "bytes_per_spin_step": B_step, "T_bar": Tbar,
                      "note": "B_step = 2*S + 40*T_bar, S = 20 B, T_bar = grid entries scanned per step (kernel counter)"},
-        "gpu_launches": args.steps,
+        "gpu_launches": launches,
         "launch_ms": times,
         "clocks": clk.summary(),
         "device": dev.name,

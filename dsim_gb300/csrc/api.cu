@@ -157,6 +157,7 @@ struct dsim_spins {
              *hscratch = nullptr;
     uint32_t sortNb = 0;        // key grid of the allocated sort buffers
     uint32_t sortEvery = 20;    // steps between reorderings (0 = never)
+    uint64_t launches = 0;      // kernels launched by dsim_mesh_run / dsim_cyl_run on this object
     bool permuted = false;      // slot i does not hold spin i
     float4* cpos = nullptr;     // cylinder layout (lazy)
     uint32_t* cseed = nullptr;  // cylinder layout (lazy)
@@ -504,6 +505,7 @@ static int spins_unpermute(dsim_spins* s) {
     if (!s->permuted) return kOk;
     int rc = launch_unpermute(s->sorted(), s->sorted2(), s->st);
     if (rc) return rc;
+    s->launches += 1;
     s->swap_buffers();
     s->permuted = false;
     return kOk;
@@ -741,6 +743,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
         // reference-grid scan: slot order = spin order
         if ((rc = spins_unpermute(s))) return rc;
         if (a.tested) { set_last_error(kErrInvalid, "entry counting needs the fine grid"); return kErrInvalid; }
+        s->launches += 1;
         return launch_mesh_step(m->dev(), a, s->dev(), kLayoutSoA, rng, s->st);
     }
     // fast path: reorder by fine cell every sortEvery steps
@@ -754,6 +757,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
             if ((rc = launch_sort_spins(s->sorted(), s->sorted2(), s->sortNb, s->keys, s->hist,
                                         s->hstart, s->hscratch, s->st)))
                 return rc;
+            s->launches += 5;  // keys, scan (3), scatter
             s->swap_buffers();
             s->permuted = true;
         }
@@ -769,6 +773,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
             rc = launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
                                        m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
         if (rc) return rc;
+        s->launches += 1;
     }
     return kOk;
 }
@@ -829,6 +834,7 @@ int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const flo
     if (rc) return rc;
     CylSpinsDev S;
     S.pos = s->cpos; S.seed4 = s->cseed; S.mag = s->mag; S.N = s->N;
+    s->launches += 1;
     return launch_cyl_step(c->dev(), a, S, replayDraws ? kRngReplay : kRngPhilox, s->st);
 }
 
@@ -868,6 +874,13 @@ int dsim_timer_stop(dsim_spins* s, float* ms) {
     float v = 0;
     DSIM_CUDA_TRY(cudaEventElapsedTime(&v, s->ev0, s->ev1));
     if (ms) *ms = v;
+    return kOk;
+}
+
+int dsim_spins_launches(dsim_spins* s, uint64_t* n, int reset) {
+    if (!s || !n) { set_last_error(kErrInvalid, "dsim_spins_launches: null argument"); return kErrInvalid; }
+    *n = s->launches;
+    if (reset) s->launches = 0;
     return kOk;
 }
 

@@ -118,6 +118,12 @@ class Spins:
         check(native().dsim_signal(self.h, float(region), out))
         return out.reshape(5, 3)
 
+    def launches(self, reset=False):
+        """Kernels launched by mesh/cylinder runs on this object."""
+        n = C.c_uint64()
+        check(native().dsim_spins_launches(self.h, C.byref(n), int(reset)))
+        return n.value
+
     def sync(self):
         check(native().dsim_sync(self.h))
 

@@ -196,6 +196,10 @@ int dsim_signal_noalloc(const float* pos, const void* spinRecords, uint32_t N, i
 int dsim_rng_draws(uint64_t seed, uint32_t spin0, uint64_t step, uint32_t stream, uint32_t n,
                    uint32_t* raw, float* draws4);
 
+/* number of kernels dsim_mesh_run / dsim_cyl_run launched for this object
+ * (step kernels, spin sorts, reorderings) since the last reset */
+int dsim_spins_launches(dsim_spins* s, uint64_t* n, int reset);
+
 /* stream control and device timing on the object's stream */
 int dsim_sync(dsim_spins* s);
 int dsim_timer_start(dsim_spins* s);
