@@ -123,6 +123,45 @@ def _declare_native(L):
     return L
 
 
+class JobDesc(C.Structure):
+    """dsim_job_desc (include/dsim_batch.h)."""
+    _fields_ = [("substrate", C.c_uint32), ("nSpins", C.c_uint32), ("steps", C.c_uint32),
+                ("deltaTime", C.c_float), ("stepSd", C.c_float * 4), ("T2", C.c_float * 4),
+                ("permeability", C.c_float), ("reflectionType", C.c_uint32), ("spinRadius", C.c_float),
+                ("innerRadiusProportion", C.c_float), ("phaseConstant", C.c_float),
+                ("waveform", C.c_uint32), ("delta", C.c_float), ("Delta", C.c_float),
+                ("frequency", C.c_float), ("table", C.c_void_p), ("seed", C.c_uint64)]
+
+
+def _declare_batch(L):
+    i32, u32, u64 = C.c_int, C.c_uint32, C.c_uint64
+    U64 = _nd(np.uint64, flags="C_CONTIGUOUS")
+    sig = {
+        "dsim_batch_create": (i32, [u64, u32, C.POINTER(VP)]),
+        "dsim_batch_free": (None, [VP]),
+        "dsim_batch_add_mesh": (i32, [VP, VP, C.POINTER(u32)]),
+        "dsim_batch_add_cyl": (i32, [VP, VP, C.POINTER(u32)]),
+        "dsim_batch_submit": (i32, [VP, C.POINTER(JobDesc), F32, U8, OU32, C.POINTER(u32)]),
+        "dsim_batch_configure": (i32, [VP, u32, u32, u32]),
+        "dsim_batch_advance": (i32, [VP, u32]),
+        "dsim_batch_run": (i32, [VP]),
+        "dsim_batch_job_status": (i32, [VP, u32, C.POINTER(u32), C.POINTER(i32)]),
+        "dsim_batch_signal": (i32, [VP, u32, F32, u32, F64]),
+        "dsim_batch_get": (i32, [VP, u32, OF32, OF32, OF32, OU8, OU32]),
+        "dsim_batch_counts": (i32, [VP, u32, U64]),
+        "dsim_batch_status": (u32, [VP]),
+        "dsim_batch_retire": (i32, [VP, u32]),
+        "dsim_batch_compact": (i32, [VP]),
+        "dsim_batch_info": (i32, [VP, U64]),
+        "dsim_batch_sync": (i32, [VP]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
 def _declare_abi3(L):
     i32, u32, f32 = C.c_int, C.c_uint, C.c_float
     sig = {
@@ -199,7 +238,7 @@ _cache = {}
 
 def native():
     if "native" not in _cache:
-        _cache["native"] = _declare_native(_load(NATIVE))
+        _cache["native"] = _declare_batch(_declare_native(_load(NATIVE)))
     return _cache["native"]
 
 

@@ -145,6 +145,26 @@ struct dsim_cyl {
     }
 };
 
+namespace dsim {
+// device views for the batch module (batch.cu)
+int mesh_views(const dsim_mesh* m, MeshDev* g, AccelDev* a) {
+    if (!m || !g || !a) return kErrInvalid;
+    if (m->nf == 0 || !m->acc_recw) {
+        set_last_error(kErrInvalid, "batch: the mesh needs its fine grid with 32-byte records");
+        return kErrInvalid;
+    }
+    *g = m->dev();
+    *a = m->acc();
+    return kOk;
+}
+int cyl_view(const dsim_cyl* c, CylDev* g) {
+    if (!c || !g) return kErrInvalid;
+    *g = c->dev();
+    return kOk;
+}
+int mesh_rebuild_accel(dsim_mesh* m, uint32_t nf) { return accel_build(m, nf); }
+}  // namespace dsim
+
 struct dsim_spins {
     uint32_t N = 0;
     cudaStream_t st = nullptr;

@@ -1,0 +1,919 @@
+// batch.cu -- many simulation jobs advanced by one step launch per chunk
+// (include/dsim_batch.h).
+//
+// Spins of all jobs live in one packed SoA array; job j owns the slot range
+// [slot0_j, slot0_j + pad_j) with pad_j = nSpins rounded up to 32, so every
+// warp belongs to one job and reads that job's substrate and parameters once.
+// Padding slots carry id 0xFFFFFFFF and do no work.  Every chunk the spins
+// are re-sorted by (job, Morton cell of a per-job sort grid) -- the job
+// ranges are preserved because job j's keys follow job j-1's -- and one step
+// kernel advances every running job by up to `chunk` steps.  The chunk loop
+// (sort, step, step-counter advance) is captured in a CUDA graph.
+//
+// Step rules: mesh jobs run the flattened collision round of flat_round.cuh
+// (dSim3/src/spinKernelCpu.cpp:198-499), cylinder jobs the dSim2 rules of
+// cyl_common.cuh (dSim2/src/spinKernelCpu.cpp:312-641).  Draws are Philox with
+// key = job seed and counter = (spin index in the job, job step, 0), the same
+// as dsim_mesh_run / dsim_cyl_run with that seed.  Instead of the reference's
+// float phase (dSim3/src/spinKernelCpu.cpp:490) each spin accumulates the
+// gradient moment M = sum w(t) pos(t) with Kahan compensation; the phase of any
+// gradient sharing the waveform is phaseConstant * (g . M), in FP64 at readout.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#pragma GCC visibility push(default)
+#include "../../include/dsim_batch.h"
+#pragma GCC visibility pop
+#include "common.cuh"
+#include "cyl_common.cuh"
+#include "engine.h"
+#include "flat_round.cuh"
+
+namespace dsim {
+
+enum SubKind : uint32_t { kSubMesh = 0, kSubCyl = 1 };
+struct SubDev {
+    uint32_t kind;
+    MeshDev g;
+    AccelDev acc;
+    CylDev c;
+};
+
+struct JobDev {
+    uint32_t sub, steps, start;  // substrate, total steps, global step of the job's step 0
+    uint32_t sortBase, sortBits;  // first sort key, Morton bits per axis of the sort grid
+    float sd[4], T2[4];
+    float perm, dt, clampHi, clampLo;
+    uint32_t reflType, maxSub;
+    float inR;                    // cylinders: (inner radius proportion)^2
+    const float* wave;            // w[steps]
+    uint32_t key0, key1;
+};
+
+// packed spin state; meta = compartment | fiber << 8 (cylinders: imo | nearest << 8)
+static constexpr int kBF = 10;  // float fields: x y z mx my mz cx cy cz mag
+static constexpr int kBU = 3;   // uint fields: meta job id
+struct BatchSpins {
+    float* f[kBF];
+    uint32_t* u[kBU];
+    uint32_t N;
+};
+enum { F_X, F_Y, F_Z, F_MX, F_MY, F_MZ, F_CX, F_CY, F_CZ, F_MAG };
+enum { U_META, U_JOB, U_ID };
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(kFlatThreads, MINB)
+k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
+             const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
+             unsigned long long* jobCounts) {
+    __shared__ FlatWarp wh[kFlatWarps];
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    FlatWarp& H = wh[threadIdx.x >> 5];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
+    const uint32_t jb = S.u[U_JOB][i & ~31u];
+    const JobDev& J = jobs[jb];
+    const uint32_t now = *stepNow;
+    const uint32_t start = J.start, steps = J.steps;
+    if (now < start || now - start >= steps) return;  // not started or finished (warp-uniform)
+    const uint32_t ls0 = now - start;
+    const uint32_t nsteps = min(chunk, steps - ls0);
+    const uint32_t id = S.u[U_ID][i];
+    const bool valid = id != 0xFFFFFFFFu;
+    float x = S.f[F_X][i], y = S.f[F_Y][i], z = S.f[F_Z][i];
+    float mx = S.f[F_MX][i], my = S.f[F_MY][i], mz = S.f[F_MZ][i];
+    float cx = S.f[F_CX][i], cy = S.f[F_CY][i], cz = S.f[F_CZ][i];
+    float mag = S.f[F_MAG][i];
+    const uint32_t meta = S.u[U_META][i];
+    uint32_t comp = meta & 0xFFu, fiber = meta >> 8;
+    const uint32_t k0 = J.key0, k1 = J.key1;
+    const float* __restrict__ wave = J.wave;
+    uint32_t nrefl = 0, nperm = 0, st = 0;
+    const SubDev& sub = subs[J.sub];
+    if (sub.kind == kSubMesh) {
+        const MeshDev g = sub.g;
+        const AccelDev acc = sub.acc;
+        const float perm = J.perm;
+        const uint32_t reflType = J.reflType, maxSub = J.maxSub;
+        uint32_t it = 0;
+        bool active = valid && nsteps > 0;
+        bool fresh = active;
+        Draw d;
+        d.nx = d.ny = d.nz = 0.0f; d.u = 1.0f;
+        float ox = x, oy = y, oz = z, px = x, py = y, pz = z;
+        uint32_t excluded = 0xFFFFFFFFu, sub_n = 0;
+        float umax = 1.0f, umin = 0.0f;
+        while (__any_sync(FULL, active)) {
+            if (fresh) {
+                d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+                ox = x; oy = y; oz = z;
+                const float sd = J.sd[comp & 3u];
+                px = x + d.nx * sd; py = y + d.ny * sd; pz = z + d.nz * sd;
+                excluded = 0xFFFFFFFFu;
+                umax = 1.0f; umin = 0.0f;
+                sub_n = 0;
+                fresh = false;
+            }
+            const bool open = active;
+            bool found;
+            FastHit best;
+            flat_round(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
+            if (open) {
+                bool finish = !found;
+                if (found) {
+                    apply_hit(g, best, d.u, perm, reflType, umax, umin, ox, oy, oz, px, py, pz, comp, fiber,
+                              excluded, nrefl, nperm);
+                    if (++sub_n >= maxSub) {
+                        st |= kStatusSubsegCap;
+                        px = ox; py = oy; pz = oz;
+                        finish = true;
+                    }
+                }
+                if (finish) {
+                    float ex = px, ey = py, ez = pz;
+                    if (ex > J.clampHi) ex = J.clampHi; else if (ex < J.clampLo) ex = J.clampLo;
+                    if (ey > J.clampHi) ey = J.clampHi; else if (ey < J.clampLo) ey = J.clampLo;
+                    if (ez > J.clampHi) ez = J.clampHi; else if (ez < J.clampLo) ez = J.clampLo;
+                    x = ex; y = ey; z = ez;
+                    const float T2 = J.T2[comp & 3u];
+                    if (T2 > 0.0f) mag += -mag / T2 * J.dt;
+                    const float w = __ldg(wave + ls0 + it);
+                    kahan_add(mx, cx, w * x);
+                    kahan_add(my, cy, w * y);
+                    kahan_add(mz, cz, w * z);
+                    if (++it >= nsteps) active = false;
+                    else fresh = true;
+                }
+            }
+            __syncwarp();
+        }
+    } else if (valid) {
+        const CylDev g = sub.c;
+        const float perm = J.perm, inR = J.inR;
+        uint32_t imo = comp, nearest = fiber;
+        if (imo < 2 && nearest >= g.nF) imo = 2;
+        for (uint32_t it = 0; it < nsteps; it++) {
+            const Draw d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+            const float ox = x, oy = y, oz = z;
+            const float sdv = J.sd[imo];
+            float px = x + d.nx * sdv, py = y + d.ny * sdv, pz = z + d.nz * sdv;
+            if (perm < 1.0f) cyl_membranes(g, ox, oy, oz, px, py, pz, d.u, perm, inR, imo, nearest, nrefl, nperm, st);
+            if (px > J.clampHi) px = J.clampHi; else if (px < J.clampLo) px = J.clampLo;
+            if (py > J.clampHi) py = J.clampHi; else if (py < J.clampLo) py = J.clampLo;
+            if (pz > J.clampHi) pz = J.clampHi; else if (pz < J.clampLo) pz = J.clampLo;
+            x = px; y = py; z = pz;
+            const float T2 = J.T2[imo];
+            if (T2 > 0.0f) mag += -mag / T2 * J.dt;
+            const float w = __ldg(wave + ls0 + it);
+            kahan_add(mx, cx, w * x);
+            kahan_add(my, cy, w * y);
+            kahan_add(mz, cz, w * z);
+        }
+        comp = imo;
+        fiber = nearest & 0xFFFFFFu;
+    }
+    if (valid) {
+        S.f[F_X][i] = x; S.f[F_Y][i] = y; S.f[F_Z][i] = z;
+        S.f[F_MX][i] = mx; S.f[F_MY][i] = my; S.f[F_MZ][i] = mz;
+        S.f[F_CX][i] = cx; S.f[F_CY][i] = cy; S.f[F_CZ][i] = cz;
+        S.f[F_MAG][i] = mag;
+        S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
+    }
+    // per-job counters: one atomic per warp
+    unsigned long long r = nrefl, p = nperm;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        p += __shfl_down_sync(FULL, p, o);
+    }
+    if (lane == 0 && (r | p)) {
+        atomicAdd(jobCounts + 2 * jb, r);
+        atomicAdd(jobCounts + 2 * jb + 1, p);
+    }
+    if (st) atomicOr(status, st);
+}
+
+__global__ void k_batch_advance(uint32_t* stepNow, uint32_t chunk) { *stepNow += chunk; }
+
+// sort key: job's base + Morton code of the spin's cell in a 2^bits grid
+// over the box; padding goes to the job's last key
+__global__ void k_batch_keys(const JobDev* __restrict__ jobs, BatchSpins S, uint32_t* keys,
+                             uint32_t* hist) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    const JobDev& J = jobs[S.u[U_JOB][i]];
+    const uint32_t bits = J.sortBits, n = 1u << bits;
+    uint32_t key;
+    if (S.u[U_ID][i] == 0xFFFFFFFFu) {
+        key = J.sortBase + (1u << (3 * bits)) - 1u;
+    } else {
+        const float s = 0.5f * (float)n;
+        uint32_t a = (uint32_t)fminf(fmaxf(floorf((S.f[F_X][i] + 1.0f) * s), 0.0f), (float)(n - 1));
+        uint32_t b = (uint32_t)fminf(fmaxf(floorf((S.f[F_Y][i] + 1.0f) * s), 0.0f), (float)(n - 1));
+        uint32_t c = (uint32_t)fminf(fmaxf(floorf((S.f[F_Z][i] + 1.0f) * s), 0.0f), (float)(n - 1));
+        key = J.sortBase + morton3(a, b, c);
+    }
+    keys[i] = key;
+    atomicAdd(hist + key, 1u);
+}
+
+__global__ void k_batch_scatter(BatchSpins S, BatchSpins D, const uint32_t* __restrict__ keys,
+                                const uint32_t* __restrict__ start, uint32_t* cursor) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    const uint32_t k = keys[i];
+    const uint32_t j = start[k] + atomicAdd(cursor + k, 1u);
+#pragma unroll
+    for (int f = 0; f < kBF; f++) D.f[f][j] = S.f[f][i];
+#pragma unroll
+    for (int u = 0; u < kBU; u++) D.u[u][j] = S.u[u][i];
+}
+
+// compaction: slot i of a kept job moves to remapped slot; job index remapped
+__global__ void k_batch_compact(BatchSpins S, BatchSpins D, const int32_t* __restrict__ jobMap,
+                                const int64_t* __restrict__ slotShift) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= S.N) return;
+    const uint32_t jb = S.u[U_JOB][i];
+    const int32_t nj = jobMap[jb];
+    if (nj < 0) return;
+    const uint32_t j = (uint32_t)((int64_t)i + slotShift[jb]);
+#pragma unroll
+    for (int f = 0; f < kBF; f++) D.f[f][j] = S.f[f][i];
+    D.u[U_META][j] = S.u[U_META][i];
+    D.u[U_JOB][j] = (uint32_t)nj;
+    D.u[U_ID][j] = S.u[U_ID][i];
+}
+
+// a job's spins in spin order
+__global__ void k_batch_gather(BatchSpins S, uint32_t slot0, uint32_t len, float* pos3, float* mag,
+                               float* mom6, uint32_t* meta) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    const uint32_t i = slot0 + k;
+    const uint32_t id = S.u[U_ID][i];
+    if (id == 0xFFFFFFFFu) return;
+    pos3[3 * id] = S.f[F_X][i]; pos3[3 * id + 1] = S.f[F_Y][i]; pos3[3 * id + 2] = S.f[F_Z][i];
+    mag[id] = S.f[F_MAG][i];
+    mom6[6 * id] = S.f[F_MX][i]; mom6[6 * id + 1] = S.f[F_MY][i]; mom6[6 * id + 2] = S.f[F_MZ][i];
+    mom6[6 * id + 3] = S.f[F_CX][i]; mom6[6 * id + 4] = S.f[F_CY][i]; mom6[6 * id + 5] = S.f[F_CZ][i];
+    meta[id] = S.u[U_META][i];
+}
+
+// FP64 signal of one job for nG gradients: partial records per (block, g)
+static constexpr int kSigThreads = 256;
+__global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint32_t slot0, uint32_t len,
+                                                              const double* __restrict__ kg, uint32_t nG,
+                                                              double* partials) {
+    __shared__ double sh[kSigThreads / 32][15];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t gi = 0; gi < nG; gi++) {
+        const double gx = kg[3 * gi], gy = kg[3 * gi + 1], gz = kg[3 * gi + 2];
+        double acc[15];
+#pragma unroll
+        for (int k = 0; k < 15; k++) acc[k] = 0.0;
+        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
+            const uint32_t i = slot0 + k;
+            if (S.u[U_ID][i] == 0xFFFFFFFFu) continue;
+            const double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
+            const double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
+            const double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
+            const double ph = gx * Mx + gy * My + gz * Mz;
+            const double m = S.f[F_MAG][i];
+            double s, c;
+            sincos(ph, &s, &c);
+            const double X = m * c, Y = m * s;
+            const uint32_t comp = S.u[U_META][i] & 3u;
+            acc[0] += X; acc[1] += Y; acc[2] += 1.0;
+#pragma unroll
+            for (uint32_t q = 0; q < 4; q++) {
+                const bool on = comp == q;
+                acc[3 + 3 * q] += on ? X : 0.0;
+                acc[4 + 3 * q] += on ? Y : 0.0;
+                acc[5 + 3 * q] += on ? 1.0 : 0.0;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 15; k++) {
+            double v = acc[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+            if (lane == 0) sh[w][k] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 15) {
+            double v = 0.0;
+            for (int j = 0; j < kSigThreads / 32; j++) v += sh[j][threadIdx.x];
+            partials[((size_t)blockIdx.x * nG + gi) * 15 + threadIdx.x] = v;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_signal_final(const double* __restrict__ partials, uint32_t nb, uint32_t nG,
+                                     double* out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nG * 15) return;
+    double v = 0.0;
+    for (uint32_t b = 0; b < nb; b++) v += partials[(size_t)b * nG * 15 + t];
+    out[t] = v;
+}
+
+}  // namespace dsim
+
+using namespace dsim;
+
+struct BatchBuf {
+    float* f[kBF] = {};
+    uint32_t* u[kBU] = {};
+};
+
+struct BatchJob {
+    uint32_t id;            // public job id
+    JobDev d;
+    uint32_t nSpins, pad;
+    uint64_t slot0;
+    float* wave = nullptr;  // device table
+    double pc = 0.0;        // phase constant 2 pi gamma dt
+    bool retired = false;
+    uint64_t counts[2] = {0, 0};
+};
+
+struct dsim_batch {
+    cudaStream_t st = nullptr;
+    uint64_t cap = 0;
+    uint32_t jobCap = 0;
+    BatchBuf buf[2];
+    int cur = 0;
+    uint64_t N = 0;
+    std::vector<SubDev> subs;
+    std::vector<const dsim_mesh*> meshes;  // per substrate (null for cylinders)
+    SubDev* d_subs = nullptr;
+    uint32_t subCap = 256;
+    std::vector<BatchJob> jobs;            // packing order
+    uint32_t nextId = 0;
+    JobDev* d_jobs = nullptr;
+    unsigned long long* d_counts = nullptr;
+    uint32_t* d_status = nullptr;
+    uint32_t* d_stepNow = nullptr;
+    uint32_t stepNow = 0;                  // host mirror of *d_stepNow
+    uint32_t* keys = nullptr;
+    uint32_t *hist = nullptr, *hstart = nullptr, *scratch = nullptr;
+    uint64_t keyCap = 0, K = 0;
+    uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
+    cudaGraphExec_t exec = nullptr;
+    bool graphValid = false;
+    int graphCur = -1;
+    uint64_t launches = 0, graphLaunches = 0, bytes = 0;
+};
+
+namespace {
+
+int balloc(dsim_batch* b, void** p, size_t bytes) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_last_error(kErrNoMem, "batch: cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+        return kErrNoMem;
+    }
+    b->bytes += bytes;
+    return kOk;
+}
+
+BatchSpins view(dsim_batch* b, int which) {
+    BatchSpins S;
+    for (int f = 0; f < kBF; f++) S.f[f] = b->buf[which].f[f];
+    for (int u = 0; u < kBU; u++) S.u[u] = b->buf[which].u[u];
+    S.N = (uint32_t)b->N;
+    return S;
+}
+
+uint32_t sort_bits(uint32_t n) {
+    // about two spins per sort cell: 2^(3 bits) ~ n / 2, 3..7 bits per axis
+    uint32_t bits = 3;
+    while (bits < 7 && (1ull << (3 * (bits + 1))) <= (uint64_t)n / 2) bits++;
+    return bits;
+}
+
+void invalidate_graph(dsim_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+    b->graphValid = false;
+}
+
+// recompute sort key bases in packing order and grow the histogram
+int layout_keys(dsim_batch* b) {
+    uint64_t K = 0, slot = 0;
+    for (auto& j : b->jobs) {
+        j.d.sortBase = (uint32_t)K;
+        K += 1ull << (3 * j.d.sortBits);
+        j.slot0 = slot;
+        slot += j.pad;
+    }
+    if (K > 0xFFFFFFF0ull) { set_last_error(kErrTooLarge, "batch: sort key space too large"); return kErrTooLarge; }
+    if (K > b->keyCap) {
+        cudaFree(b->hist); cudaFree(b->hstart); cudaFree(b->scratch);
+        b->hist = b->hstart = b->scratch = nullptr;
+        uint64_t cap = std::max<uint64_t>(K, 1u << 16) * 2;
+        int rc;
+        if ((rc = balloc(b, (void**)&b->hist, cap * 4)) || (rc = balloc(b, (void**)&b->hstart, (cap + 1) * 4)) ||
+            (rc = balloc(b, (void**)&b->scratch, scan_scratch_words((uint32_t)cap) * 4)))
+            return rc;
+        b->keyCap = cap;
+    }
+    b->K = K;
+    return kOk;
+}
+
+int upload_jobs(dsim_batch* b) {
+    std::vector<JobDev> h(b->jobs.size());
+    for (size_t k = 0; k < b->jobs.size(); k++) h[k] = b->jobs[k].d;
+    if (!h.empty()) DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_jobs, h.data(), h.size() * sizeof(JobDev), cudaMemcpyHostToDevice, b->st));
+    return kOk;
+}
+
+// one chunk: sort into the other buffer, step, advance the step counter
+int enqueue_chunk(dsim_batch* b) {
+    const uint32_t N = (uint32_t)b->N;
+    const uint32_t nb = (N + 255) / 256;
+    BatchSpins S = view(b, b->cur), D = view(b, 1 - b->cur);
+    DSIM_CUDA_TRY(cudaMemsetAsync(b->hist, 0, b->K * 4, b->st));
+    k_batch_keys<<<nb, 256, 0, b->st>>>(b->d_jobs, S, b->keys, b->hist);
+    int rc = launch_scan_exclusive(b->hist, b->hstart, (uint32_t)b->K, b->scratch, b->st);
+    if (rc) return rc;
+    DSIM_CUDA_TRY(cudaMemsetAsync(b->hist, 0, b->K * 4, b->st));
+    k_batch_scatter<<<nb, 256, 0, b->st>>>(S, D, b->keys, b->hstart, b->hist);
+    b->cur = 1 - b->cur;
+    const uint32_t grid = (N + kFlatThreads - 1) / kFlatThreads;
+    if (b->occupancy >= 8)
+        k_batch_step<8><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+    else if (b->occupancy >= 6)
+        k_batch_step<6><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+    else
+        k_batch_step<4><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+    k_batch_advance<<<1, 1, 0, b->st>>>(b->d_stepNow, b->chunk);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    b->launches += 7;  // keys, scan (3), scatter, step, advance
+    return kOk;
+}
+
+int capture_graph(dsim_batch* b) {
+    invalidate_graph(b);
+    const uint32_t G = b->graphChunks & ~1u;  // even: the buffers end where they start
+    if (G == 0) return kOk;
+    const int cur0 = b->cur;
+    const uint64_t launches0 = b->launches;
+    cudaGraph_t graph = nullptr;
+    DSIM_CUDA_TRY(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    int rc = kOk;
+    for (uint32_t c = 0; c < G && !rc; c++) rc = enqueue_chunk(b);
+    cudaError_t e = cudaStreamEndCapture(b->st, &graph);
+    b->cur = cur0;
+    b->launches = launches0;
+    if (rc) { if (graph) cudaGraphDestroy(graph); return rc; }
+    if (e != cudaSuccess) { set_last_cuda_error(e, "cudaStreamEndCapture", __FILE__, __LINE__); return kErrCuda; }
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { b->exec = nullptr; set_last_cuda_error(e, "cudaGraphInstantiate", __FILE__, __LINE__); return kErrCuda; }
+    b->graphValid = true;
+    b->graphCur = cur0;
+    return kOk;
+}
+
+bool job_finished(const dsim_batch* b, const BatchJob& j) {
+    return b->stepNow >= j.d.start && b->stepNow - j.d.start >= j.d.steps;
+}
+
+BatchJob* find_job(dsim_batch* b, uint32_t id) {
+    for (auto& j : b->jobs)
+        if (j.id == id) return &j;
+    return nullptr;
+}
+
+constexpr double kPi = 3.14159265358979323846;
+
+std::vector<float> make_wave(const dsim_job_desc* d) {
+    std::vector<float> w(d->steps, 0.0f);
+    if (d->waveform == DSIM_WAVE_TABLE) {
+        for (uint32_t s = 0; s < d->steps; s++) w[s] = d->table[s];
+        return w;
+    }
+    const long nd = lround((double)d->delta / (double)d->deltaTime);
+    const long nD = lround((double)d->Delta / (double)d->deltaTime);
+    for (uint32_t s = 0; s < d->steps; s++) {
+        const long t = (long)s;
+        if (t < nd) {
+            w[s] = d->waveform == DSIM_WAVE_OGSE
+                       ? (float)std::cos(2.0 * kPi * (double)d->frequency * 1e-3 * (double)t * (double)d->deltaTime)
+                       : 1.0f;
+        } else if (t >= nD && t < nD + nd) {
+            w[s] = d->waveform == DSIM_WAVE_OGSE
+                       ? -(float)std::cos(2.0 * kPi * (double)d->frequency * 1e-3 * (double)(t - nD) * (double)d->deltaTime)
+                       : -1.0f;
+        }
+    }
+    return w;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** out) {
+    if (!out || spinCapacity == 0 || jobCapacity == 0 || spinCapacity > 0xFFFFFFE0ull) {
+        set_last_error(kErrInvalid, "dsim_batch_create: bad argument");
+        return kErrInvalid;
+    }
+    *out = nullptr;
+    dsim_batch* b = new dsim_batch();
+    b->cap = (spinCapacity + 31) & ~31ull;
+    b->jobCap = jobCapacity;
+    int rc = kOk;
+    if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) rc = kErrCuda;
+    for (int k = 0; k < 2 && !rc; k++) {
+        for (int f = 0; f < kBF && !rc; f++) rc = balloc(b, (void**)&b->buf[k].f[f], b->cap * 4);
+        for (int u = 0; u < kBU && !rc; u++) rc = balloc(b, (void**)&b->buf[k].u[u], b->cap * 4);
+    }
+    if (!rc) rc = balloc(b, (void**)&b->keys, b->cap * 4);
+    if (!rc) rc = balloc(b, (void**)&b->d_jobs, (size_t)jobCapacity * sizeof(JobDev));
+    if (!rc) rc = balloc(b, (void**)&b->d_subs, (size_t)b->subCap * sizeof(SubDev));
+    if (!rc) rc = balloc(b, (void**)&b->d_counts, (size_t)2 * jobCapacity * 8);
+    if (!rc) rc = balloc(b, (void**)&b->d_status, 4);
+    if (!rc) rc = balloc(b, (void**)&b->d_stepNow, 4);
+    if (!rc && (cudaMemset(b->d_status, 0, 4) != cudaSuccess || cudaMemset(b->d_stepNow, 0, 4) != cudaSuccess ||
+                cudaMemset(b->d_counts, 0, (size_t)2 * jobCapacity * 8) != cudaSuccess))
+        rc = kErrCuda;
+    if (rc) { dsim_batch_free(b); return rc; }
+    *out = b;
+    return kOk;
+}
+
+void dsim_batch_free(dsim_batch* b) {
+    if (!b) return;
+    if (b->st) cudaStreamSynchronize(b->st);
+    invalidate_graph(b);
+    for (int k = 0; k < 2; k++) {
+        for (int f = 0; f < kBF; f++) cudaFree(b->buf[k].f[f]);
+        for (int u = 0; u < kBU; u++) cudaFree(b->buf[k].u[u]);
+    }
+    for (auto& j : b->jobs) cudaFree(j.wave);
+    cudaFree(b->keys); cudaFree(b->hist); cudaFree(b->hstart); cudaFree(b->scratch);
+    cudaFree(b->d_jobs); cudaFree(b->d_subs); cudaFree(b->d_counts); cudaFree(b->d_status);
+    cudaFree(b->d_stepNow);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+}
+
+static int add_sub(dsim_batch* b, const SubDev& s, const dsim_mesh* m, uint32_t* id) {
+    if (b->subs.size() >= b->subCap) { set_last_error(kErrTooLarge, "batch: too many substrates"); return kErrTooLarge; }
+    b->subs.push_back(s);
+    b->meshes.push_back(m);
+    DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_subs + (b->subs.size() - 1), &s, sizeof(SubDev), cudaMemcpyHostToDevice, b->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    *id = (uint32_t)(b->subs.size() - 1);
+    return kOk;
+}
+
+int dsim_batch_add_mesh(dsim_batch* b, const dsim_mesh* m, uint32_t* substrate) {
+    if (!b || !m || !substrate) { set_last_error(kErrInvalid, "dsim_batch_add_mesh: null argument"); return kErrInvalid; }
+    SubDev s;
+    memset(&s, 0, sizeof(s));
+    s.kind = kSubMesh;
+    int rc = mesh_views(m, &s.g, &s.acc);
+    if (rc) return rc;
+    return add_sub(b, s, m, substrate);
+}
+
+int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate) {
+    if (!b || !c || !substrate) { set_last_error(kErrInvalid, "dsim_batch_add_cyl: null argument"); return kErrInvalid; }
+    SubDev s;
+    memset(&s, 0, sizeof(s));
+    s.kind = kSubCyl;
+    int rc = cyl_view(c, &s.c);
+    if (rc) return rc;
+    return add_sub(b, s, nullptr, substrate);
+}
+
+int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, const uint8_t* comp,
+                      const uint32_t* fiber, uint32_t* jobId) {
+    if (!b || !d || !pos3 || !comp || !jobId || d->nSpins == 0 || d->steps == 0 || d->substrate >= b->subs.size() ||
+        !(d->deltaTime > 0.0f) || (d->waveform == DSIM_WAVE_TABLE && !d->table) || d->waveform > DSIM_WAVE_TABLE) {
+        set_last_error(kErrInvalid, "dsim_batch_submit: bad argument");
+        return kErrInvalid;
+    }
+    const uint32_t pad = (d->nSpins + 31u) & ~31u;
+    if (b->N + pad > b->cap || b->jobs.size() >= b->jobCap) {
+        set_last_error(kErrNoMem, "dsim_batch_submit: batch full (%llu + %u spins of %llu, %zu jobs of %u)",
+                       (unsigned long long)b->N, pad, (unsigned long long)b->cap, b->jobs.size(), b->jobCap);
+        return kErrNoMem;
+    }
+    const bool cyl = b->subs[d->substrate].kind == kSubCyl;
+    BatchJob j;
+    j.id = b->nextId;
+    j.nSpins = d->nSpins;
+    j.pad = pad;
+    j.pc = (double)d->phaseConstant;
+    JobDev& J = j.d;
+    memset(&J, 0, sizeof(J));
+    J.sub = d->substrate;
+    J.steps = d->steps;
+    J.start = b->stepNow;
+    J.sortBits = sort_bits(d->nSpins);
+    for (int k = 0; k < 4; k++) { J.sd[k] = d->stepSd[k]; J.T2[k] = d->T2[k]; }
+    J.perm = d->permeability;
+    J.dt = d->deltaTime;
+    J.clampHi = 1.0f - d->spinRadius;
+    J.clampLo = -1.0f + d->spinRadius;
+    J.reflType = d->reflectionType;
+    J.maxSub = 4096;
+    J.inR = d->innerRadiusProportion * d->innerRadiusProportion;
+    J.key0 = (uint32_t)d->seed;
+    J.key1 = (uint32_t)(d->seed >> 32);
+    std::vector<float> w = make_wave(d);
+    int rc = balloc(b, (void**)&j.wave, w.size() * 4);
+    if (rc) return rc;
+    J.wave = j.wave;
+    if (!J.wave || w.size() < J.steps) {
+        cudaFree(j.wave);
+        set_last_error(kErrInvalid, "dsim_batch_submit: waveform table missing");
+        return kErrInvalid;
+    }
+    if (cudaMemcpyAsync(j.wave, w.data(), w.size() * 4, cudaMemcpyHostToDevice, b->st) != cudaSuccess) {
+        cudaFree(j.wave);
+        set_last_error(kErrCuda, "dsim_batch_submit: waveform upload");
+        return kErrCuda;
+    }
+    // host staging of the packed slots [N, N + pad)
+    std::vector<float> hf[kBF];
+    std::vector<uint32_t> hu[kBU];
+    for (int f = 0; f < kBF; f++) hf[f].assign(pad, 0.0f);
+    for (int u = 0; u < kBU; u++) hu[u].assign(pad, 0u);
+    const uint32_t jobIndex = (uint32_t)b->jobs.size();
+    for (uint32_t k = 0; k < pad; k++) {
+        hu[U_JOB][k] = jobIndex;
+        if (k < d->nSpins) {
+            hf[F_X][k] = pos3[3 * k]; hf[F_Y][k] = pos3[3 * k + 1]; hf[F_Z][k] = pos3[3 * k + 2];
+            hf[F_MAG][k] = 1.0f;
+            uint32_t fb = fiber ? fiber[k] : 0xFFFFFFFFu;
+            fb = cyl ? (fb & 0xFFFFFFu) : (fb & 0xFFFFu);
+            hu[U_META][k] = (uint32_t)comp[k] | (fb << 8);
+            hu[U_ID][k] = k;
+        } else {
+            hu[U_ID][k] = 0xFFFFFFFFu;
+        }
+    }
+    for (int f = 0; f < kBF; f++)
+        DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].f[f] + b->N, hf[f].data(), (size_t)pad * 4, cudaMemcpyHostToDevice, b->st));
+    for (int u = 0; u < kBU; u++)
+        DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].u[u] + b->N, hu[u].data(), (size_t)pad * 4, cudaMemcpyHostToDevice, b->st));
+    b->jobs.push_back(j);
+    b->nextId++;
+    b->N += pad;
+    if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
+    DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 2 * jobIndex, 0, 16, b->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    invalidate_graph(b);
+    *jobId = j.id;
+    return kOk;
+}
+
+int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint32_t graphChunks) {
+    if (!b || chunk == 0 || (occupancy != 4 && occupancy != 6 && occupancy != 8)) {
+        set_last_error(kErrInvalid, "dsim_batch_configure: chunk > 0, occupancy 4, 6 or 8");
+        return kErrInvalid;
+    }
+    b->chunk = chunk;
+    b->occupancy = occupancy;
+    b->graphChunks = graphChunks;
+    invalidate_graph(b);
+    return kOk;
+}
+
+static uint32_t remaining_steps(const dsim_batch* b) {
+    uint32_t r = 0;
+    for (const auto& j : b->jobs) {
+        if (j.retired || job_finished(b, j)) continue;
+        uint32_t left = j.d.steps - (b->stepNow - j.d.start);
+        r = std::max(r, left);
+    }
+    return r;
+}
+
+int dsim_batch_advance(dsim_batch* b, uint32_t steps) {
+    if (!b) return kErrInvalid;
+    if (b->N == 0 || steps == 0) return kOk;
+    uint32_t chunks = (steps + b->chunk - 1) / b->chunk;
+    const uint32_t G = b->graphChunks & ~1u;
+    while (chunks > 0) {
+        if (G > 0 && chunks >= G) {
+            if (!b->graphValid || b->graphCur != b->cur) {
+                int rc = capture_graph(b);
+                if (rc) return rc;
+            }
+            DSIM_CUDA_TRY(cudaGraphLaunch(b->exec, b->st));
+            b->graphLaunches++;
+            b->launches += 7ull * G;
+            b->stepNow += G * b->chunk;
+            chunks -= G;
+        } else {
+            int rc = enqueue_chunk(b);
+            if (rc) return rc;
+            b->stepNow += b->chunk;
+            chunks--;
+        }
+    }
+    return kOk;
+}
+
+int dsim_batch_run(dsim_batch* b) {
+    if (!b) return kErrInvalid;
+    uint32_t left = remaining_steps(b);
+    int rc = dsim_batch_advance(b, left);
+    if (rc) return rc;
+    DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    return kOk;
+}
+
+int dsim_batch_job_status(dsim_batch* b, uint32_t jobId, uint32_t* stepsDone, int* done) {
+    BatchJob* j = b ? find_job(b, jobId) : nullptr;
+    if (!j) { set_last_error(kErrInvalid, "dsim_batch_job_status: unknown job %u", jobId); return kErrInvalid; }
+    uint32_t s = b->stepNow >= j->d.start ? std::min(b->stepNow - j->d.start, j->d.steps) : 0u;
+    if (stepsDone) *stepsDone = s;
+    if (done) *done = s >= j->d.steps ? 1 : 0;
+    return kOk;
+}
+
+int dsim_batch_signal(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG, double* out) {
+    BatchJob* j = b ? find_job(b, jobId) : nullptr;
+    if (!j || !gradScaled || !out || nG == 0) { set_last_error(kErrInvalid, "dsim_batch_signal: bad argument"); return kErrInvalid; }
+    const uint32_t nb = std::min<uint32_t>(608u, (j->pad + kSigThreads * 4 - 1) / (kSigThreads * 4));
+    std::vector<double> kg(3 * (size_t)nG);
+    // phase = phaseConstant * (g . M); the job keeps phaseConstant in its descriptor
+    for (uint32_t g = 0; g < nG; g++)
+        for (int c = 0; c < 3; c++) kg[3 * g + c] = j->pc * (double)gradScaled[3 * g + c];
+    double *dk = nullptr, *dp = nullptr, *dout = nullptr;
+    int rc;
+    if ((rc = balloc(b, (void**)&dk, kg.size() * 8)) || (rc = balloc(b, (void**)&dp, (size_t)nb * nG * 15 * 8)) ||
+        (rc = balloc(b, (void**)&dout, (size_t)nG * 15 * 8))) {
+        cudaFree(dk); cudaFree(dp); cudaFree(dout);
+        return rc;
+    }
+    b->bytes -= kg.size() * 8 + (size_t)nb * nG * 15 * 8 + (size_t)nG * 15 * 8;
+    cudaError_t e = cudaMemcpyAsync(dk, kg.data(), kg.size() * 8, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) {
+        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, dp);
+        k_batch_signal_final<<<(nG * 15 + 127) / 128, 128, 0, b->st>>>(dp, nb, nG, dout);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)nG * 15 * 8, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    cudaFree(dk); cudaFree(dp); cudaFree(dout);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_batch_signal", __FILE__, __LINE__); return kErrCuda; }
+    return kOk;
+}
+
+int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float* moments6, uint8_t* compartment,
+                   uint32_t* fiber) {
+    BatchJob* j = b ? find_job(b, jobId) : nullptr;
+    if (!j) { set_last_error(kErrInvalid, "dsim_batch_get: unknown job %u", jobId); return kErrInvalid; }
+    const uint32_t n = j->nSpins;
+    float *dp = nullptr, *dm = nullptr, *dmo = nullptr;
+    uint32_t* dme = nullptr;
+    int rc;
+    if ((rc = balloc(b, (void**)&dp, (size_t)n * 12)) || (rc = balloc(b, (void**)&dm, (size_t)n * 4)) ||
+        (rc = balloc(b, (void**)&dmo, (size_t)n * 24)) || (rc = balloc(b, (void**)&dme, (size_t)n * 4))) {
+        cudaFree(dp); cudaFree(dm); cudaFree(dmo); cudaFree(dme);
+        return rc;
+    }
+    b->bytes -= (size_t)n * 44;
+    k_batch_gather<<<(j->pad + 255) / 256, 256, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dp, dm, dmo, dme);
+    cudaError_t e = cudaGetLastError();
+    std::vector<float> hp(3 * (size_t)n), hm(n), hmo(6 * (size_t)n);
+    std::vector<uint32_t> hme(n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), dp, (size_t)n * 12, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), dm, (size_t)n * 4, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hmo.data(), dmo, (size_t)n * 24, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hme.data(), dme, (size_t)n * 4, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    cudaFree(dp); cudaFree(dm); cudaFree(dmo); cudaFree(dme);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_batch_get", __FILE__, __LINE__); return kErrCuda; }
+    if (pos3) memcpy(pos3, hp.data(), hp.size() * 4);
+    if (mag) memcpy(mag, hm.data(), hm.size() * 4);
+    if (moments6) memcpy(moments6, hmo.data(), hmo.size() * 4);
+    for (uint32_t k = 0; k < n; k++) {
+        if (compartment) compartment[k] = (uint8_t)(hme[k] & 0xFFu);
+        if (fiber) fiber[k] = hme[k] >> 8;
+    }
+    return kOk;
+}
+
+int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]) {
+    if (!b || !counts) return kErrInvalid;
+    for (size_t k = 0; k < b->jobs.size(); k++) {
+        if (b->jobs[k].id != jobId) continue;
+        unsigned long long c[2];
+        DSIM_CUDA_TRY(cudaMemcpyAsync(c, b->d_counts + 2 * k, 16, cudaMemcpyDeviceToHost, b->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+        counts[0] = c[0]; counts[1] = c[1];
+        return kOk;
+    }
+    set_last_error(kErrInvalid, "dsim_batch_counts: unknown job %u", jobId);
+    return kErrInvalid;
+}
+
+uint32_t dsim_batch_status(dsim_batch* b) {
+    if (!b) return 0;
+    uint32_t s = 0;
+    if (cudaMemcpyAsync(&s, b->d_status, 4, cudaMemcpyDeviceToHost, b->st) != cudaSuccess ||
+        cudaStreamSynchronize(b->st) != cudaSuccess)
+        return 0xFFFFFFFFu;
+    return s;
+}
+
+int dsim_batch_retire(dsim_batch* b, uint32_t jobId) {
+    BatchJob* j = b ? find_job(b, jobId) : nullptr;
+    if (!j) { set_last_error(kErrInvalid, "dsim_batch_retire: unknown job %u", jobId); return kErrInvalid; }
+    j->retired = true;
+    return kOk;
+}
+
+int dsim_batch_compact(dsim_batch* b) {
+    if (!b) return kErrInvalid;
+    bool any = false;
+    for (auto& j : b->jobs) any |= j.retired;
+    if (!any) return kOk;
+    const size_t nj = b->jobs.size();
+    std::vector<int32_t> map(nj, -1);
+    std::vector<int64_t> shift(nj, 0);
+    std::vector<BatchJob> kept;
+    std::vector<unsigned long long> oldCounts(2 * nj), newCounts;
+    if (nj) {
+        DSIM_CUDA_TRY(cudaMemcpyAsync(oldCounts.data(), b->d_counts, 16 * nj, cudaMemcpyDeviceToHost, b->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    }
+    uint64_t slot = 0;
+    for (size_t k = 0; k < nj; k++) {
+        BatchJob& j = b->jobs[k];
+        if (j.retired) { cudaFree(j.wave); j.wave = nullptr; continue; }
+        map[k] = (int32_t)kept.size();
+        shift[k] = (int64_t)slot - (int64_t)j.slot0;
+        slot += j.pad;
+        kept.push_back(j);
+        newCounts.push_back(oldCounts[2 * k]);
+        newCounts.push_back(oldCounts[2 * k + 1]);
+    }
+    int32_t* dmap = nullptr;
+    int64_t* dshift = nullptr;
+    int rc;
+    if ((rc = balloc(b, (void**)&dmap, nj * 4)) || (rc = balloc(b, (void**)&dshift, nj * 8))) {
+        cudaFree(dmap); cudaFree(dshift);
+        return rc;
+    }
+    b->bytes -= nj * 12;
+    cudaError_t e = cudaMemcpyAsync(dmap, map.data(), nj * 4, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dshift, shift.data(), nj * 8, cudaMemcpyHostToDevice, b->st);
+    if (e == cudaSuccess && b->N) {
+        k_batch_compact<<<(uint32_t)((b->N + 255) / 256), 256, 0, b->st>>>(view(b, b->cur), view(b, 1 - b->cur), dmap, dshift);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    cudaFree(dmap); cudaFree(dshift);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_batch_compact", __FILE__, __LINE__); return kErrCuda; }
+    b->cur = 1 - b->cur;
+    b->jobs = kept;
+    b->N = slot;
+    if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
+    if (!newCounts.empty())
+        DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_counts, newCounts.data(), newCounts.size() * 8, cudaMemcpyHostToDevice, b->st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    invalidate_graph(b);
+    return kOk;
+}
+
+int dsim_batch_info(dsim_batch* b, uint64_t info[6]) {
+    if (!b || !info) return kErrInvalid;
+    uint64_t running = 0;
+    for (const auto& j : b->jobs) running += (!j.retired && !job_finished(b, j)) ? 1 : 0;
+    info[0] = b->N; info[1] = b->jobs.size(); info[2] = running; info[3] = b->bytes;
+    info[4] = b->launches; info[5] = b->graphLaunches;
+    return kOk;
+}
+
+int dsim_batch_sync(dsim_batch* b) {
+    if (!b) return kErrInvalid;
+    DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    return kOk;
+}
+
+}  // extern "C"

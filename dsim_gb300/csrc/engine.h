@@ -7,6 +7,9 @@
 
 #include "common.cuh"
 
+struct dsim_mesh;
+struct dsim_cyl;
+
 namespace dsim {
 
 enum Layout : int { kLayoutSoA = 0, kLayoutAoS = 1 };
@@ -178,7 +181,11 @@ struct CylStepArgs {
 int launch_cyl_step(const CylDev& g, const CylStepArgs& a, const CylSpinsDev& S, int rng,
                     cudaStream_t st);
 
-// ---- host helpers (engine.cpp) -------------------------------------------
+// ---- host helpers --------------------------------------------------------
 const char* last_error_message();
+// api.cu: device views of native substrate handles (for batch.cu)
+int mesh_views(const ::dsim_mesh* m, MeshDev* g, AccelDev* a);
+int cyl_view(const ::dsim_cyl* c, CylDev* g);
+int mesh_rebuild_accel(::dsim_mesh* m, uint32_t nf);
 
 }  // namespace dsim

@@ -308,3 +308,130 @@ def cyl_run(cyl, spins, params, g=(0, 0, 0), iterations=1, seed=1, step0=0, draw
     gp = None if grad_per_step is None else np.ascontiguousarray(grad_per_step, F).reshape(-1)
     check(native().dsim_cyl_run(cyl.h, spins.h, C.byref(params), gg, gp, int(iterations),
                                 int(seed), int(step0), d, 1 if count else 0))
+
+
+WAVES = {"pgse": 0, "ogse": 1, "table": 2}
+
+
+class Batch:
+    """Many jobs advanced together (include/dsim_batch.h).  Each job keeps
+    per-spin gradient moments; signal(job, gradScaled) evaluates any gradient
+    that shares the job's waveform."""
+
+    def __init__(self, spin_capacity, job_capacity=1024):
+        self.h = C.c_void_p()
+        check(native().dsim_batch_create(int(spin_capacity), int(job_capacity), C.byref(self.h)))
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            native().dsim_batch_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_mesh(self, mesh):
+        sid = C.c_uint32()
+        check(native().dsim_batch_add_mesh(self.h, mesh.h, C.byref(sid)))
+        self._keep.append(mesh)
+        return sid.value
+
+    def add_cyl(self, cyl):
+        sid = C.c_uint32()
+        check(native().dsim_batch_add_cyl(self.h, cyl.h, C.byref(sid)))
+        self._keep.append(cyl)
+        return sid.value
+
+    def submit(self, substrate, pos, comp, fiber, steps, dt, step_sd, T2, phase_constant, seed,
+               permeability=0.0, waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None,
+               reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0):
+        pos = np.ascontiguousarray(pos, F).reshape(-1)
+        n = len(pos) // 3
+        d = _lib.JobDesc()
+        d.substrate, d.nSpins, d.steps = int(substrate), n, int(steps)
+        d.deltaTime = float(dt)
+        sd = list(np.asarray(step_sd, F).reshape(-1)) + [0.0] * 4
+        t2 = list(np.asarray(T2, F).reshape(-1)) + [0.0] * 4
+        d.stepSd[:] = [float(x) for x in sd[:4]]
+        d.T2[:] = [float(x) for x in t2[:4]]
+        d.permeability = float(permeability)
+        d.reflectionType = int(reflection_type)
+        d.spinRadius = float(spin_radius)
+        d.innerRadiusProportion = float(inner_radius_proportion)
+        d.phaseConstant = float(phase_constant)
+        d.waveform = WAVES[waveform]
+        d.delta, d.Delta, d.frequency = float(delta), float(Delta), float(frequency)
+        tab = None
+        if table is not None:
+            tab = np.ascontiguousarray(table, F)
+            assert len(tab) >= steps
+            d.table = tab.ctypes.data
+        d.seed = int(seed)
+        jid = C.c_uint32()
+        comp = np.ascontiguousarray(comp, np.uint8)
+        fib = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
+        check(native().dsim_batch_submit(self.h, C.byref(d), pos, comp, fib, C.byref(jid)))
+        return jid.value
+
+    def configure(self, chunk=20, occupancy=4, graph_chunks=8):
+        check(native().dsim_batch_configure(self.h, int(chunk), int(occupancy), int(graph_chunks)))
+
+    def advance(self, steps):
+        check(native().dsim_batch_advance(self.h, int(steps)))
+
+    def run(self):
+        check(native().dsim_batch_run(self.h))
+
+    def sync(self):
+        check(native().dsim_batch_sync(self.h))
+
+    def job_status(self, job):
+        s = C.c_uint32()
+        d = C.c_int()
+        check(native().dsim_batch_job_status(self.h, int(job), C.byref(s), C.byref(d)))
+        return s.value, bool(d.value)
+
+    def signal(self, job, grad_scaled):
+        g = np.ascontiguousarray(grad_scaled, F).reshape(-1, 3)
+        out = np.zeros(15 * len(g), np.float64)
+        check(native().dsim_batch_signal(self.h, int(job), g.reshape(-1), len(g), out))
+        return out.reshape(len(g), 5, 3)
+
+    def get(self, job, n):
+        pos = np.zeros(3 * n, F); mag = np.zeros(n, F); mom = np.zeros(6 * n, F)
+        comp = np.zeros(n, np.uint8); fib = np.zeros(n, np.uint32)
+        check(native().dsim_batch_get(self.h, int(job), pos, mag, mom, comp, fib))
+        return pos, mag, mom.reshape(n, 6), comp, fib
+
+    def counts(self, job):
+        c = np.zeros(2, np.uint64)
+        check(native().dsim_batch_counts(self.h, int(job), c))
+        return c
+
+    def status(self):
+        return int(native().dsim_batch_status(self.h))
+
+    def retire(self, job):
+        check(native().dsim_batch_retire(self.h, int(job)))
+
+    def compact(self):
+        check(native().dsim_batch_compact(self.h))
+
+    def info(self):
+        a = np.zeros(6, np.uint64)
+        check(native().dsim_batch_info(self.h, a))
+        keys = ("spins", "jobs", "running", "bytes", "launches", "graph_launches")
+        return dict(zip(keys, [int(x) for x in a]))
+
+
+def pgse_table(steps, dt, delta, Delta):
+    """The DSIM_WAVE_PGSE waveform as a table: +1 on [0, nd), -1 on [nD, nD + nd)."""
+    w = np.zeros(steps, F)
+    nd, nD = int(round(delta / dt)), int(round(Delta / dt))
+    w[:min(nd, steps)] = 1
+    w[nD:min(nD + nd, steps)] = -1
+    return w

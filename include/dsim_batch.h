@@ -1,0 +1,104 @@
+/*
+ * dsim_batch.h -- many simulation jobs in one step launch (libdsim_gb300.so).
+ *
+ * No counterpart in the reference: rfdougherty/dSim runs one substrate and
+ * one gradient per walk, one walk after another (dSim3/src/diffusion.cpp:553-625
+ * resets the spins for every gradient).  A batch holds the spins of many jobs
+ * (each with its own substrate, step count, time step, diffusivities, T2,
+ * permeability, waveform and seed) packed in one device array with a per-spin
+ * job index, and advances all of them with one step launch per chunk of steps.
+ *
+ * Per spin the batch keeps the gradient moment M = sum_t w(t) pos(t) (w: the
+ * job's waveform, pos: normalised position after step t) with compensated
+ * (Kahan) FP32 summation, instead of one phase.  Every gradient G that shares
+ * the waveform then has phase phi = phaseConstant * (gradScaled(G) . M),
+ * evaluated in FP64 at readout, so one walk serves all directions and
+ * magnitudes of a gradient table.  The mesh step rules, random draws and
+ * positions are those of dsim_mesh_run (a job alone in a batch reproduces
+ * dsim_mesh_run's positions bit for bit); cylinder jobs follow dsim_cyl_run.
+ *
+ * All functions return 0 or a negative DSIM_E* status (dsim.h); a batch is
+ * used from one host thread at a time.
+ */
+#ifndef DSIM_BATCH_H
+#define DSIM_BATCH_H
+#include <stddef.h>
+#include <stdint.h>
+#include "dsim.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dsim_batch dsim_batch;
+
+#define DSIM_WAVE_PGSE 0  /* +1 for steps [0, nd), -1 for [nD, nD + nd), else 0 */
+#define DSIM_WAVE_OGSE 1  /* cos(2 pi f t) on [0, nd), -cos(2 pi f (t - Delta)) on [nD, nD + nd) */
+#define DSIM_WAVE_TABLE 2 /* explicit w(t), one value per step */
+
+typedef struct {
+    uint32_t substrate;    /* index from dsim_batch_add_mesh / dsim_batch_add_cyl */
+    uint32_t nSpins;
+    uint32_t steps;
+    float deltaTime;       /* ms */
+    float stepSd[4];       /* normalised step sigma per compartment: mesh 0 extra,
+                              1 intra, 2 myelin, 3 glia; cylinders 0 core, 1 myelin, 2 outside */
+    float T2[4];           /* ms per compartment; <= 0: no decay */
+    float permeability;
+    uint32_t reflectionType;       /* mesh: 1 mirror reflection, 0 back to the segment start */
+    float spinRadius;              /* positions clamp to +-(1 - spinRadius) */
+    float innerRadiusProportion;   /* cylinders: myelin inner radius / outer radius */
+    float phaseConstant;           /* 2 pi gamma dt, as SpinSystem::updateSpins */
+    uint32_t waveform;             /* DSIM_WAVE_* */
+    float delta, Delta;            /* ms (PGSE, OGSE); step counts nd = round(delta/dt) */
+    float frequency;               /* Hz (OGSE) */
+    const float* table;            /* DSIM_WAVE_TABLE: `steps` values (host) */
+    uint64_t seed;                 /* Philox key; counter = (spin, step, 0) */
+} dsim_job_desc;
+
+/* spinCapacity: packed spin slots (each job is padded to a multiple of 32) */
+int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** out);
+void dsim_batch_free(dsim_batch* b);
+/* substrates are shared with the batch (keep them alive while it runs); the
+ * mesh needs its fine grid (dsim_mesh_set_accel > 0, the default) */
+int dsim_batch_add_mesh(dsim_batch* b, const dsim_mesh* m, uint32_t* substrate);
+int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate);
+/* Adds a job: initial state from host arrays (pos3 normalised; compartment:
+ * mesh compartment 0..3 or cylinder region imo 0..2; fiber: mesh fiber index
+ * or nearest cylinder, 0xFFFFFFFF none).  The job's step 0 runs in the next
+ * chunk.  DSIM_ENOMEM when spin or job capacity is exhausted. */
+int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* job, const float* pos3,
+                      const uint8_t* compartment, const uint32_t* fiber, uint32_t* jobId);
+/* chunk: steps between spin sorts (default 20); occupancy: 4 (default), 6 or 8
+ * resident blocks per SM for the step kernel; graphChunks: chunks captured in
+ * one CUDA graph launch (0 = plain launches, default 8) */
+int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint32_t graphChunks);
+/* advance every unfinished job by `steps` steps (rounded up to whole chunks) */
+int dsim_batch_advance(dsim_batch* b, uint32_t steps);
+/* advance until every job has finished */
+int dsim_batch_run(dsim_batch* b);
+/* steps done and total for a job; *done = 1 when finished */
+int dsim_batch_job_status(dsim_batch* b, uint32_t jobId, uint32_t* stepsDone, int* done);
+/* FP64 signal of a job for nG gradients sharing its waveform: gradScaled =
+ * G[mT/m] * 1e-9 * spaceScale (3 floats per gradient); out[15 g + 3 c + k] as
+ * dsim_signal (c = 0 all, 1 + compartment).  Synchronous. */
+int dsim_batch_signal(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG,
+                      double* out);
+/* a job's spins in spin order: pos3, mag, moments (M and its compensation,
+ * 6 per spin), compartment, fiber (any pointer may be NULL).  Synchronous. */
+int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float* moments6,
+                   uint8_t* compartment, uint32_t* fiber);
+/* per-job {reflections or rejections, permeations} and status bits */
+int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]);
+uint32_t dsim_batch_status(dsim_batch* b);
+/* drop finished jobs whose results were read and repack the others */
+int dsim_batch_retire(dsim_batch* b, uint32_t jobId);
+int dsim_batch_compact(dsim_batch* b);
+/* {packed spins, jobs, jobs running, device bytes, kernels launched, graph launches} */
+int dsim_batch_info(dsim_batch* b, uint64_t info[6]);
+/* wait for everything queued on the batch's stream */
+int dsim_batch_sync(dsim_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
