@@ -154,6 +154,18 @@ def _declare_batch(L):
         "dsim_batch_compact": (i32, [VP]),
         "dsim_batch_info": (i32, [VP, U64]),
         "dsim_batch_sync": (i32, [VP]),
+        "dsim_batch_autotune": (i32, [VP, u32, _nd(np.uint32, flags="C_CONTIGUOUS"), C.POINTER(C.c_float)]),
+        "dsim_server_create": (i32, [u64, u32, u64, C.POINTER(VP)]),
+        "dsim_server_free": (None, [VP]),
+        "dsim_server_add_mesh": (i32, [VP, VP, C.POINTER(u32)]),
+        "dsim_server_add_cyl": (i32, [VP, VP, C.POINTER(u32)]),
+        "dsim_server_configure": (i32, [VP, u32, u32, u32]),
+        "dsim_server_start": (i32, [VP]),
+        "dsim_server_submit": (i32, [VP, C.POINTER(JobDesc), F32, U8, OU32, F32, u32, C.POINTER(u32)]),
+        "dsim_server_poll": (i32, [VP, u32, C.POINTER(i32), _Opt(np.float64), _Opt(np.float64)]),
+        "dsim_server_drain": (i32, [VP]),
+        "dsim_server_stop": (i32, [VP]),
+        "dsim_server_stats": (i32, [VP, F64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

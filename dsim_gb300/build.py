@@ -24,9 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 EXACT = {"mesh.cu", "cyl.cu", "accel.cu", "coop.cu", "flat.cu", "batch.cu"}
 
 UNITS = ["mesh.cu", "accel.cu", "coop.cu", "flat.cu", "cyl.cu", "scan.cu", "reduce.cu", "api.cu", "compat3.cu", "compat2.cu",
-         "host_formats.cpp", "noalloc.cu", "batch.cu"]
+         "host_formats.cpp", "noalloc.cu", "batch.cu", "serve.cpp"]
 LIBS = {
-    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "flat", "cyl", "scan", "reduce", "noalloc", "batch"],
+    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "flat", "cyl", "scan", "reduce", "noalloc", "batch", "serve"],
     "libdsim3.so": ["compat3", "mesh", "accel", "flat", "scan"],
     "libdsim2.so": ["compat2", "cyl"],
 }
@@ -90,7 +90,7 @@ def build(verbose=False, jobs=None):
         target = os.path.join(LIB, lib)
         objs = [os.path.join(OBJ, p + ".o") for p in parts]
         if _stale(target, objs):
-            cmd = [nvcc(), "-shared", "-o", target + ".tmp"] + objs + ARCH + ["-Xcompiler", "-fPIC"]
+            cmd = [nvcc(), "-shared", "-o", target + ".tmp"] + objs + ARCH + ["-Xcompiler", "-fPIC", "-lpthread"]
             p = subprocess.run(cmd, capture_output=True, text=True)
             if p.returncode != 0:
                 raise RuntimeError("link %s failed:\n%s\n%s" % (lib, " ".join(cmd), p.stderr))

@@ -901,6 +901,104 @@ int dsim_batch_compact(dsim_batch* b) {
     return kOk;
 }
 
+// Autotuner: times `trialSteps` steps of the current jobs for each candidate
+// (step-kernel occupancy x chunk length x fine-grid cells per reference cell
+// edge of every mesh substrate) from a snapshot of the spin state, restores
+// the snapshot and keeps the fastest configuration.
+int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], float* bestMs) {
+    if (!b || !best || trialSteps == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: bad argument"); return kErrInvalid; }
+    if (b->N == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: no jobs"); return kErrInvalid; }
+    const size_t words = (size_t)(kBF + kBU) * b->N;
+    uint32_t* snap = nullptr;
+    int rc = balloc(b, (void**)&snap, words * 4);
+    if (rc) return rc;
+    b->bytes -= words * 4;
+    const size_t nj = b->jobs.size();
+    std::vector<unsigned long long> counts0(2 * nj);
+    auto save = [&](void) -> cudaError_t {
+        cudaError_t e = cudaSuccess;
+        for (int f = 0; f < kBF && e == cudaSuccess; f++)
+            e = cudaMemcpyAsync(snap + (size_t)f * b->N, b->buf[b->cur].f[f], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        for (int u = 0; u < kBU && e == cudaSuccess; u++)
+            e = cudaMemcpyAsync(snap + (size_t)(kBF + u) * b->N, b->buf[b->cur].u[u], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(counts0.data(), b->d_counts, 16 * nj, cudaMemcpyDeviceToHost, b->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+        return e;
+    };
+    const int cur0 = b->cur;
+    const uint32_t step0 = b->stepNow;
+    auto restore = [&](void) -> cudaError_t {
+        b->cur = cur0;
+        cudaError_t e = cudaSuccess;
+        for (int f = 0; f < kBF && e == cudaSuccess; f++)
+            e = cudaMemcpyAsync(b->buf[b->cur].f[f], snap + (size_t)f * b->N, b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        for (int u = 0; u < kBU && e == cudaSuccess; u++)
+            e = cudaMemcpyAsync(b->buf[b->cur].u[u], snap + (size_t)(kBF + u) * b->N, b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        b->stepNow = step0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_stepNow, &b->stepNow, 4, cudaMemcpyHostToDevice, b->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_counts, counts0.data(), 16 * nj, cudaMemcpyHostToDevice, b->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+        return e;
+    };
+    // fine-grid resolutions: cells per reference-cell edge x 2
+    const uint32_t gridHalves[] = {2, 3, 4, 5};  // 1, 1.5, 2, 2.5 fine cells per reference cell
+    const uint32_t occs[] = {4, 6, 8};
+    const uint32_t chunks[] = {10, 20, 40};
+    bool haveMesh = false;
+    for (auto* m : b->meshes) haveMesh |= (m != nullptr);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float bestT = 3.4e38f;
+    uint32_t bg = 0, bo = b->occupancy, bc = b->chunk;
+    const uint32_t graph0 = b->graphChunks;
+    cudaError_t e = save();
+    auto set_grid = [&](uint32_t halves) -> int {
+        for (size_t k = 0; k < b->meshes.size(); k++) {
+            if (!b->meshes[k]) continue;
+            SubDev& sd = b->subs[k];
+            uint32_t nf = std::min<uint32_t>(1024u, (sd.g.n * halves + 1) / 2);
+            int r = mesh_rebuild_accel(const_cast<dsim_mesh*>(b->meshes[k]), nf);
+            if (r) return r;
+            r = mesh_views(b->meshes[k], &sd.g, &sd.acc);
+            if (r) return r;
+            if (cudaMemcpy(b->d_subs + k, &sd, sizeof(SubDev), cudaMemcpyHostToDevice) != cudaSuccess) return kErrCuda;
+        }
+        return kOk;
+    };
+    for (uint32_t gi = 0; gi < (haveMesh ? 4u : 1u) && e == cudaSuccess && !rc; gi++) {
+        if (haveMesh && (rc = set_grid(gridHalves[gi]))) break;
+        for (uint32_t oc : occs) {
+            for (uint32_t ch : chunks) {
+                if ((e = restore()) != cudaSuccess) break;
+                b->occupancy = oc; b->chunk = ch; b->graphChunks = 0;
+                invalidate_graph(b);
+                cudaEventRecord(e0, b->st);
+                if ((rc = dsim_batch_advance(b, trialSteps))) break;
+                cudaEventRecord(e1, b->st);
+                if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                ms *= (float)trialSteps / (float)(((trialSteps + ch - 1) / ch) * ch);  // per requested step
+                if (ms < bestT) { bestT = ms; bg = haveMesh ? gridHalves[gi] : 0; bo = oc; bc = ch; }
+            }
+            if (rc || e != cudaSuccess) break;
+        }
+    }
+    if (!rc && e == cudaSuccess && haveMesh) rc = set_grid(bg);
+    if (!rc && e == cudaSuccess) e = restore();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(snap);
+    b->occupancy = bo; b->chunk = bc; b->graphChunks = graph0;
+    invalidate_graph(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_batch_autotune", __FILE__, __LINE__); return kErrCuda; }
+    best[0] = bo; best[1] = bc; best[2] = bg;
+    if (bestMs) *bestMs = bestT;
+    return kOk;
+}
+
 int dsim_batch_info(dsim_batch* b, uint64_t info[6]) {
     if (!b || !info) return kErrInvalid;
     uint64_t running = 0;

@@ -351,26 +351,9 @@ class Batch:
                reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0):
         pos = np.ascontiguousarray(pos, F).reshape(-1)
         n = len(pos) // 3
-        d = _lib.JobDesc()
-        d.substrate, d.nSpins, d.steps = int(substrate), n, int(steps)
-        d.deltaTime = float(dt)
-        sd = list(np.asarray(step_sd, F).reshape(-1)) + [0.0] * 4
-        t2 = list(np.asarray(T2, F).reshape(-1)) + [0.0] * 4
-        d.stepSd[:] = [float(x) for x in sd[:4]]
-        d.T2[:] = [float(x) for x in t2[:4]]
-        d.permeability = float(permeability)
-        d.reflectionType = int(reflection_type)
-        d.spinRadius = float(spin_radius)
-        d.innerRadiusProportion = float(inner_radius_proportion)
-        d.phaseConstant = float(phase_constant)
-        d.waveform = WAVES[waveform]
-        d.delta, d.Delta, d.frequency = float(delta), float(Delta), float(frequency)
-        tab = None
-        if table is not None:
-            tab = np.ascontiguousarray(table, F)
-            assert len(tab) >= steps
-            d.table = tab.ctypes.data
-        d.seed = int(seed)
+        d, tab = _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability, waveform,
+                           delta, Delta, frequency, table, reflection_type, spin_radius,
+                           inner_radius_proportion)
         jid = C.c_uint32()
         comp = np.ascontiguousarray(comp, np.uint8)
         fib = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
@@ -421,6 +404,14 @@ class Batch:
     def compact(self):
         check(native().dsim_batch_compact(self.h))
 
+    def autotune(self, trial_steps=40):
+        """Times every candidate configuration on a snapshot; returns
+        ({occupancy, chunk, fine_cells_per_ref_cell}, ms)."""
+        best = np.zeros(3, np.uint32)
+        ms = C.c_float()
+        check(native().dsim_batch_autotune(self.h, int(trial_steps), best, C.byref(ms)))
+        return {"occupancy": int(best[0]), "chunk": int(best[1]), "fine_per_ref": best[2] / 2.0}, ms.value
+
     def info(self):
         a = np.zeros(6, np.uint64)
         check(native().dsim_batch_info(self.h, a))
@@ -435,3 +426,102 @@ def pgse_table(steps, dt, delta, Delta):
     w[:min(nd, steps)] = 1
     w[nD:min(nD + nd, steps)] = -1
     return w
+
+
+def _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability=0.0,
+              waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None, reflection_type=1,
+              spin_radius=0.005, inner_radius_proportion=1.0):
+    d = _lib.JobDesc()
+    d.substrate, d.nSpins, d.steps = int(substrate), int(n), int(steps)
+    d.deltaTime = float(dt)
+    sd = list(np.asarray(step_sd, F).reshape(-1)) + [0.0] * 4
+    t2 = list(np.asarray(T2, F).reshape(-1)) + [0.0] * 4
+    d.stepSd[:] = [float(x) for x in sd[:4]]
+    d.T2[:] = [float(x) for x in t2[:4]]
+    d.permeability = float(permeability)
+    d.reflectionType = int(reflection_type)
+    d.spinRadius = float(spin_radius)
+    d.innerRadiusProportion = float(inner_radius_proportion)
+    d.phaseConstant = float(phase_constant)
+    d.waveform = WAVES[waveform]
+    d.delta, d.Delta, d.frequency = float(delta), float(Delta), float(frequency)
+    tab = None
+    if table is not None:
+        tab = np.ascontiguousarray(table, F)
+        assert len(tab) >= steps
+        d.table = tab.ctypes.data
+    d.seed = int(seed)
+    return d, tab
+
+
+class Server:
+    """Continuous-batching request loop (include/dsim_serve.h)."""
+
+    def __init__(self, spin_capacity, job_capacity=1024, hbm_cap=150e9):
+        self.h = C.c_void_p()
+        check(native().dsim_server_create(int(spin_capacity), int(job_capacity), int(hbm_cap), C.byref(self.h)))
+        self._keep = []
+        self.nG = {}
+
+    def add_mesh(self, mesh):
+        sid = C.c_uint32()
+        check(native().dsim_server_add_mesh(self.h, mesh.h, C.byref(sid)))
+        self._keep.append(mesh)
+        return sid.value
+
+    def add_cyl(self, cyl):
+        sid = C.c_uint32()
+        check(native().dsim_server_add_cyl(self.h, cyl.h, C.byref(sid)))
+        self._keep.append(cyl)
+        return sid.value
+
+    def configure(self, chunk=20, occupancy=4, graph_chunks=8):
+        check(native().dsim_server_configure(self.h, int(chunk), int(occupancy), int(graph_chunks)))
+
+    def start(self):
+        check(native().dsim_server_start(self.h))
+
+    def submit(self, substrate, pos, comp, fiber, grad_scaled, steps, dt, step_sd, T2, phase_constant, seed,
+               **kw):
+        pos = np.ascontiguousarray(pos, F).reshape(-1)
+        n = len(pos) // 3
+        d, tab = _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, **kw)
+        g = np.ascontiguousarray(grad_scaled, F).reshape(-1)
+        comp = np.ascontiguousarray(comp, np.uint8)
+        fib = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
+        t = C.c_uint32()
+        check(native().dsim_server_submit(self.h, C.byref(d), pos, comp, fib, g, len(g) // 3, C.byref(t)))
+        self.nG[t.value] = len(g) // 3
+        return t.value
+
+    def poll(self, ticket):
+        """(done, signals (nG, 5, 3) or None, times {submit, admit, done})"""
+        done = C.c_int()
+        out = np.zeros(15 * self.nG[ticket], np.float64)
+        times = np.zeros(3, np.float64)
+        check(native().dsim_server_poll(self.h, int(ticket), C.byref(done), out, times))
+        return bool(done.value), (out.reshape(-1, 5, 3) if done.value else None), times
+
+    def drain(self):
+        check(native().dsim_server_drain(self.h))
+
+    def stop(self):
+        check(native().dsim_server_stop(self.h))
+
+    def stats(self):
+        a = np.zeros(8, np.float64)
+        check(native().dsim_server_stats(self.h, a))
+        keys = ("jobs_done", "spin_steps", "busy_s", "max_inflight", "hbm_peak", "quanta", "compactions",
+                "errors")
+        return dict(zip(keys, a.tolist()))
+
+    def close(self):
+        if self.h:
+            native().dsim_server_free(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
