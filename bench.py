@@ -435,6 +435,8 @@ def run_ours(args, rank, world):
         e = e2e_abi3(W, m, max(2, min(args.steps, 5)), 1, pinned)
         e["pinned"] = is_pinned
         res["e2e"] = e
+    if rank == 0 and not args.no_forms:
+        res["forms"] = run_forms(args, W, m)
     if rank == 0 and not args.no_cpu:
         threads = 1
         rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
@@ -459,6 +461,156 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# --------------------------------------------------------------------------
+# batched and served forms on a seeded job mix
+# --------------------------------------------------------------------------
+def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False):
+    from dsim_gb300 import jobs as JB
+    t0 = time.time()
+    subs = [JB.mesh_substrate(W.axons, 1, mesh=m, tube=W.tube), JB.mesh_substrate(100, 7),
+            JB.cyl_substrate(64, 1), JB.cyl_substrate(256, 2)]
+    rng = np.random.default_rng(seed)
+    mix = [JB.make_job(rng, subs, spins_range=spins_range, steps_range=steps_range, permeable=permeable,
+                       seed=1000 + k) for k in range(n_jobs)]
+    log("job mix: %d jobs, %.3g spin-steps, %d gradients, built in %.1fs" % (
+        n_jobs, sum(j["n"] * j["steps"] for j in mix), sum(len(j["grads"]) for j in mix), time.time() - t0))
+    return subs, mix
+
+
+def _submit_kw(j):
+    return dict(steps=j["steps"], dt=j["dt"], step_sd=j["step_sd"], T2=j["T2"], phase_constant=j["phase_constant"],
+                seed=j["seed"], permeability=j["permeability"], waveform="pgse", delta=j["delta"],
+                Delta=j["Delta"], inner_radius_proportion=j["inner"])
+
+
+def run_plain_mix(mix):
+    """One job at a time through the plain path (dsim_mesh_run / dsim_cyl_run),
+    one walk with the job's first gradient; host clock from upload to signal."""
+    from dsim_gb300.engine import Spins, cyl_params, cyl_run, mesh_params, mesh_run, pgse_table
+    per = []
+    for k, j in enumerate([mix[0]] + list(mix)):  # the first job once untimed (module load)
+        sub = j["sub"]
+        w = pgse_table(j["steps"], float(j["dt"]), j["delta"], j["Delta"])
+        gps = (w[:, None] * j["grads"][0][None, :]).astype(F)
+        s = Spins(j["n"])
+        t0 = time.perf_counter()
+        if sub.kind == "mesh":
+            s.set(j["pos"], np.ones(j["n"], F), np.zeros(j["n"], F), j["comp"], j["fiber"].astype(np.uint16))
+            p = mesh_params(j["step_sd"], j["T2"], j["permeability"], j["dt"], j["phase_constant"])
+            mesh_run(sub.handle, s, p, grad_per_step=gps, iterations=j["steps"], seed=j["seed"])
+        else:
+            s.set_cyl(j["pos"], None, None, j["comp"].astype(np.uint32), j["fiber"])
+            p = cyl_params(2.0, 2.0, 0.2, sub.spaceScale, 70.0, 8.0, 80.0, j["permeability"], j["inner"],
+                           j["dt"], j["phase_constant"])
+            cyl_run(sub.handle, s, p, grad_per_step=gps, iterations=j["steps"], seed=j["seed"])
+        s.signal()
+        if k > 0:
+            per.append(time.perf_counter() - t0)
+        del s
+    return per
+
+
+def run_batched_mix(subs, mix, cfg):
+    from dsim_gb300.engine import Batch
+    cap = sum((j["n"] + 31) // 32 * 32 for j in mix)
+    b = Batch(cap, len(mix))
+    sids = {id(sb): (b.add_mesh(sb.handle) if sb.kind == "mesh" else b.add_cyl(sb.handle)) for sb in subs}
+    b.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
+    t0 = time.perf_counter()
+    ids = [b.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], **_submit_kw(j)) for j in mix]
+    b.run()
+    sigs = [b.signal(i, j["grads"]) for i, j in zip(ids, mix)]
+    el = time.perf_counter() - t0
+    info = b.info()
+    st = b.status()
+    b.close()
+    return el, sigs, info, st
+
+
+def tune_mix(subs, mix):
+    """Autotune on the first jobs of the mix (a separate batch)."""
+    from dsim_gb300.engine import Batch
+    sample = mix[:8]
+    cap = sum((j["n"] + 31) // 32 * 32 for j in sample)
+    b = Batch(cap, len(sample))
+    sids = {id(sb): (b.add_mesh(sb.handle) if sb.kind == "mesh" else b.add_cyl(sb.handle)) for sb in subs}
+    for j in sample:
+        b.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], **_submit_kw(j))
+    best, ms = b.autotune(trial_steps=60)
+    b.close()
+    return best, ms
+
+
+def run_served_mix(subs, mix, cfg, rate, seed=3):
+    """Poisson arrivals at `rate` jobs/s into the request loop."""
+    from dsim_gb300.engine import Server
+    cap = max(sum((j["n"] + 31) // 32 * 32 for j in mix) // 2, max((j["n"] + 31) // 32 * 32 for j in mix))
+    srv = Server(spin_capacity=cap, job_capacity=len(mix), hbm_cap=150e9)
+    sids = {id(sb): (srv.add_mesh(sb.handle) if sb.kind == "mesh" else srv.add_cyl(sb.handle)) for sb in subs}
+    srv.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
+    srv.start()
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, len(mix))
+    t0 = time.perf_counter()
+    tickets = []
+    t_next = t0
+    for j, gap in zip(mix, gaps):
+        t_next += gap
+        d = t_next - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        tickets.append(srv.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], j["grads"], **_submit_kw(j)))
+    srv.drain()
+    st = srv.stats()
+    srv.stop()
+    lat, first, last = [], None, None
+    for t in tickets:
+        done, sig, tm = srv.poll(t)
+        lat.append(tm[2] - tm[0])
+        first = tm[0] if first is None else min(first, tm[0])
+        last = tm[2] if last is None else max(last, tm[2])
+    srv.close()
+    work = sum(j["n"] * j["steps"] for j in mix)
+    return {"rate_jobs_per_s": rate, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "spin_steps_per_s": work / (last - first), "max_jobs_in_flight": int(st["max_inflight"]),
+            "errors": int(st["errors"])}
+
+
+def run_forms(args, W, m):
+    n_jobs = args.mix_jobs
+    spins_range = (4096, args.mix_max_spins)
+    steps_range = (args.mix_min_steps, args.mix_max_steps)
+    subs, mix = build_mix(W, m, n_jobs, 11, spins_range, steps_range)
+    work = sum(j["n"] * j["steps"] for j in mix)
+    grad_work = sum(j["n"] * j["steps"] * len(j["grads"]) for j in mix)
+    best, tune_ms = tune_mix(subs, mix)
+    log("autotune: %s (%.1f ms for 60 steps of 8 jobs)" % (best, tune_ms))
+    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+    per = run_plain_mix(mix)
+    plain_s = sum(per)
+    el, sigs, info, st = run_batched_mix(subs, mix, cfg)
+    plain_rate = work / plain_s
+    out = {
+        "mix": {"jobs": n_jobs, "spins": list(spins_range), "steps": list(steps_range), "dt_us": [5, 10],
+                "substrates": "beaded tubes 400 and 100 axons (2.56M / 0.64M triangles), packed cylinders 64 and 256",
+                "gradients_per_job": "6-128 directions x 3 b-values (b <= 3000 s/mm2), one PGSE waveform",
+                "spin_steps": work},
+        "plain": {"spin_steps_per_s": plain_rate, "seconds": plain_s,
+                  "note": "one job at a time (dsim_mesh_run / dsim_cyl_run), one walk per job"},
+        "batched": {"spin_steps_per_s": work / el, "seconds": el, "speedup_vs_plain": (work / el) / plain_rate,
+                    "signals_speedup_vs_plain": (grad_work / el) / plain_rate,
+                    "note": "all jobs in one batch; signals_speedup counts one plain walk per gradient, as the "
+                            "reference re-walks every gradient",
+                    "autotuned": best, "kernel_launches": info["launches"], "graph_launches": info["graph_launches"],
+                    "status": st},
+    }
+    cap_jobs = n_jobs / plain_s
+    out["served"] = [run_served_mix(subs, mix, cfg, r * cap_jobs) for r in args.serve_rates]
+    for o, r in zip(out["served"], args.serve_rates):
+        o["rate_x_plain_capacity"] = r
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -494,6 +646,12 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched / served job-mix runs")
+    ap.add_argument("--mix-jobs", type=int, default=48)
+    ap.add_argument("--mix-max-spins", type=int, default=1 << 18)
+    ap.add_argument("--mix-min-steps", type=int, default=400)
+    ap.add_argument("--mix-max-steps", type=int, default=2000)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0, 1.5])
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
