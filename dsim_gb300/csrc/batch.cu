@@ -52,6 +52,8 @@ struct JobDev {
     uint32_t key0, key1;
 };
 
+static_assert(sizeof(JobDev) % 4 == 0 && sizeof(SubDev) % 4 == 0, "records are copied by 32-bit words");
+
 // packed spin state; meta = compartment | fiber << 8 (cylinders: imo | nearest << 8)
 static constexpr int kBF = 10;  // float fields: x y z mx my mz cx cy cz mag
 static constexpr int kBU = 3;   // uint fields: meta job id
@@ -76,13 +78,32 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
              const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
              unsigned long long* jobCounts) {
     __shared__ FlatWarp wh[kFlatWarps];
+    // gradient moments and their compensation live in shared memory (touched
+    // once per step), which keeps the collision loop's registers free
+    __shared__ float mom[6][kFlatThreads];
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tx = threadIdx.x;
     FlatWarp& H = wh[threadIdx.x >> 5];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
     const uint32_t jb = S.u[U_JOB][i & ~31u];
-    const JobDev& J = jobs[jb];
+    // the warp's job and substrate records, copied to shared memory once and
+    // read from there (kept out of the collision loop's registers)
+    __shared__ JobDev jobS[kFlatWarps];
+    __shared__ SubDev subS[kFlatWarps];
+    const uint32_t wi = threadIdx.x >> 5;
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(jobS + wi);
+        for (uint32_t k = lane; k < sizeof(JobDev) / 4; k += 32) dst[k] = __ldg(src + k);
+        __syncwarp();
+        const uint32_t* s2 = reinterpret_cast<const uint32_t*>(subs + jobS[wi].sub);
+        uint32_t* d2 = reinterpret_cast<uint32_t*>(subS + wi);
+        for (uint32_t k = lane; k < sizeof(SubDev) / 4; k += 32) d2[k] = __ldg(s2 + k);
+        __syncwarp();
+    }
+    const JobDev& J = jobS[wi];
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;  // not started or finished (warp-uniform)
@@ -91,18 +112,18 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     const uint32_t id = S.u[U_ID][i];
     const bool valid = id != 0xFFFFFFFFu;
     float x = S.f[F_X][i], y = S.f[F_Y][i], z = S.f[F_Z][i];
-    float mx = S.f[F_MX][i], my = S.f[F_MY][i], mz = S.f[F_MZ][i];
-    float cx = S.f[F_CX][i], cy = S.f[F_CY][i], cz = S.f[F_CZ][i];
+    mom[0][tx] = S.f[F_MX][i]; mom[1][tx] = S.f[F_MY][i]; mom[2][tx] = S.f[F_MZ][i];
+    mom[3][tx] = S.f[F_CX][i]; mom[4][tx] = S.f[F_CY][i]; mom[5][tx] = S.f[F_CZ][i];
     float mag = S.f[F_MAG][i];
     const uint32_t meta = S.u[U_META][i];
     uint32_t comp = meta & 0xFFu, fiber = meta >> 8;
     const uint32_t k0 = J.key0, k1 = J.key1;
     const float* __restrict__ wave = J.wave;
     uint32_t nrefl = 0, nperm = 0, st = 0;
-    const SubDev& sub = subs[J.sub];
+    const SubDev& sub = subS[wi];
     if (sub.kind == kSubMesh) {
-        const MeshDev g = sub.g;
-        const AccelDev acc = sub.acc;
+        const MeshDev& g = sub.g;
+        const AccelDev& acc = sub.acc;
         const float perm = J.perm;
         const uint32_t reflType = J.reflType, maxSub = J.maxSub;
         uint32_t it = 0;
@@ -148,9 +169,9 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
                     const float T2 = J.T2[comp & 3u];
                     if (T2 > 0.0f) mag += -mag / T2 * J.dt;
                     const float w = __ldg(wave + ls0 + it);
-                    kahan_add(mx, cx, w * x);
-                    kahan_add(my, cy, w * y);
-                    kahan_add(mz, cz, w * z);
+                    kahan_add(mom[0][tx], mom[3][tx], w * x);
+                    kahan_add(mom[1][tx], mom[4][tx], w * y);
+                    kahan_add(mom[2][tx], mom[5][tx], w * z);
                     if (++it >= nsteps) active = false;
                     else fresh = true;
                 }
@@ -158,7 +179,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
             __syncwarp();
         }
     } else if (valid) {
-        const CylDev g = sub.c;
+        const CylDev& g = sub.c;
         const float perm = J.perm, inR = J.inR;
         uint32_t imo = comp, nearest = fiber;
         if (imo < 2 && nearest >= g.nF) imo = 2;
@@ -175,17 +196,17 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
             const float T2 = J.T2[imo];
             if (T2 > 0.0f) mag += -mag / T2 * J.dt;
             const float w = __ldg(wave + ls0 + it);
-            kahan_add(mx, cx, w * x);
-            kahan_add(my, cy, w * y);
-            kahan_add(mz, cz, w * z);
+            kahan_add(mom[0][tx], mom[3][tx], w * x);
+            kahan_add(mom[1][tx], mom[4][tx], w * y);
+            kahan_add(mom[2][tx], mom[5][tx], w * z);
         }
         comp = imo;
         fiber = nearest & 0xFFFFFFu;
     }
     if (valid) {
         S.f[F_X][i] = x; S.f[F_Y][i] = y; S.f[F_Z][i] = z;
-        S.f[F_MX][i] = mx; S.f[F_MY][i] = my; S.f[F_MZ][i] = mz;
-        S.f[F_CX][i] = cx; S.f[F_CY][i] = cy; S.f[F_CZ][i] = cz;
+        S.f[F_MX][i] = mom[0][tx]; S.f[F_MY][i] = mom[1][tx]; S.f[F_MZ][i] = mom[2][tx];
+        S.f[F_CX][i] = mom[3][tx]; S.f[F_CY][i] = mom[4][tx]; S.f[F_CZ][i] = mom[5][tx];
         S.f[F_MAG][i] = mag;
         S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
     }
