@@ -130,7 +130,8 @@ class JobDesc(C.Structure):
                 ("permeability", C.c_float), ("reflectionType", C.c_uint32), ("spinRadius", C.c_float),
                 ("innerRadiusProportion", C.c_float), ("phaseConstant", C.c_float),
                 ("waveform", C.c_uint32), ("delta", C.c_float), ("Delta", C.c_float),
-                ("frequency", C.c_float), ("table", C.c_void_p), ("seed", C.c_uint64)]
+                ("frequency", C.c_float), ("table", C.c_void_p), ("seed", C.c_uint64), ("flags", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 def _declare_batch(L):
@@ -150,6 +151,7 @@ def _declare_batch(L):
         "dsim_batch_get": (i32, [VP, u32, OF32, OF32, OF32, OU8, OU32]),
         "dsim_batch_counts": (i32, [VP, u32, U64]),
         "dsim_batch_status": (u32, [VP]),
+        "dsim_batch_precision_counts": (i32, [VP, u32, U64]),
         "dsim_batch_retire": (i32, [VP, u32]),
         "dsim_batch_compact": (i32, [VP]),
         "dsim_batch_info": (i32, [VP, U64]),

@@ -50,6 +50,8 @@ struct JobDev {
     float inR;                    // cylinders: (inner radius proportion)^2
     const float* wave;            // w[steps]
     uint32_t key0, key1;
+    uint32_t flags;               // DSIM_JOB_PRECISE
+    uint32_t pad_;
 };
 
 static_assert(sizeof(JobDev) % 4 == 0 && sizeof(SubDev) % 4 == 0, "records are copied by 32-bit words");
@@ -72,7 +74,9 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     s = t;
 }
 
-template <int MINB>
+// PREC: the instantiation for precision-form jobs (FP64 re-test of
+// near-degenerate intersections); each instantiation skips the other's warps
+template <int MINB, bool PREC>
 __global__ void __launch_bounds__(kFlatThreads, MINB)
 k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
              const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
@@ -104,6 +108,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
+    if (((J.flags & DSIM_JOB_PRECISE) != 0) != PREC) return;  // warp-uniform
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;  // not started or finished (warp-uniform)
@@ -120,6 +125,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     const uint32_t k0 = J.key0, k1 = J.key1;
     const float* __restrict__ wave = J.wave;
     uint32_t nrefl = 0, nperm = 0, st = 0;
+    PrecCount pc;
     const SubDev& sub = subS[wi];
     if (sub.kind == kSubMesh) {
         const MeshDev& g = sub.g;
@@ -148,7 +154,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
             const bool open = active;
             bool found;
             FastHit best;
-            flat_round(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
+            flat_round_mode<PREC>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pc);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -210,16 +216,22 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
         S.f[F_MAG][i] = mag;
         S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
     }
-    // per-job counters: one atomic per warp
-    unsigned long long r = nrefl, p = nperm;
+    // per-job counters {reflections, permeations, exact tests, FP64 re-tests}: one atomic per warp
+    unsigned long long r = nrefl, p = nperm, te = pc.tests, re = pc.retests;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         r += __shfl_down_sync(FULL, r, o);
         p += __shfl_down_sync(FULL, p, o);
+        if (PREC) {
+            te += __shfl_down_sync(FULL, te, o);
+            re += __shfl_down_sync(FULL, re, o);
+        }
     }
-    if (lane == 0 && (r | p)) {
-        atomicAdd(jobCounts + 2 * jb, r);
-        atomicAdd(jobCounts + 2 * jb + 1, p);
+    if (lane == 0) {
+        if (r) atomicAdd(jobCounts + 4 * jb, r);
+        if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+        if (PREC && te) atomicAdd(jobCounts + 4 * jb + 2, te);
+        if (PREC && re) atomicAdd(jobCounts + 4 * jb + 3, re);
     }
     if (st) atomicOr(status, st);
 }
@@ -392,6 +404,7 @@ struct dsim_batch {
     uint32_t *hist = nullptr, *hstart = nullptr, *scratch = nullptr;
     uint64_t keyCap = 0, K = 0;
     uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
+    bool anyPrecise = false;
     cudaGraphExec_t exec = nullptr;
     bool graphValid = false;
     int graphCur = -1;
@@ -478,14 +491,16 @@ int enqueue_chunk(dsim_batch* b) {
     b->cur = 1 - b->cur;
     const uint32_t grid = (N + kFlatThreads - 1) / kFlatThreads;
     if (b->occupancy >= 8)
-        k_batch_step<8><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+        k_batch_step<8, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
     else if (b->occupancy >= 6)
-        k_batch_step<6><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+        k_batch_step<6, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
     else
-        k_batch_step<4><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+        k_batch_step<4, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+    if (b->anyPrecise)
+        k_batch_step<4, true><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
     k_batch_advance<<<1, 1, 0, b->st>>>(b->d_stepNow, b->chunk);
     DSIM_CUDA_TRY(cudaGetLastError());
-    b->launches += 7;  // keys, scan (3), scatter, step, advance
+    b->launches += b->anyPrecise ? 8 : 7;  // keys, scan (3), scatter, step (x2), advance
     return kOk;
 }
 
@@ -569,11 +584,11 @@ int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** 
     if (!rc) rc = balloc(b, (void**)&b->keys, b->cap * 4);
     if (!rc) rc = balloc(b, (void**)&b->d_jobs, (size_t)jobCapacity * sizeof(JobDev));
     if (!rc) rc = balloc(b, (void**)&b->d_subs, (size_t)b->subCap * sizeof(SubDev));
-    if (!rc) rc = balloc(b, (void**)&b->d_counts, (size_t)2 * jobCapacity * 8);
+    if (!rc) rc = balloc(b, (void**)&b->d_counts, (size_t)4 * jobCapacity * 8);
     if (!rc) rc = balloc(b, (void**)&b->d_status, 4);
     if (!rc) rc = balloc(b, (void**)&b->d_stepNow, 4);
     if (!rc && (cudaMemset(b->d_status, 0, 4) != cudaSuccess || cudaMemset(b->d_stepNow, 0, 4) != cudaSuccess ||
-                cudaMemset(b->d_counts, 0, (size_t)2 * jobCapacity * 8) != cudaSuccess))
+                cudaMemset(b->d_counts, 0, (size_t)4 * jobCapacity * 8) != cudaSuccess))
         rc = kErrCuda;
     if (rc) { dsim_batch_free(b); return rc; }
     *out = b;
@@ -661,6 +676,11 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     J.inR = d->innerRadiusProportion * d->innerRadiusProportion;
     J.key0 = (uint32_t)d->seed;
     J.key1 = (uint32_t)(d->seed >> 32);
+    J.flags = d->flags & DSIM_JOB_PRECISE;
+    if (J.flags && cyl) {
+        set_last_error(kErrInvalid, "dsim_batch_submit: the precision form applies to mesh jobs");
+        return kErrInvalid;
+    }
     std::vector<float> w = make_wave(d);
     int rc = balloc(b, (void**)&j.wave, w.size() * 4);
     if (rc) return rc;
@@ -702,8 +722,9 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     b->nextId++;
     b->N += pad;
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
-    DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 2 * jobIndex, 0, 16, b->st));
+    DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 4 * jobIndex, 0, 32, b->st));
     DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    if (J.flags) b->anyPrecise = true;
     invalidate_graph(b);
     *jobId = j.id;
     return kOk;
@@ -744,7 +765,7 @@ int dsim_batch_advance(dsim_batch* b, uint32_t steps) {
             }
             DSIM_CUDA_TRY(cudaGraphLaunch(b->exec, b->st));
             b->graphLaunches++;
-            b->launches += 7ull * G;
+            b->launches += (b->anyPrecise ? 8ull : 7ull) * G;
             b->stepNow += G * b->chunk;
             chunks -= G;
         } else {
@@ -843,13 +864,27 @@ int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]) {
     if (!b || !counts) return kErrInvalid;
     for (size_t k = 0; k < b->jobs.size(); k++) {
         if (b->jobs[k].id != jobId) continue;
-        unsigned long long c[2];
-        DSIM_CUDA_TRY(cudaMemcpyAsync(c, b->d_counts + 2 * k, 16, cudaMemcpyDeviceToHost, b->st));
+        unsigned long long c[4];
+        DSIM_CUDA_TRY(cudaMemcpyAsync(c, b->d_counts + 4 * k, 32, cudaMemcpyDeviceToHost, b->st));
         DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
         counts[0] = c[0]; counts[1] = c[1];
         return kOk;
     }
     set_last_error(kErrInvalid, "dsim_batch_counts: unknown job %u", jobId);
+    return kErrInvalid;
+}
+
+int dsim_batch_precision_counts(dsim_batch* b, uint32_t jobId, uint64_t out[2]) {
+    if (!b || !out) return kErrInvalid;
+    for (size_t k = 0; k < b->jobs.size(); k++) {
+        if (b->jobs[k].id != jobId) continue;
+        unsigned long long c[4];
+        DSIM_CUDA_TRY(cudaMemcpyAsync(c, b->d_counts + 4 * k, 32, cudaMemcpyDeviceToHost, b->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+        out[0] = c[2]; out[1] = c[3];
+        return kOk;
+    }
+    set_last_error(kErrInvalid, "dsim_batch_precision_counts: unknown job %u", jobId);
     return kErrInvalid;
 }
 
@@ -878,9 +913,9 @@ int dsim_batch_compact(dsim_batch* b) {
     std::vector<int32_t> map(nj, -1);
     std::vector<int64_t> shift(nj, 0);
     std::vector<BatchJob> kept;
-    std::vector<unsigned long long> oldCounts(2 * nj), newCounts;
+    std::vector<unsigned long long> oldCounts(4 * nj), newCounts;
     if (nj) {
-        DSIM_CUDA_TRY(cudaMemcpyAsync(oldCounts.data(), b->d_counts, 16 * nj, cudaMemcpyDeviceToHost, b->st));
+        DSIM_CUDA_TRY(cudaMemcpyAsync(oldCounts.data(), b->d_counts, 32 * nj, cudaMemcpyDeviceToHost, b->st));
         DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
     }
     uint64_t slot = 0;
@@ -891,8 +926,7 @@ int dsim_batch_compact(dsim_batch* b) {
         shift[k] = (int64_t)slot - (int64_t)j.slot0;
         slot += j.pad;
         kept.push_back(j);
-        newCounts.push_back(oldCounts[2 * k]);
-        newCounts.push_back(oldCounts[2 * k + 1]);
+        for (int q = 0; q < 4; q++) newCounts.push_back(oldCounts[4 * k + q]);
     }
     int32_t* dmap = nullptr;
     int64_t* dshift = nullptr;
@@ -914,6 +948,8 @@ int dsim_batch_compact(dsim_batch* b) {
     b->cur = 1 - b->cur;
     b->jobs = kept;
     b->N = slot;
+    b->anyPrecise = false;
+    for (const auto& j : b->jobs) b->anyPrecise |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
     if (!newCounts.empty())
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_counts, newCounts.data(), newCounts.size() * 8, cudaMemcpyHostToDevice, b->st));
@@ -935,14 +971,14 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
     if (rc) return rc;
     b->bytes -= words * 4;
     const size_t nj = b->jobs.size();
-    std::vector<unsigned long long> counts0(2 * nj);
+    std::vector<unsigned long long> counts0(4 * nj);
     auto save = [&](void) -> cudaError_t {
         cudaError_t e = cudaSuccess;
         for (int f = 0; f < kBF && e == cudaSuccess; f++)
             e = cudaMemcpyAsync(snap + (size_t)f * b->N, b->buf[b->cur].f[f], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
         for (int u = 0; u < kBU && e == cudaSuccess; u++)
             e = cudaMemcpyAsync(snap + (size_t)(kBF + u) * b->N, b->buf[b->cur].u[u], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(counts0.data(), b->d_counts, 16 * nj, cudaMemcpyDeviceToHost, b->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(counts0.data(), b->d_counts, 32 * nj, cudaMemcpyDeviceToHost, b->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
         return e;
     };
@@ -957,7 +993,7 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
             e = cudaMemcpyAsync(b->buf[b->cur].u[u], snap + (size_t)(kBF + u) * b->N, b->N * 4, cudaMemcpyDeviceToDevice, b->st);
         b->stepNow = step0;
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_stepNow, &b->stepNow, 4, cudaMemcpyHostToDevice, b->st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_counts, counts0.data(), 16 * nj, cudaMemcpyHostToDevice, b->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_counts, counts0.data(), 32 * nj, cudaMemcpyHostToDevice, b->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
         return e;
     };

@@ -78,13 +78,28 @@ __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, flo
     return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
 }
 
+// the same in the plain (reference FP32) or the precision form
+template <bool PREC>
+__device__ __forceinline__ bool test_wide_mode(const MeshDev& g, float4 q, float4 pt, uint32_t excl, float ox,
+                                               float oy, float oz, float dx, float dy, float dz, FastHit& h,
+                                               PrecCount& pc) {
+    if (!PREC) return test_wide_loaded(g, q, pt, excl, ox, oy, oz, dx, dy, dz, h);
+    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
+    const uint32_t t = __float_as_uint(pt.w);
+    if (t == excl) return false;
+    return test_prec(g, q.x, q.y, q.z, pt.x, pt.y, pt.z, t, ox, oy, oz, dx, dy, dz, h, pc);
+}
+
 // One round for every lane of the warp (all 32 lanes call it).  open: the lane
 // has a sub-segment (o -> p, `excluded` = last-hit triangle) to test.  On
 // return, for open lanes, found / best hold the reference's collision result.
-__device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
-                                           uint32_t lane, bool open, float ox, float oy, float oz,
-                                           float px, float py, float pz, uint32_t excluded,
-                                           bool& found, FastHit& best) {
+// PREC selects the precision form's FP64 re-test of near-degenerate
+// intersections (counted in pc); the plain form is the reference's FP32 test.
+template <bool PREC>
+__device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
+                                                uint32_t lane, bool open, float ox, float oy, float oz,
+                                                float px, float py, float pz, uint32_t excluded,
+                                                bool& found, FastHit& best, PrecCount& pc) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
@@ -144,11 +159,11 @@ __device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const 
                 if (v0) { q0 = __ldg(&acc.recw[e0].q); t0 = __ldg(&acc.recw[e0].pt); }
                 if (v1) { q1 = __ldg(&acc.recw[e1].q); t1 = __ldg(&acc.recw[e1].pt); }
                 FastHit h;
-                if (v0 && test_wide_loaded(g, q0, t0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
-                                           H.dx[o0], H.dy[o0], H.dz[o0], h))
+                if (v0 && test_wide_mode<PREC>(g, q0, t0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
+                                           H.dx[o0], H.dy[o0], H.dz[o0], h, pc))
                     flat_file_hit(H, o0, h);
-                if (v1 && test_wide_loaded(g, q1, t1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1],
-                                           H.dx[o1], H.dy[o1], H.dz[o1], h))
+                if (v1 && test_wide_mode<PREC>(g, q1, t1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1],
+                                           H.dx[o1], H.dy[o1], H.dz[o1], h, pc))
                     flat_file_hit(H, o1, h);
             }
         } else {
@@ -172,7 +187,9 @@ __device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const 
             uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
             for (uint32_t k = b0; k < b1; k++) {
                 FastHit h;
-                if (test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h)) flat_file_hit(H, lane, h);
+                const bool hit = (PREC && acc.wide) ? test_entry_mode<true>(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h, pc)
+                                                    : test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h);
+                if (hit) flat_file_hit(H, lane, h);
             }
         }
     }
@@ -181,7 +198,7 @@ __device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const 
     if (!open) return;
     const uint32_t n = H.n[lane];
     if (n > (uint32_t)kFlatSlots) {
-        ref_scan(g, ox, oy, oz, px, py, pz, excluded, best, found);
+        ref_scan_mode<PREC>(g, ox, oy, oz, px, py, pz, excluded, best, found, pc);
     } else if (n > 0) {
         // the reference's traversal of its grid over the hits filed in
         // this lane's slots (a triangle filed twice from two fine cells
@@ -221,6 +238,14 @@ __device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const 
             best.x = H.x[bq][lane]; best.y = H.y[bq][lane]; best.z = H.z[bq][lane];
         }
     }
+}
+
+// plain form (the reference's FP32 tests)
+__device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const AccelDev& acc, uint32_t lane,
+                                           bool open, float ox, float oy, float oz, float px, float py, float pz,
+                                           uint32_t excluded, bool& found, FastHit& best) {
+    PrecCount pc;
+    flat_round_mode<false>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pc);
 }
 
 // Reflection or permeation at the round's hit `best`: the permeation interval

@@ -348,12 +348,12 @@ class Batch:
 
     def submit(self, substrate, pos, comp, fiber, steps, dt, step_sd, T2, phase_constant, seed,
                permeability=0.0, waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None,
-               reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0):
+               reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0, precise=False):
         pos = np.ascontiguousarray(pos, F).reshape(-1)
         n = len(pos) // 3
         d, tab = _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability, waveform,
                            delta, Delta, frequency, table, reflection_type, spin_radius,
-                           inner_radius_proportion)
+                           inner_radius_proportion, precise)
         jid = C.c_uint32()
         comp = np.ascontiguousarray(comp, np.uint8)
         fib = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
@@ -398,6 +398,12 @@ class Batch:
     def status(self):
         return int(native().dsim_batch_status(self.h))
 
+    def precision_counts(self, job):
+        """{exact tests, FP64 re-tests} of a precision-form job."""
+        c = np.zeros(2, np.uint64)
+        check(native().dsim_batch_precision_counts(self.h, int(job), c))
+        return int(c[0]), int(c[1])
+
     def retire(self, job):
         check(native().dsim_batch_retire(self.h, int(job)))
 
@@ -430,7 +436,7 @@ def pgse_table(steps, dt, delta, Delta):
 
 def _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability=0.0,
               waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None, reflection_type=1,
-              spin_radius=0.005, inner_radius_proportion=1.0):
+              spin_radius=0.005, inner_radius_proportion=1.0, precise=False):
     d = _lib.JobDesc()
     d.substrate, d.nSpins, d.steps = int(substrate), int(n), int(steps)
     d.deltaTime = float(dt)
@@ -451,6 +457,7 @@ def _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permea
         assert len(tab) >= steps
         d.table = tab.ctypes.data
     d.seed = int(seed)
+    d.flags = 1 if precise else 0
     return d, tab
 
 
@@ -525,3 +532,11 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def rng_draws(seed, spin0, step, n, stream=0):
+    """The step kernels' draws (n.x, n.y, n.z, u) for spins [spin0, spin0 + n)
+    at global step `step` (Philox key = seed, counter word 3 = stream)."""
+    out = np.zeros(4 * n, F)
+    check(native().dsim_rng_draws(int(seed), int(spin0), int(step), int(stream), int(n), None, out))
+    return out.reshape(n, 4)

@@ -53,7 +53,15 @@ typedef struct {
     float frequency;               /* Hz (OGSE) */
     const float* table;            /* DSIM_WAVE_TABLE: `steps` values (host) */
     uint64_t seed;                 /* Philox key; counter = (spin, step, 0) */
+    uint32_t flags;                /* DSIM_JOB_PRECISE: precision form (mesh jobs) */
+    uint32_t reserved;
 } dsim_job_desc;
+
+/* Precision form: intersections whose FP32 outcome lies within the FP32 error
+ * band of a decision boundary (segment end on the plane, triangle edge) are
+ * decided again in FP64; the others keep the reference's FP32 result.  Phase
+ * moments are Kahan-compensated in every form. */
+#define DSIM_JOB_PRECISE 1u
 
 /* spinCapacity: packed spin slots (each job is padded to a multiple of 32) */
 int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** out);
@@ -89,6 +97,8 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
                    uint8_t* compartment, uint32_t* fiber);
 /* per-job {reflections or rejections, permeations} and status bits */
 int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]);
+/* precision form: {exact intersection tests, of which re-tested in FP64} */
+int dsim_batch_precision_counts(dsim_batch* b, uint32_t jobId, uint64_t out[2]);
 uint32_t dsim_batch_status(dsim_batch* b);
 /* drop finished jobs whose results were read and repack the others */
 int dsim_batch_retire(dsim_batch* b, uint32_t jobId);

@@ -95,6 +95,16 @@ uint32_t or3_integrate_f64(const or3_params* p, uint32_t N, double* pos, double*
                            double phaseConstant, uint32_t iterations, const float* draws,
                            uint32_t* counts);
 
+/* the FP64 walk recording gradient moments M_k = sum_t w_k(t) pos(t) for
+ * nWaves waveforms (moments[N][nWaves][3]); OpenMP over spins */
+uint32_t or3_integrate_f64_moments(const or3_params* p, uint32_t N, double* pos, double* mag,
+                                   uint8_t* comp, uint16_t* fiber, uint32_t nT,
+                                   const double* vertices, const uint32_t* trgls,
+                                   const uint32_t* triInfo, const uint32_t* cubeCounter,
+                                   const uint32_t* trianglesInCubes, uint32_t nWaves,
+                                   const double* waves, uint32_t iterations, const float* draws,
+                                   double* moments, uint32_t* counts, int nthreads);
+
 /* getMrSignal(double[]) spinSystem.cpp:1452-1500: out[0]=total, out[1+c]=c */
 void or3_signal(uint32_t N, const float* mag, const float* phase, const uint8_t* comp,
                 double out[5]);

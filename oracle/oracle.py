@@ -105,6 +105,10 @@ def _declare(L):
                                     P_U16, C.c_uint32, P_F64, P_U32, P_U32, P_U32, P_U32, P_F64,
                                     C.c_double, C.c_uint32, P_F32, _opt(P_U32)]
     L.or3_integrate_f64.restype = C.c_uint32
+    L.or3_integrate_f64_moments.argtypes = [C.POINTER(Params3), C.c_uint32, P_F64, P_F64, P_U8, P_U16,
+                                            C.c_uint32, P_F64, P_U32, P_U32, P_U32, P_U32, C.c_uint32,
+                                            P_F64, C.c_uint32, P_F32, P_F64, _opt(P_U32), C.c_int]
+    L.or3_integrate_f64_moments.restype = C.c_uint32
     L.or3_signal.argtypes = [C.c_uint32, P_F32, P_F32, P_U8, P_F64]
     L.or2_load_fibers.argtypes = [C.c_char_p, C.c_float, _opt(P_F32), C.POINTER(C.c_float)]
     L.or2_load_fibers.restype = C.c_int
@@ -252,3 +256,23 @@ def spin_fields(raw):
     rec = np.frombuffer(raw.tobytes(), np.dtype([("mag", "<f4"), ("phase", "<f4"), ("comp", "u1"),
                                                  ("pad", "u1"), ("fiber", "<u2")]))
     return (rec["mag"].copy(), rec["phase"].copy(), rec["comp"].copy(), rec["fiber"].copy())
+
+
+def integrate3_f64_moments(p, pos, mag, comp, fiber, vertices, trgls, triInfo, cc, tic, waves, draws,
+                           counts=None, nthreads=1):
+    """FP64 walk (the precision oracle) recording M_k = sum_t w_k(t) pos(t)
+    for each waveform row of `waves` [nWaves][iterations].  pos, mag (float64)
+    and comp, fiber are updated in place.  Returns (capped, moments[N][nWaves][3])."""
+    L = lib()
+    N = len(mag)
+    waves = np.ascontiguousarray(waves, np.float64).reshape(-1, np.shape(waves)[-1])
+    nW, iters = waves.shape
+    mom = np.zeros(N * nW * 3, np.float64)
+    v64 = np.ascontiguousarray(vertices, np.float64)
+    capped = L.or3_integrate_f64_moments(C.byref(p), N, pos, mag, comp, fiber, len(trgls) // 3, v64,
+                                         np.ascontiguousarray(trgls, np.uint32),
+                                         np.ascontiguousarray(triInfo, np.uint32), cc,
+                                         np.ascontiguousarray(tic, np.uint32), nW, waves.reshape(-1), iters,
+                                         np.ascontiguousarray(draws, np.float32).reshape(-1), mom, counts,
+                                         int(nthreads))
+    return capped, mom.reshape(N, nW, 3)

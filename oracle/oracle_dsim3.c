@@ -404,6 +404,62 @@ uint32_t or3_integrate_f64(const or3_params* p, uint32_t N, double* pos, double*
     return capped;
 }
 
+/* FP64 walk that records gradient moments instead of one phase: for every
+ * waveform k (waves[k * iterations + t]) M_k += w_k(t) * pos(t) after each
+ * step, in double.  The phase of a gradient g with waveform k is then
+ * phaseConstant * (g . M_k), the quantity the GPU batch form accumulates.
+ * Spins are independent, so they run in parallel (OpenMP); counts may be NULL. */
+uint32_t or3_integrate_f64_moments(const or3_params* p, uint32_t N, double* pos, double* mag,
+                                   uint8_t* comp, uint16_t* fiber, uint32_t nT,
+                                   const double* vertices, const uint32_t* trgls,
+                                   const uint32_t* triInfo, const uint32_t* cubeCounter,
+                                   const uint32_t* trianglesInCubes, uint32_t nWaves,
+                                   const double* waves, uint32_t iterations, const float* draws,
+                                   double* moments, uint32_t* counts, int nthreads) {
+    double* H = (double*)malloc((size_t)nT * 12 * sizeof(double));
+    if (!H) return 0xFFFFFFFFu;
+    for (uint32_t t = 0; t < nT; t++) {
+        const double* a = vertices + 3 * (size_t)trgls[t * 3];
+        const double* b = vertices + 3 * (size_t)trgls[t * 3 + 1];
+        const double* c = vertices + 3 * (size_t)trgls[t * 3 + 2];
+        double nx = (b[1] - a[1]) * (c[2] - a[2]) - (b[2] - a[2]) * (c[1] - a[1]);
+        double ny = (b[2] - a[2]) * (c[0] - a[0]) - (b[0] - a[0]) * (c[2] - a[2]);
+        double nz = (b[0] - a[0]) * (c[1] - a[1]) - (b[1] - a[1]) * (c[0] - a[0]);
+        double len = sqrt(nx * nx + ny * ny + nz * nz);
+        double* h = H + (size_t)t * 12;
+        h[0] = nx / len; h[1] = ny / len; h[2] = nz / len;
+        h[3] = c[0] - a[0]; h[4] = c[1] - a[1]; h[5] = c[2] - a[2];
+        h[6] = b[0] - a[0]; h[7] = b[1] - a[1]; h[8] = b[2] - a[2];
+        h[9] = h[3] * h[6] + h[4] * h[7] + h[5] * h[8];
+        h[10] = h[3] * h[3] + h[4] * h[4] + h[5] * h[5];
+        h[11] = h[6] * h[6] + h[7] * h[7] + h[8] * h[8];
+    }
+    uint32_t capped = 0;
+    if (nthreads < 1) nthreads = 1;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : capped)
+    for (int64_t ii = 0; ii < (int64_t)N; ii++) {
+        const uint32_t i = (uint32_t)ii;
+        double phase = 0.0;
+        double* M = moments + (size_t)i * nWaves * 3;
+        for (uint32_t it = 0; it < iterations; it++) {
+            const float* src = draws + ((size_t)it * N + i) * 4;
+            double d[4] = {src[0], src[1], src[2], src[3]};
+            capped += step_f64(p, pos + 3 * (size_t)i, mag + i, &phase, comp + i, fiber + i, vertices, H,
+                               triInfo, cubeCounter, trianglesInCubes, 0.0, 0.0, 0.0, 0.0, d,
+                               counts ? counts + 2 * (size_t)i : NULL);
+            const double* P = pos + 3 * (size_t)i;
+            for (uint32_t k = 0; k < nWaves; k++) {
+                const double w = waves[(size_t)k * iterations + it];
+                M[3 * k] += w * P[0];
+                M[3 * k + 1] += w * P[1];
+                M[3 * k + 2] += w * P[2];
+            }
+        }
+    }
+    free(H);
+    return capped;
+}
+
 /* getMrSignal(double mrSignal[]), spinSystem.cpp:1452-1500 */
 void or3_signal(uint32_t N, const float* mag, const float* phase, const uint8_t* comp,
                 double out[5]) {

@@ -179,3 +179,42 @@ def test_matlab_hand_collision_case(tmp_path):
     qq = (o.astype(np.float64) + d[0, 0, :3])
     expect = ip + (np.eye(3) - 2 * np.outer(n, n)) @ (qq - ip)
     assert np.allclose(pos, expect, atol=2e-6)
+
+
+def test_fp64_oracle_moments_equal_its_phase_and_track_fp32(tmp_path):
+    """The FP64 precision oracle: its moment form reproduces its own phase form
+    (phase = pc * (g . M)), and its trajectories stay with the FP32 oracle's
+    (pinned to the reference above) for nearly every spin."""
+    from dsim_gb300.engine import grad_scaled, phase_constant, pgse_table
+    g = _load("mesh_am")
+    prm = json.loads(str(g["params"]))
+    path = tmp_path / "mesh.txt"
+    path.write_bytes(g["mesh_text"].tobytes())
+    m = O.Mesh(str(path), prm["spaceScale"])
+    cc, tic, maxtpc = O.populate_cubes(m.vertices, m.trgls, 50)
+    N, iters = prm["N"], prm["iters"]
+    p = O.params3(g["stdDevs"], g["T2"], prm["perm"], prm["dt"], 50, maxtpc)
+    gs = grad_scaled([prm["gx"], prm["gy"], prm["gz"]], prm["spaceScale"]).astype(np.float64)
+    pc = float(phase_constant(prm["gamma"], prm["dt"]))
+    w = pgse_table(iters, prm["dt"], 0.2 * iters * prm["dt"], 0.5 * iters * prm["dt"]).astype(np.float64)
+    mag0, ph0, comp0, fib0 = O.spin_fields(g["spins0"])
+    v64 = m.vertices.astype(np.float64)
+
+    def fresh():
+        return (g["pos0"].astype(np.float64), mag0.astype(np.float64), comp0.copy(), fib0.copy())
+
+    pos_a, mag_a, comp_a, fib_a = fresh()
+    ph_a = np.zeros(N, np.float64)
+    L = O.lib()
+    L.or3_integrate_f64(C.byref(p), N, pos_a, mag_a, ph_a, comp_a, fib_a, len(m.trgls) // 3, v64, m.trgls,
+                        m.triInfo, cc, tic, np.ascontiguousarray(w[:, None] * gs[None, :]).reshape(-1), pc, iters,
+                        np.ascontiguousarray(g["draws"], np.float32).reshape(-1), None)
+    pos_b, mag_b, comp_b, fib_b = fresh()
+    capped, M = O.integrate3_f64_moments(p, pos_b, mag_b, comp_b, fib_b, v64, m.trgls, m.triInfo, cc, tic,
+                                         w[None, :], g["draws"], nthreads=2)
+    assert capped == 0
+    assert np.array_equal(pos_a, pos_b) and np.array_equal(comp_a, comp_b)
+    assert np.allclose(pc * (M[:, 0, :] @ gs), ph_a, rtol=1e-12, atol=1e-12)
+    # against the FP32 oracle's (= the reference's) end positions
+    d = np.abs(pos_b.reshape(-1, 3) - g["pos1"].reshape(-1, 3).astype(np.float64)).max(1)
+    assert (d < 1e-5).mean() >= 0.95
