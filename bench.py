@@ -24,6 +24,7 @@ workload.  Multi-GPU (--gpus N under torchrun): independent replicas, one
 per rank, no collective on the data path (weak scaling).
 """
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -439,6 +440,8 @@ def run_ours(args, rank, world):
         res["forms"] = run_forms(args, W, m)
     if rank == 0 and not args.no_precision:
         res["precision"] = run_precision(args, W, m)
+    if rank == 0 and not args.no_cylinders:
+        res["cylinders"] = run_cylinders(args)
     if rank == 0 and not args.no_cpu:
         threads = 1
         rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
@@ -616,6 +619,107 @@ def run_forms(args, W, m):
 
 
 # --------------------------------------------------------------------------
+# cylinders (C1): 64 z-cylinders, 10k spins, 5000 steps, 48 PGSE gradients
+# --------------------------------------------------------------------------
+def run_cylinders(args):
+    from dsim_gb300 import jobs as JB
+    from dsim_gb300.engine import Batch, Spins, cyl_params, cyl_run, grad_scaled, pgse_table, phase_constant
+    sub = JB.cyl_substrate(64, 1)          # 20 x 20 um cell, spaceScale 10
+    c = sub.handle
+    N, dt, steps, delta, Delta = args.c1_spins, 0.01, args.c1_steps, 10.0, 30.0
+    rng = np.random.default_rng(1)
+    pos = rng.uniform(-0.995, 0.995, (N, 3)).astype(F)
+    imo, near = JB.cyl_regions(sub.geom, pos, sub.spaceScale)
+    dirs = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, 0, 1], [0, 1, 1]], np.float64)
+    dirs /= np.linalg.norm(dirs, axis=1)[:, None]
+    G = np.concatenate([lv * dirs for lv in np.linspace(0.0, 80.0, 8)])          # 48 x 3, mT/m
+    gs = grad_scaled(G, sub.spaceScale).astype(F).reshape(-1, 3)
+    pc = phase_constant(42576.0, dt)
+    w = pgse_table(steps, dt, delta, Delta)
+    ss = F(sub.spaceScale)
+    sd = [float(np.sqrt(F(2) * (F(adc) / (ss * ss)) * F(dt))) for adc in (2.0, 2.0, 2.0)] + [0.0]
+    T2 = [0.0, 0.0, 0.0, 0.0]                                               # no T2 decay in C1
+    # plain path: one fresh walk per gradient, one after another (the reference's order)
+    p = cyl_params(2.0, 2.0, 2.0, sub.spaceScale, 1e30, 1e30, 1e30, 0.0, 1.0, dt, pc)
+    s = Spins(N)
+    s.set_cyl(pos, None, None, imo.astype(np.uint32), near)
+    cyl_run(c, s, p, grad_per_step=(w[:, None] * gs[0][None, :]).astype(F), iterations=50, seed=99)
+    s.sync()
+    t0 = time.perf_counter()
+    plain_S = []
+    for k, g in enumerate(gs):
+        s.set_cyl(pos, None, None, imo.astype(np.uint32), near)
+        cyl_run(c, s, p, grad_per_step=(w[:, None] * g[None, :]).astype(F), iterations=steps, seed=k + 1)
+        sums = s.signal()
+        plain_S.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
+    plain_s = time.perf_counter() - t0
+    # batch form: the same 48 fresh walks as 48 jobs of one launch
+    b = Batch(48 * ((N + 31) // 32 * 32), 48)
+    sid = b.add_cyl(c)
+    t0 = time.perf_counter()
+    ids = [b.submit(sid, pos.reshape(-1), imo, near, steps, dt, sd, T2, pc, k + 1, waveform="pgse", delta=delta,
+                    Delta=Delta, inner_radius_proportion=1.0) for k in range(len(gs))]
+    b.run()
+    batch_S = []
+    for k, j in enumerate(ids):
+        sums = b.signal(j, gs[k][None, :])[0]
+        batch_S.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
+    batch_s = time.perf_counter() - t0
+    counts = b.counts(ids[0])
+    b.close()
+    # one shared walk: every gradient from the moments of a single walk
+    b = Batch((N + 31) // 32 * 32, 1)
+    sid = b.add_cyl(c)
+    t0 = time.perf_counter()
+    j = b.submit(sid, pos.reshape(-1), imo, near, steps, dt, sd, T2, pc, 1, waveform="pgse", delta=delta,
+                 Delta=Delta, inner_radius_proportion=1.0)
+    b.run()
+    sums = b.signal(j, gs)
+    shared_S = (np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]).tolist()
+    shared_s = time.perf_counter() - t0
+    b.close()
+    # C-bar: cell-list entries a step examines (own fiber inside; the new
+    # position's cell list outside), from the initial state
+    cc, cubes, fp = c.grid()
+    n3 = c.numCubes
+    cell = np.clip(np.floor((pos.astype(np.float64) + 1.0) / float(c.cubeLength)), 0, n3 - 1).astype(np.int64)
+    key = cell[:, 2] * n3 * n3 + cell[:, 1] * n3 + cell[:, 0]
+    Cbar = float(np.where(imo < 2, 1.0, cc[key].astype(np.float64)).mean())
+    work = len(gs) * N * steps
+    res = {"workload": "64 z-cylinders (Gamma radii mean 1 um, 0.5 packing, 20 x 20 um, spaceScale 10), %d spins, "
+                       "dt 10 us, %d steps, PGSE delta 10 Delta 30 ms, 8 levels 0-80 mT/m x 6 directions" % (N, steps),
+           "boundary": "clamped box (the reference has no periodic boundaries)",
+           "plain_spin_steps_per_s": work / plain_s, "batched_spin_steps_per_s": work / batch_s,
+           "shared_walk_signals_per_s": len(gs) / shared_s, "shared_walk_seconds": shared_s,
+           "plain_seconds": plain_s, "batched_seconds": batch_s,
+           "signal_plain": plain_S[::8], "signal_batched": batch_S[::8], "signal_shared_walk": shared_S[::8],
+           "rejections_per_spin_step": float(counts[0]) / (N * steps),
+           "roofline": {"bytes_per_spin_step": 2 * 20 + 16 * Cbar, "C_bar": Cbar,
+                        "achieved_GBs_batched": (2 * 20 + 16 * Cbar) * work / batch_s / 1e9},
+           "note": "signals listed for every 8th gradient (G = 0 .. 80 mT/m along x)"}
+    # the reference's CPU path (oracle port, MWC draws) on a sample
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    P = O.Params2()
+    P.intraAdcScaled = P.extraAdcScaled = P.myelinAdcScaled = F(2.0) / (ss * ss)
+    P.T2fiber = P.T2myelin = P.T2outside = 1e30
+    P.permeability, P.innerRadiusProportion, P.spinRadius, P.deltaTime = 0.0, 1.0, 0.005, dt
+    P.numCubes, P.maxFibersPerCube, P.cubeLength = c.numCubes, c.maxFPC, c.cubeLength
+    ns, it = 2000, 400
+    p4 = np.zeros((ns, 4), F); p4[:, :3] = pos[:ns]
+    sd4 = np.zeros((ns, 4), np.uint32)
+    sd4[:, :2] = rng.integers(1, 2 ** 31, (ns, 2))
+    par = np.zeros((ns, 5), F); par[:, 0] = 1.0
+    par[:, 2] = np.where(imo[:ns] < 2, near[:ns], 0).astype(F); par[:, 3] = imo[:ns].astype(F)
+    t0 = time.perf_counter()
+    O.lib().or2_integrate(C.byref(P), ns, p4.reshape(-1), sd4.reshape(-1), par.reshape(-1), fp, cc, cubes,
+                          float(gs[-1][0]), float(gs[-1][1]), float(gs[-1][2]), float(pc), it, None, None, None)
+    res["cpu_port_spin_steps_per_s"] = ns * it / (time.perf_counter() - t0)
+    res["cpu_port_sample"] = "%d spins x %d steps, 1 thread, the reference's MWC draws" % (ns, it)
+    return res
+
+
+# --------------------------------------------------------------------------
 # precision form (C5): FP32 + Kahan moments + FP64 re-test vs the FP64 oracle
 # --------------------------------------------------------------------------
 def c5_waves(steps, dt):
@@ -770,6 +874,9 @@ def main():
     ap.add_argument("--mix-max-steps", type=int, default=2000)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0, 1.5])
     ap.add_argument("--no-precision", action="store_true", help="skip the precision-form comparison")
+    ap.add_argument("--no-cylinders", action="store_true", help="skip the cylinder workload")
+    ap.add_argument("--c1-spins", type=int, default=10000)
+    ap.add_argument("--c1-steps", type=int, default=5000)
     ap.add_argument("--c5-steps", type=int, default=20000)
     ap.add_argument("--c5-sample", type=int, default=512)
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
