@@ -114,6 +114,8 @@ def _declare_native(L):
         "dsim_timer_stop": (i32, [VP, C.POINTER(f32)]),
         "dsim_flush_l2": (i32, [VP, C.c_size_t]),
         "dsim_spins_launches": (i32, [VP, C.POINTER(u64), i32]),
+        "dsim_spins_set_spin_base": (i32, [VP, u32]),
+        "dsim_mesh_compartments": (i32, [VP, VP, u64, f32, C.POINTER(u32)]),
         "dsim_rng_draws": (i32, [u64, u32, u64, u32, u32, OU32, OF32]),
     }
     for name, (res, args) in sig.items():

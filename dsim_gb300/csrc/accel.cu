@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc,
             float4 q = __ldg(a.draws + (size_t)it * S.N + id);
             d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
         } else {
-            d = philox_draw(id, a.step0 + it, a.stream, k0, k1);
+            d = philox_draw(a.spinBase + id, a.step0 + it, a.stream, k0, k1);
         }
         float ox = x, oy = y, oz = z;
         float sd = a.sd[comp & 3u];

@@ -72,6 +72,7 @@ struct dsim_mesh {
     uint32_t* acc_tri = nullptr;
     AccelRecWide* acc_recw = nullptr;
     uint32_t accWide = 1;  // 32-byte fine-grid records (0: 16-byte)
+    float maxabs[3] = {1.0f, 1.0f, 1.0f};  // max(1, max |vertex coordinate|) per axis, as initFibers keeps
     MeshDev dev() const {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
@@ -178,6 +179,7 @@ struct dsim_spins {
     uint32_t sortNb = 0;        // key grid of the allocated sort buffers
     uint32_t sortEvery = 20;    // steps between reorderings (0 = never)
     uint64_t launches = 0;      // kernels launched by dsim_mesh_run / dsim_cyl_run on this object
+    uint32_t spinBase = 0;      // global index of spin 0 in the Philox counter (replica shards)
     bool permuted = false;      // slot i does not hold spin i
     float4* cpos = nullptr;     // cylinder layout (lazy)
     uint32_t* cseed = nullptr;  // cylinder layout (lazy)
@@ -233,6 +235,8 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     int rc;
     m->nV = (uint32_t)(Vn.size() / 3);
     m->nT = (uint32_t)(trgls.size() / 3);
+    for (uint32_t v = 0; v < m->nV; v++)
+        for (int k = 0; k < 3; k++) m->maxabs[k] = fmaxf(fabsf(Vn[3 * v + k]), m->maxabs[k]);
     for (uint32_t t = 0; t < m->nT; t++)
         for (int k = 0; k < 3; k++)
             if (trgls[3 * t + k] >= m->nV) {
@@ -747,6 +751,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
     a.stream = 0;
     a.maxSub = p->maxSubsegments ? p->maxSubsegments : 4096u;
     a.status = s->status;
+    a.spinBase = s->spinBase;
     a.counts = (countCollisions & 1) ? s->counts : nullptr;
     if (countCollisions & 2) {
         if (!s->tested) {
@@ -849,6 +854,7 @@ int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const flo
     a.key0 = (uint32_t)seed; a.key1 = (uint32_t)(seed >> 32);
     a.step0 = step0;
     a.status = s->status;
+    a.spinBase = s->spinBase;
     a.counts = countCollisions ? s->counts : nullptr;
     int rc = upload_grad_draws(s, gradPerStep, replayDraws, iterations, &a.grad, &a.draws);
     if (rc) return rc;
@@ -894,6 +900,37 @@ int dsim_timer_stop(dsim_spins* s, float* ms) {
     float v = 0;
     DSIM_CUDA_TRY(cudaEventElapsedTime(&v, s->ev0, s->ev1));
     if (ms) *ms = v;
+    return kOk;
+}
+
+int dsim_mesh_compartments(dsim_mesh* m, dsim_spins* s, uint64_t seed, float startBoxSize, uint32_t* moved) {
+    if (!m || !s) { set_last_error(kErrInvalid, "dsim_mesh_compartments: null argument"); return kErrInvalid; }
+    if (m->nf == 0 || !m->acc_recw) {
+        set_last_error(kErrInvalid, "dsim_mesh_compartments: needs the fine grid with 32-byte records");
+        return kErrInvalid;
+    }
+    uint32_t* dmoved = nullptr;
+    int rc = dev_alloc(&dmoved, 1);
+    if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(dmoved, 0, 4, s->st);
+    if (e == cudaSuccess) {
+        rc = launch_compartments(m->dev(), m->acc(), s->sorted(), m->maxabs, startBoxSize, seed, 20, 8, s->status,
+                                 dmoved, s->st);
+        uint32_t h = 0;
+        if (!rc) e = cudaMemcpyAsync(&h, dmoved, 4, cudaMemcpyDeviceToHost, s->st);
+        if (!rc && e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+        if (moved) *moved = h;
+    }
+    cudaFree(dmoved);
+    if (rc) return rc;
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_mesh_compartments", __FILE__, __LINE__); return kErrCuda; }
+    return kOk;
+}
+
+int dsim_spins_set_spin_base(dsim_spins* s, uint32_t base) {
+    if (!s) { set_last_error(kErrInvalid, "dsim_spins_set_spin_base: null argument"); return kErrInvalid; }
+    if ((uint64_t)base + s->N > 0x100000000ull) { set_last_error(kErrTooLarge, "spin base + N exceeds 2^32"); return kErrTooLarge; }
+    s->spinBase = base;
     return kOk;
 }
 

@@ -26,6 +26,8 @@ enum Status : int {
 enum StatusBits : uint32_t {
     kStatusSubsegCap = 1u,   // a spin hit the sub-segment cap in one step
     kStatusBadCell = 2u,     // a cell index fell outside the grid (never expected)
+    kStatusParityOverflow = 4u,  // compartment search: more than 32 membranes on one line
+    kStatusUnresolved = 8u,      // compartment search: every line and position was ambiguous
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

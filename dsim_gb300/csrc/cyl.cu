@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_cyl_step(CylDev g, CylStepArgs a, CylSp
             float4 q = __ldg(a.draws + (size_t)it * S.N + i);
             d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
         } else {
-            d = philox_draw(i, a.step0 + it, a.stream, k0, k1);
+            d = philox_draw(a.spinBase + i, a.step0 + it, a.stream, k0, k1);
         }
         float ox = x, oy = y, oz = z;
         float sdv = (imo == 0) ? a.intraSd : ((imo == 1) ? a.myelinSd : a.extraSd);

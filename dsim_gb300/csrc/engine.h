@@ -54,6 +54,7 @@ struct MeshStepArgs {
     uint32_t* counts;     // [2N] reflections, permeations (or null)
     uint32_t* tested;     // [N] grid entries scanned (or null)
     const uint32_t* spinKeys;  // per-spin Philox keys [2N] by id (kRngPhiloxPerSpinKey, fast path)
+    uint32_t spinBase;    // added to the spin index in the Philox counter (replica shards)
 };
 
 // ---- accel.cu -------------------------------------------------------------
@@ -127,6 +128,11 @@ int launch_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT, const uin
 int launch_mesh_step(const MeshDev& g, const MeshStepArgs& a, const SpinsDev& S, int layout,
                      int rng, cudaStream_t st);
 
+// ---- compartments.cu ------------------------------------------------------
+int launch_compartments(const MeshDev& g, const AccelDev& acc, const SpinsSorted& S, const float maxabs[3],
+                        float startBox, uint64_t seed, uint32_t maxTries, uint32_t maxMoves, uint32_t* status,
+                        uint32_t* moved, cudaStream_t st);
+
 // ---- scan.cu --------------------------------------------------------------
 // exclusive prefix sum: out[0..n] (out[n] = total); scratch >= scan_scratch_words(n)
 size_t scan_scratch_words(uint32_t n);
@@ -176,6 +182,7 @@ struct CylStepArgs {
     const float4* draws;
     uint32_t* status;
     uint32_t* counts;
+    uint32_t spinBase;    // added to the spin index in the Philox counter (replica shards)
 };
 // rng: kRngPhilox (key0/key1), kRngPhiloxPerSpinKey (seed4.x/.y), kRngReplay
 int launch_cyl_step(const CylDev& g, const CylStepArgs& a, const CylSpinsDev& S, int rng,

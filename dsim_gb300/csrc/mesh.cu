@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(256) k_mesh_step(MeshDev g, MeshStepArgs a, Sp
             float4 q = __ldg(a.draws + (size_t)it * S.N + i);
             d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
         } else {
-            d = philox_draw(i, a.step0 + it, a.stream, k0, k1);
+            d = philox_draw(a.spinBase + i, a.step0 + it, a.stream, k0, k1);
         }
         float gx = a.gx, gy = a.gy, gz = a.gz;
         if (a.grad) { float4 G = __ldg(a.grad + it); gx = G.x; gy = G.y; gz = G.z; }

@@ -118,6 +118,10 @@ class Spins:
         check(native().dsim_signal(self.h, float(region), out))
         return out.reshape(5, 3)
 
+    def set_spin_base(self, base):
+        """Global index of spin 0 in the random stream (replica shards)."""
+        check(native().dsim_spins_set_spin_base(self.h, int(base)))
+
     def launches(self, reset=False):
         """Kernels launched by mesh/cylinder runs on this object."""
         n = C.c_uint64()
@@ -184,6 +188,13 @@ class Mesh:
 
     def set_records(self, nbytes):
         check(native().dsim_mesh_set_records(self.h, int(nbytes)))
+
+    def compartments(self, spins, seed=1, start_box=1.0):
+        """Assign every spin's compartment and fiber from its position (ray
+        parity, as findSpinsInFibers); returns the number of spins moved."""
+        moved = C.c_uint32()
+        check(native().dsim_mesh_compartments(self.h, spins.h, int(seed), float(start_box), C.byref(moved)))
+        return moved.value
 
     def set_kernel(self, variant):
         check(native().dsim_mesh_set_kernel(self.h, int(variant)))

@@ -34,6 +34,8 @@ extern "C" {
 /* status bits reported by dsim_spins_status */
 #define DSIM_STATUS_SUBSEG_CAP 1u  /* a step hit the collision sub-segment cap */
 #define DSIM_STATUS_BAD_CELL 2u    /* a grid list referenced a missing fiber    */
+#define DSIM_STATUS_PARITY_OVERFLOW 4u /* compartment search: > 32 membranes on one line */
+#define DSIM_STATUS_UNRESOLVED 8u  /* compartment search: no unambiguous line found */
 
 typedef struct dsim_mesh dsim_mesh;
 typedef struct dsim_cyl dsim_cyl;
@@ -78,6 +80,15 @@ int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
  * dependent load for records that pass) */
 int dsim_mesh_set_records(dsim_mesh* m, uint32_t bytesPerRecord);
 int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]);
+/* Compartment and fiber of every spin of `s` from its position (the
+ * reference's findSpinsInFibers, dSim3/src/spinSystem.cpp:1615-1852): parity of
+ * the crossings of a line out of the volume with each closed membrane,
+ * innermost membrane type first; ambiguous lines (edge or vertex hits) are
+ * tilted and retried 20 times, then the spin is moved to a random position in
+ * [-startBoxSize, startBoxSize]^3 (draws from Philox keyed by seed).  Writes
+ * the compartment and fiber (and moved positions) into s; *moved = spins
+ * moved.  Needs the mesh's fine grid with 32-byte records. */
+int dsim_mesh_compartments(dsim_mesh* m, dsim_spins* s, uint64_t seed, float startBoxSize, uint32_t* moved);
 /* copies the CSR grid: cellStart[numCubes^3 + 1], cellTri[entries] */
 int dsim_mesh_grid(const dsim_mesh* m, uint32_t* cellStart, uint32_t* cellTri);
 /* copies normalised vertices[3V] and triInfo[3T] = {fiber, membrane, first vertex} */
@@ -120,6 +131,10 @@ int dsim_spins_status(dsim_spins* s, uint32_t* status, int reset);
  * (default 20; 0 = never) so that neighbouring threads read the same cell
  * records.  Each spin keeps its identity (random stream, counters, getters). */
 int dsim_spins_set_sort_interval(dsim_spins* s, uint32_t steps);
+/* Global index of this object's spin 0 in the Philox counter (default 0).
+ * A job split over several GPUs gives each shard the index of its first spin,
+ * so the shards together draw exactly what one GPU running all spins draws. */
+int dsim_spins_set_spin_base(dsim_spins* s, uint32_t base);
 /* bytes of device memory held by the object */
 uint64_t dsim_spins_bytes(const dsim_spins* s);
 void dsim_spins_free(dsim_spins* s);
