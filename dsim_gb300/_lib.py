@@ -125,6 +125,18 @@ def _declare_native(L):
     return L
 
 
+class Config(C.Structure):
+    """dsim_config (include/dsim_sim.h)."""
+    _fields_ = [("dialect", C.c_int), ("stepsPerUpdate", C.c_uint32), ("useGpu", C.c_int),
+                ("useDisplay", C.c_int), ("writeOut", C.c_int), ("numSpins", C.c_uint32), ("gamma", C.c_float),
+                ("timeStep", C.c_float), ("extraAdc", C.c_float), ("intraAdc", C.c_float),
+                ("myelinAdc", C.c_float), ("extraT2", C.c_float), ("intraT2", C.c_float),
+                ("myelinT2", C.c_float), ("spaceScale", C.c_float), ("startBox", C.c_float),
+                ("permeability", C.c_float), ("innerRadiusFraction", C.c_float),
+                ("gradsFile", C.c_char * 512), ("gradsStr", C.c_char * 512), ("outFile", C.c_char * 512),
+                ("fiberFile", C.c_char * 512)]
+
+
 class JobDesc(C.Structure):
     """dsim_job_desc (include/dsim_batch.h)."""
     _fields_ = [("substrate", C.c_uint32), ("nSpins", C.c_uint32), ("steps", C.c_uint32),
@@ -170,6 +182,13 @@ def _declare_batch(L):
         "dsim_server_drain": (i32, [VP]),
         "dsim_server_stop": (i32, [VP]),
         "dsim_server_stats": (i32, [VP, F64]),
+        "dsim_config_load": (i32, [C.c_char_p, C.POINTER(Config)]),
+        "dsim_grads_parse_file": (i32, [C.c_char_p, OF32, u32, C.POINTER(u32)]),
+        "dsim_grads_parse_string": (i32, [C.c_char_p, OF32, u32, C.POINTER(u32)]),
+        "dsim_pgse_schedule": (i32, [F32, C.c_float, u32, OF32, u32, C.POINTER(u32)]),
+        "dsim_tensor_fit": (i32, [F32, F64, u32, F64, F64, F32, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                  C.POINTER(C.c_float)]),
+        "dsim_simulate": (i32, [C.c_char_p, u64, u32, F64, u32, C.POINTER(u32), C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

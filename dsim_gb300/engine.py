@@ -551,3 +551,61 @@ def rng_draws(seed, spin0, step, n, stream=0):
     out = np.zeros(4 * n, F)
     check(native().dsim_rng_draws(int(seed), int(spin0), int(step), int(stream), int(n), None, out))
     return out.reshape(n, 4)
+
+
+# ---- the simulate call: config, gradients, sequencer, tensor fit ------------
+def load_config(path):
+    """sim.cfg (dSim3 or dSim2 keys) as a dict."""
+    c = _lib.Config()
+    check(native().dsim_config_load(str(path).encode(), C.byref(c)))
+    out = {}
+    for name, _ in c._fields_:
+        v = getattr(c, name)
+        out[name] = v.decode() if isinstance(v, bytes) else v
+    return out
+
+
+def parse_grads(path=None, text=None):
+    """Gradient rows [n, 6]: delta, Delta, readout (ms), Gx, Gy, Gz (mT/m)."""
+    n = C.c_uint32()
+    if path is not None:
+        f = native().dsim_grads_parse_file
+        arg = str(path).encode()
+    else:
+        f = native().dsim_grads_parse_string
+        arg = str(text).encode()
+    check(f(arg, None, 0, C.byref(n)))
+    rows = np.zeros(6 * max(n.value, 1), F)
+    check(f(arg, rows, n.value, C.byref(n)))
+    return rows[:6 * n.value].reshape(-1, 6)
+
+
+def pgse_schedule(row, dt, steps_per_update):
+    """Per-step gradient (mT/m) of one sequencer run, [steps, 3]."""
+    r = np.ascontiguousarray(row, F)
+    n = C.c_uint32()
+    check(native().dsim_pgse_schedule(r, float(dt), int(steps_per_update), None, 0, C.byref(n)))
+    g = np.zeros(3 * max(n.value, 1), F)
+    check(native().dsim_pgse_schedule(r, float(dt), int(steps_per_update), g, n.value, C.byref(n)))
+    return g[:3 * n.value].reshape(-1, 3)
+
+
+def tensor_fit(rows, signal):
+    """{tensor, eigvecs (columns), eigvals ascending, md, fa, rd}."""
+    rows = np.ascontiguousarray(rows, F).reshape(-1)
+    sig = np.ascontiguousarray(signal, np.float64)
+    T = np.zeros(9); E = np.zeros(9); ev = np.zeros(3, F)
+    md, fa, rd = C.c_float(), C.c_float(), C.c_float()
+    check(native().dsim_tensor_fit(rows, sig, len(sig), T, E, ev, C.byref(md), C.byref(fa), C.byref(rd)))
+    return {"tensor": T.reshape(3, 3), "eigvecs": E.reshape(3, 3), "eigvals": ev, "md": md.value, "fa": fa.value,
+            "rd": rd.value}
+
+
+def simulate(cfg_path, seed=1, shared_walk=False, write_out=False, cap=4096):
+    """Run a sim.cfg on the GPU: (signals [nG, 5], seconds)."""
+    out = np.zeros(5 * cap, np.float64)
+    n = C.c_uint32()
+    sec = C.c_double()
+    flags = (1 if shared_walk else 0) | (2 if write_out else 0)
+    check(native().dsim_simulate(str(cfg_path).encode(), int(seed), flags, out, cap, C.byref(n), C.byref(sec)))
+    return out[:5 * n.value].reshape(-1, 5), sec.value

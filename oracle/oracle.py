@@ -276,3 +276,86 @@ def integrate3_f64_moments(p, pos, mag, comp, fiber, vertices, trgls, triInfo, c
                                          np.ascontiguousarray(draws, np.float32).reshape(-1), mom, counts,
                                          int(nthreads))
     return capped, mom.reshape(N, nW, 3)
+
+
+# ---- the reference's driver around the path (restated in Python) -------------
+def sequencer_runs(rows, timeStep, stepsPerUpdate):
+    """dSim3/src/diffusion.cpp:522-737 (update()) replayed as a state machine:
+    the gradient passed to every updateSpins call of each run, from the call
+    that resets the spins to the one before the signal is read.  Returns a list
+    of arrays [updates, 3] (mT/m), one per gradient row, or None for a row
+    whose signal the reference never reads (the read branch is reached only
+    when no earlier branch of the same update index matches)."""
+    f32 = np.float32
+    rows = np.asarray(rows, f32).reshape(-1, 6)
+    curNumUpdates, nUpdates = 0, -1
+    lD = bD = ro = 0
+    curG = np.zeros(3, f32)
+    g = np.zeros(3, f32)
+    idx, done = 0, False
+    runs, cur = [None] * len(rows), None
+    while not done:
+        measured = False
+        if curNumUpdates <= nUpdates:
+            if curNumUpdates == 0:
+                cur = []
+                g = curG.copy()
+            elif curNumUpdates == lD and curNumUpdates < bD:
+                g = np.zeros(3, f32)
+            elif curNumUpdates == bD:
+                g = curG * f32(-1.0)
+            elif curNumUpdates == bD + lD:
+                g = np.zeros(3, f32)
+            elif curNumUpdates == bD + lD + ro:
+                runs[idx - 1] = np.array(cur, f32).reshape(-1, 3)
+                measured = True
+            curNumUpdates += 1
+        else:
+            curNumUpdates = 0
+            if idx >= len(rows):
+                done = True
+                continue
+            r = rows[idx]
+            idx += 1
+            curG = r[3:6].copy()
+            per = f32(timeStep) * f32(stepsPerUpdate)
+            lD = int(float(r[0] / per) + 0.5)
+            bD = int(float(r[1] / per) + 0.5)
+            ro = int(float(r[2] / per) + 0.5)
+            nUpdates = bD + lD + ro
+            continue
+        if cur is not None and not measured:
+            cur.append(g.copy())          # updateSpins(timeStep, stepsPerUpdate) with gradient g
+    return runs
+
+
+def tensor_fit_reference(rows, signal):
+    """computeTensor, dSim3/src/diffusion.cpp:286-511, restated with numpy:
+    ADC per non-zero gradient, rows [x^2, y^2, z^2, 2xy, 2xz, 2yz] rounded to
+    1e-6, pseudo-inverse from an SVD whose factors are rounded to 1e-6, then
+    the eigen-decomposition (ascending) and md, fa, rd as float32."""
+    rows = np.asarray(rows, np.float64).reshape(-1, 6)
+    sig = np.asarray(signal, np.float64)
+    rnd = lambda a: np.floor(a * 1000000.0 + 0.5) / 1000000.0
+    norm = np.sqrt((rows[:, 3:6] ** 2).sum(1))
+    b = ((2.0 * 3.1415926535 * 42576.0) * norm / 1000000000 * rows[:, 0]) ** 2 * (rows[:, 1] - rows[:, 0] / 3.0)
+    zero = norm == 0
+    logB0 = np.log(sig[zero] + 1e-6).mean()
+    nz = ~zero
+    adc = -1.0 / b[nz] * (np.log(sig[nz] + 1e-6) - logB0)
+    d = rows[nz, 3:6] / norm[nz, None]
+    M = rnd(np.stack([d[:, 0] ** 2, d[:, 1] ** 2, d[:, 2] ** 2, 2 * d[:, 0] * d[:, 1], 2 * d[:, 0] * d[:, 2],
+                      2 * d[:, 1] * d[:, 2]], 1))
+    U, S, Vt = np.linalg.svd(M, full_matrices=False)
+    S, U, V = rnd(S), rnd(U), rnd(Vt.T)
+    Sinv = np.where(S == 0, 0.0, 1.0 / np.where(S == 0, 1.0, S))
+    Minv = rnd(V @ np.diag(Sinv) @ U.T)
+    c = Minv @ adc
+    D = np.array([[c[0], c[3], c[4]], [c[3], c[1], c[5]], [c[4], c[5], c[2]]])
+    w, _ = np.linalg.eigh(D)
+    lam = w.astype(np.float32)
+    md = np.float32((lam[0] + lam[1] + lam[2]) / np.float32(3.0))
+    fa = np.float32(np.sqrt(1.5) * np.sqrt(((lam.astype(np.float64) - md) ** 2).sum()) /
+                    np.sqrt((lam.astype(np.float64) ** 2).sum()))
+    rd = np.float32((lam[0] + lam[1]) / np.float32(2.0))
+    return D, lam, md, fa, rd

@@ -9,6 +9,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INC = os.path.join(ROOT, "include")
 HEADERS = {"dsim.h": "libdsim_gb300.so", "dsim_batch.h": "libdsim_gb300.so", "dsim_serve.h": "libdsim_gb300.so",
+           "dsim_sim.h": "libdsim_gb300.so",
            "dsim3_abi.h": "libdsim3.so",
            "dsim2_abi.h": "libdsim2.so"}
 
