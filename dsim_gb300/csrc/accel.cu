@@ -9,9 +9,10 @@
 // list (lowest index on ties, the last-hit triangle excluded).
 //
 // Here every triangle the sub-segment hits is first collected from a finer
-// grid whose lists hold each triangle in every fine cell its bounding box
-// (widened by kAccelEps) overlaps: a triangle that the float test reports as
-// hit lies within rounding of the segment, so it is always found.  With no
+// grid whose lists hold each triangle in every fine cell it touches (a
+// separating-axis test against the cell widened by kAccelEps): a triangle
+// that the float test reports as hit lies within rounding of the segment, so
+// it is always found.  With no
 // hit (the common case) the step is done.  Otherwise the reference's
 // traversal is replayed over the found hits only: a hit counts for a
 // reference cell when the triangle is in that cell's (sorted) list, found by
@@ -44,6 +45,47 @@ __device__ __forceinline__ void tri_fine_range(const TriPlane& P, const TriBary&
     }
 }
 
+// Separating-axis test of a triangle (corners relative to the box centre)
+// against a box of half-extent h: the triangle's plane normal and the nine
+// cross products of box axes with triangle edges.  The three box axes are
+// already satisfied by the cell range (the triangle's widened bounding box).
+// Evaluated in double on float inputs, with the box widened by kAccelEps, so
+// every cell the float triangle touches passes.
+__device__ __forceinline__ bool tri_box_overlap(const double v[3][3], const double h[3]) {
+    const double e0[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+    const double e1[3] = {v[2][0] - v[1][0], v[2][1] - v[1][1], v[2][2] - v[1][2]};
+    const double e2[3] = {v[0][0] - v[2][0], v[0][1] - v[2][1], v[0][2] - v[2][2]};
+    const double* E[3] = {e0, e1, e2};
+#pragma unroll
+    for (int i = 0; i < 3; i++) {      // box axis i
+#pragma unroll
+        for (int j = 0; j < 3; j++) {  // triangle edge j: axis = unit_i x E[j]
+            double a[3] = {0.0, 0.0, 0.0};
+            const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+            a[i1] = -E[j][i2];
+            a[i2] = E[j][i1];
+            const double p0 = a[0] * v[0][0] + a[1] * v[0][1] + a[2] * v[0][2];
+            const double p1 = a[0] * v[1][0] + a[1] * v[1][1] + a[2] * v[1][2];
+            const double p2 = a[0] * v[2][0] + a[1] * v[2][1] + a[2] * v[2][2];
+            const double r = h[0] * fabs(a[0]) + h[1] * fabs(a[1]) + h[2] * fabs(a[2]);
+            const double mn = fmin(p0, fmin(p1, p2)), mx = fmax(p0, fmax(p1, p2));
+            if (mn > r || mx < -r) return false;
+        }
+    }
+    const double n[3] = {e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0]};
+    const double d = n[0] * v[0][0] + n[1] * v[0][1] + n[2] * v[0][2];
+    const double r = h[0] * fabs(n[0]) + h[1] * fabs(n[1]) + h[2] * fabs(n[2]);
+    return fabs(d) <= r;
+}
+
+// box of fine cell index k on one axis, widened by kAccelEps; the outermost
+// cells reach to infinity because coordinates beyond the box clamp into them
+__device__ __forceinline__ void cell_span(uint32_t k, uint32_t nf, double& lo, double& hi) {
+    const double Lf = 2.0 / (double)nf;
+    lo = (k == 0) ? -1.0e6 : -1.0 + (double)k * Lf - (double)kAccelEps;
+    hi = (k == nf - 1) ? 1.0e6 : -1.0 + (double)(k + 1) * Lf + (double)kAccelEps;
+}
+
 template <bool FILL>
 __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                               const TriBary* __restrict__ bary, uint32_t nf, float invLf,
@@ -55,9 +97,28 @@ __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
     TriBary B = bary[t];
     uint32_t lo[3], hi[3];
     tri_fine_range(P, B, invLf, nf, lo, hi);
+    // corners as the intersection test sees the triangle: p1, p1 + v, p1 + u
+    const float c0[3] = {P.p1x, P.p1y, P.p1z};
+    const float c1[3] = {P.p1x + B.vx, P.p1y + B.vy, P.p1z + B.vz};
+    const float c2[3] = {P.p1x + B.ux, P.p1y + B.uy, P.p1z + B.uz};
+    const bool many = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) > 1;
     for (uint32_t x = lo[0]; x <= hi[0]; x++)
         for (uint32_t y = lo[1]; y <= hi[1]; y++)
             for (uint32_t z = lo[2]; z <= hi[2]; z++) {
+                if (many) {
+                    double bl[3], bh[3], ctr[3], h[3], v[3][3];
+                    cell_span(x, nf, bl[0], bh[0]);
+                    cell_span(y, nf, bl[1], bh[1]);
+                    cell_span(z, nf, bl[2], bh[2]);
+                    for (int k = 0; k < 3; k++) {
+                        ctr[k] = 0.5 * (bl[k] + bh[k]);
+                        h[k] = 0.5 * (bh[k] - bl[k]);
+                        v[0][k] = (double)c0[k] - ctr[k];
+                        v[1][k] = (double)c1[k] - ctr[k];
+                        v[2][k] = (double)c2[k] - ctr[k];
+                    }
+                    if (!tri_box_overlap(v, h)) continue;
+                }
                 uint32_t key = morton3(x, y, z);
                 uint32_t slot = atomicAdd(counter + key, 1u);
                 if (FILL) {
