@@ -90,7 +90,7 @@ template <bool FILL>
 __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                               const TriBary* __restrict__ bary, uint32_t nf, float invLf,
                               uint32_t* counter, const uint32_t* __restrict__ start, AccelRec* rec,
-                              uint32_t* tri, AccelRecWide* recw) {
+                              uint32_t* tri, AccelRecWide* recw, AccelRecFull* recf) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nT) return;
     TriPlane P = plane[t];
@@ -123,7 +123,14 @@ __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
                 uint32_t slot = atomicAdd(counter + key, 1u);
                 if (FILL) {
                     const float4 q = make_float4(P.nx, P.ny, P.nz, P.nx * P.p1x + P.ny * P.p1y + P.nz * P.p1z);
-                    if (recw) {
+                    if (recf) {
+                        AccelRecFull r;
+                        r.a = make_float4(P.nx, P.ny, P.nz, P.vv);
+                        r.b = make_float4(P.p1x, P.p1y, P.p1z, __uint_as_float(t));
+                        r.c = make_float4(B.ux, B.uy, B.uz, B.vx);
+                        r.d = make_float4(B.vy, B.vz, B.uv, B.uu);
+                        recf[start[key] + slot] = r;
+                    } else if (recw) {
                         AccelRecWide r;
                         r.q = q;
                         r.pt = make_float4(P.p1x, P.p1y, P.p1z, __uint_as_float(t));
@@ -140,13 +147,13 @@ __global__ void k_accel_cells(uint32_t nT, const TriPlane* __restrict__ plane,
 
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st) {
+                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st, AccelRecFull* recf) {
     if (nT == 0) return kOk;
     float invLf = (float)nf / 2.0f;
     if (fill)
-        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw);
+        k_accel_cells<true><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw, recf);
     else
-        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw);
+        k_accel_cells<false><<<(nT + 127) / 128, 128, 0, st>>>(nT, plane, bary, nf, invLf, counter, start, rec, tri, recw, recf);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

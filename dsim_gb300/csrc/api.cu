@@ -71,7 +71,8 @@ struct dsim_mesh {
     AccelRec* acc_rec = nullptr;
     uint32_t* acc_tri = nullptr;
     AccelRecWide* acc_recw = nullptr;
-    uint32_t accWide = 1;  // 32-byte fine-grid records (0: 16-byte)
+    AccelRecFull* acc_recf = nullptr;
+    uint32_t accWide = 1;  // fine-grid records: 0 16-byte, 1 32-byte, 2 64-byte
     float maxabs[3] = {1.0f, 1.0f, 1.0f};  // max(1, max |vertex coordinate|) per axis, as initFibers keeps
     MeshDev dev() const {
         MeshDev g;
@@ -81,16 +82,16 @@ struct dsim_mesh {
     }
     AccelDev acc() const {
         AccelDev a;
-        a.start = acc_start; a.rec = acc_rec; a.tri = acc_tri; a.recw = acc_recw; a.nf = nf;
-        a.invLf = (float)nf / 2.0f; a.wide = acc_recw ? 1u : 0u;
+        a.start = acc_start; a.rec = acc_rec; a.tri = acc_tri; a.recw = acc_recw; a.recf = acc_recf; a.nf = nf;
+        a.invLf = (float)nf / 2.0f; a.wide = acc_recf ? 2u : (acc_recw ? 1u : 0u);
         return a;
     }
 };
 
 // (Re)build the fine acceleration grid with nf cells per axis (0 removes it).
 static int accel_build(dsim_mesh* m, uint32_t nf) {
-    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
-    m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr;
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw); cudaFree(m->acc_recf);
+    m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr; m->acc_recf = nullptr;
     m->nf = 0; m->accEntries = 0; m->accBytes = 0;
     if (nf == 0) return kOk;
     if (nf > 1024) { set_last_error(kErrTooLarge, "accel grid: %u cells per axis > 1024", nf); return kErrTooLarge; }
@@ -110,14 +111,16 @@ static int accel_build(dsim_mesh* m, uint32_t nf) {
         if (cudaMemcpyAsync(&total, m->acc_start + nkeys, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->accEntries = total;
-        if (m->accWide) {
+        if (m->accWide == 2) {
+            if ((rc = dev_alloc(&m->acc_recf, total, &m->accBytes))) break;
+        } else if (m->accWide) {
             if ((rc = dev_alloc(&m->acc_recw, total, &m->accBytes))) break;
         } else {
             if ((rc = dev_alloc(&m->acc_rec, total, &m->accBytes))) break;
             if ((rc = dev_alloc(&m->acc_tri, total, &m->accBytes))) break;
         }
         if (cudaMemsetAsync(counter, 0, (size_t)nkeys * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
-        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, m->acc_tri, m->acc_recw, st))) break;
+        if ((rc = launch_accel_cells(true, m->nT, m->plane, m->bary, nf, counter, m->acc_start, m->acc_rec, m->acc_tri, m->acc_recw, st, m->acc_recf))) break;
         if (cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }
         m->nf = nf;
     } while (0);
@@ -125,8 +128,8 @@ static int accel_build(dsim_mesh* m, uint32_t nf) {
     cudaFree(counter);
     cudaFree(scratch);
     if (rc) {
-        cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
-        m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr; m->nf = 0;
+        cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw); cudaFree(m->acc_recf);
+        m->acc_start = nullptr; m->acc_rec = nullptr; m->acc_tri = nullptr; m->acc_recw = nullptr; m->acc_recf = nullptr; m->nf = 0;
     }
     return rc;
 }
@@ -150,8 +153,8 @@ namespace dsim {
 // device views for the batch module (batch.cu)
 int mesh_views(const dsim_mesh* m, MeshDev* g, AccelDev* a) {
     if (!m || !g || !a) return kErrInvalid;
-    if (m->nf == 0 || !m->acc_recw) {
-        set_last_error(kErrInvalid, "batch: the mesh needs its fine grid with 32-byte records");
+    if (m->nf == 0 || !(m->acc_recw || m->acc_recf)) {
+        set_last_error(kErrInvalid, "batch: the mesh needs its fine grid with 32- or 64-byte records");
         return kErrInvalid;
     }
     *g = m->dev();
@@ -225,7 +228,7 @@ static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
     cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
-    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw);
+    cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw); cudaFree(m->acc_recf);
     delete m;
 }
 
@@ -815,11 +818,11 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis) {
 }
 
 int dsim_mesh_set_records(dsim_mesh* m, uint32_t bytesPerRecord) {
-    if (!m || (bytesPerRecord != 16 && bytesPerRecord != 32)) {
-        set_last_error(kErrInvalid, "record size must be 16 or 32 bytes");
+    if (!m || (bytesPerRecord != 16 && bytesPerRecord != 32 && bytesPerRecord != 64)) {
+        set_last_error(kErrInvalid, "record size must be 16, 32 or 64 bytes");
         return kErrInvalid;
     }
-    m->accWide = bytesPerRecord == 32 ? 1u : 0u;
+    m->accWide = bytesPerRecord == 64 ? 2u : (bytesPerRecord == 32 ? 1u : 0u);
     return accel_build(m, m->nf);
 }
 
@@ -905,8 +908,8 @@ int dsim_timer_stop(dsim_spins* s, float* ms) {
 
 int dsim_mesh_compartments(dsim_mesh* m, dsim_spins* s, uint64_t seed, float startBoxSize, uint32_t* moved) {
     if (!m || !s) { set_last_error(kErrInvalid, "dsim_mesh_compartments: null argument"); return kErrInvalid; }
-    if (m->nf == 0 || !m->acc_recw) {
-        set_last_error(kErrInvalid, "dsim_mesh_compartments: needs the fine grid with 32-byte records");
+    if (m->nf == 0) {
+        set_last_error(kErrInvalid, "dsim_mesh_compartments: needs the fine grid");
         return kErrInvalid;
     }
     uint32_t* dmoved = nullptr;

@@ -79,15 +79,9 @@ __global__ void __launch_bounds__(128) k_compartments(MeshDev g, AccelDev acc, S
                         const uint32_t key = morton3(c0, c1, c2);
                         const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
                         for (uint32_t k = b0; k < b1; k++) {
-                            const float4 q = __ldg(&acc.recw[k].q);
-                            if (!plane_may_cross(q, sx, sy, sz, dx, dy, dz)) continue;
-                            const float4 pt = __ldg(&acc.recw[k].pt);
-                            const uint32_t t = __float_as_uint(pt.w);
                             FastHit h;
-                            const float vv = __ldg(&g.plane[t].vv);
-                            if (!test_rec(g, make_float4(q.x, q.y, q.z, pt.x), make_float4(pt.y, pt.z, vv, pt.w),
-                                          sx, sy, sz, dx, dy, dz, h))
-                                continue;
+                            if (!test_entry(g, acc, k, 0xFFFFFFFFu, sx, sy, sz, dx, dy, dz, h)) continue;
+                            const uint32_t t = h.t;
                             // count the crossing in the cell that holds it
                             if (fine_coord(h.x, acc.invLf, acc.nf) != c0 || fine_coord(h.y, acc.invLf, acc.nf) != c1 ||
                                 fine_coord(h.z, acc.invLf, acc.nf) != c2)

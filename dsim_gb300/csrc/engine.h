@@ -71,11 +71,17 @@ struct __align__(16) AccelRec {
 struct __align__(32) AccelRecWide {
     float4 q, pt;
 };
+// 64-byte record: everything the exact test reads, so a record is decided
+// with no dependent load: {n, vv} {p1, t} {u, v.x} {v.y, v.z, uv, uu}
+struct __align__(16) AccelRecFull {
+    float4 a, b, c, d;
+};
 struct AccelDev {
     const uint32_t* start;  // Morton key -> first record (keys + 1 entries)
     const AccelRec* rec;    // 16-byte records (wide == 0)
     const uint32_t* tri;    // triangle of each record (wide == 0)
     const AccelRecWide* recw;  // 32-byte records (wide == 1)
+    const AccelRecFull* recf;  // 64-byte records (wide == 2)
     uint32_t nf;            // fine cells per axis
     float invLf;            // nf / 2
     uint32_t wide;
@@ -93,7 +99,7 @@ __host__ __device__ inline uint32_t accel_keys(uint32_t nf) {
 }
 int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriBary* bary,
                        uint32_t nf, uint32_t* counter, const uint32_t* start, AccelRec* rec,
-                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st);
+                       uint32_t* tri, AccelRecWide* recw, cudaStream_t st, AccelRecFull* recf = nullptr);
 int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
                       uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st);
 int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,

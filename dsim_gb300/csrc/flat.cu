@@ -29,7 +29,7 @@
 
 namespace dsim {
 
-template <bool STATS, int MINB>
+template <bool STATS, int MINB, int LAYOUT>
 __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g, AccelDev acc,
                                                                        MeshStepArgs a, SpinsSorted S,
                                                                        int rng) {
@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
         {
             bool found;
             FastHit best;
-            flat_round(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
+            PrecCount pcnt;
+            flat_round_mode<false, LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pcnt);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -135,10 +136,20 @@ int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepA
                           const SpinsSorted& S, int rng, cudaStream_t st, int occupancy) {
     if (S.N == 0 || a.iterations == 0) return kOk;
     dim3 block(kFlatThreads), grid((S.N + kFlatThreads - 1) / kFlatThreads);
-    if (a.tested) k_mesh_step_flat<true, 4><<<grid, block, 0, st>>>(g, acc, a, S, rng);
-    else if (occupancy >= 8) k_mesh_step_flat<false, 8><<<grid, block, 0, st>>>(g, acc, a, S, rng);
-    else if (occupancy >= 6) k_mesh_step_flat<false, 6><<<grid, block, 0, st>>>(g, acc, a, S, rng);
-    else k_mesh_step_flat<false, 4><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    // one instantiation per record layout keeps each kernel's registers to its own path
+    if (a.tested) k_mesh_step_flat<true, 4, 0><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    else if (acc.wide == 2) {
+        if (occupancy >= 8) k_mesh_step_flat<false, 8, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+        else if (occupancy >= 6) k_mesh_step_flat<false, 6, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+        else k_mesh_step_flat<false, 4, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    } else if (acc.wide == 1) {
+        if (occupancy >= 8) k_mesh_step_flat<false, 8, 1><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+        else if (occupancy >= 6) k_mesh_step_flat<false, 6, 1><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+        else k_mesh_step_flat<false, 4, 1><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    } else {
+        if (occupancy >= 6) k_mesh_step_flat<false, 6, 0><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+        else k_mesh_step_flat<false, 4, 0><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    }
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

@@ -95,7 +95,9 @@ __device__ __forceinline__ bool test_wide_mode(const MeshDev& g, float4 q, float
 // return, for open lanes, found / best hold the reference's collision result.
 // PREC selects the precision form's FP64 re-test of near-degenerate
 // intersections (counted in pc); the plain form is the reference's FP32 test.
-template <bool PREC>
+// LAYOUT: 1 or 2 compile only the 32- or 64-byte record path; 0 dispatches
+// on acc.wide at run time (every layout)
+template <bool PREC, int LAYOUT = 0>
 __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
                                                 uint32_t lane, bool open, float ox, float oy, float oz,
                                                 float px, float py, float pz, uint32_t excluded,
@@ -145,7 +147,37 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
         const uint32_t rincl = warp_incl_scan(cnt, lane);
         const uint32_t rtotal = __shfl_sync(FULL, rincl, 31);
         const uint32_t rbase = b0 - (rincl - cnt);  // record index = rbase of its item + flat index
-        if (acc.wide) {
+        if (LAYOUT == 2 || (LAYOUT == 0 && acc.wide == 2)) {
+            for (uint32_t rb = 0; rb < rtotal; rb += 64) {
+                const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
+                const uint32_t j0 = min(warp_find(rincl, r0), 31u);
+                const uint32_t j1 = min(warp_find(rincl, r1), 31u);
+                const uint32_t e0 = __shfl_sync(FULL, rbase, j0) + r0;
+                const uint32_t e1 = __shfl_sync(FULL, rbase, j1) + r1;
+                const uint32_t o0 = __shfl_sync(FULL, ow, j0);
+                const uint32_t o1 = __shfl_sync(FULL, ow, j1);
+                const bool v0 = r0 < rtotal, v1 = r1 < rtotal;
+                AccelRecFull f0, f1;
+                if (v0) f0 = load_full(acc.recf + e0);
+                if (v1) f1 = load_full(acc.recf + e1);
+                FastHit h;
+                if (PREC) {
+                    if (v0 && __float_as_uint(f0.b.w) != H.excl[o0] &&
+                        test_prec(g, f0.a.x, f0.a.y, f0.a.z, f0.b.x, f0.b.y, f0.b.z, __float_as_uint(f0.b.w),
+                                  H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h, pc))
+                        flat_file_hit(H, o0, h);
+                    if (v1 && __float_as_uint(f1.b.w) != H.excl[o1] &&
+                        test_prec(g, f1.a.x, f1.a.y, f1.a.z, f1.b.x, f1.b.y, f1.b.z, __float_as_uint(f1.b.w),
+                                  H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h, pc))
+                        flat_file_hit(H, o1, h);
+                } else {
+                    if (v0 && test_full(f0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h))
+                        flat_file_hit(H, o0, h);
+                    if (v1 && test_full(f1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h))
+                        flat_file_hit(H, o1, h);
+                }
+            }
+        } else if (LAYOUT == 1 || (LAYOUT == 0 && acc.wide)) {
             for (uint32_t rb = 0; rb < rtotal; rb += 64) {
                 const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
                 const uint32_t j0 = min(warp_find(rincl, r0), 31u);
@@ -166,7 +198,7 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                                            H.dx[o1], H.dy[o1], H.dz[o1], h, pc))
                     flat_file_hit(H, o1, h);
             }
-        } else {
+        } else if (LAYOUT == 0) {
             for (uint32_t rb = 0; rb < rtotal; rb += 32) {
                 const uint32_t r0 = rb + lane;
                 const uint32_t j0 = min(warp_find(rincl, r0), 31u);

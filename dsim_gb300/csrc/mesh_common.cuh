@@ -58,8 +58,9 @@ __device__ __forceinline__ uint32_t ref_coord(float p, float L, uint32_t n) {
 
 // full test of one accel record against the sub-segment (same float
 // expressions as triCollDetect); returns true and fills h on a hit
-__device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, float ox, float oy,
-                                         float oz, float dx, float dy, float dz, FastHit& h) {
+// a = {n, p1.x}, b = {p1.y, p1.z, vv, t}, u4 = {u, v.x}, v4 = {v.y, v.z, uv, uu}
+__device__ __forceinline__ bool test_rec_uv(float4 a, float4 b, float4 u4, float4 v4, float ox, float oy,
+                                            float oz, float dx, float dy, float dz, FastHit& h) {
     float num = a.x * (a.w - ox) + a.y * (b.x - oy) + a.z * (b.y - oz);
     float den = a.x * dx + a.y * dy + a.z * dz;
     if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
@@ -68,8 +69,6 @@ __device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, f
     float r = num / den;
     if (!((0.0f < r) & (r < 1.0f))) return false;
     uint32_t t = __float_as_uint(b.w);
-    const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
-    float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);
     float wx = ox + r * dx - a.w;
     float wy = oy + r * dy - b.x;
     float wz = oz + r * dz - b.y;
@@ -90,6 +89,33 @@ __device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, f
     }
     h.type = type;
     return true;
+}
+
+// the same, reading u, v, uv, uu from the triangle's records
+__device__ __forceinline__ bool test_rec(const MeshDev& g, float4 a, float4 b, float ox, float oy,
+                                         float oz, float dx, float dy, float dz, FastHit& h) {
+    float num = a.x * (a.w - ox) + a.y * (b.x - oy) + a.z * (b.y - oz);
+    float den = a.x * dx + a.y * dy + a.z * dz;
+    if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
+        ((__float_as_uint(num) ^ __float_as_uint(den)) & 0x80000000u))
+        return false;
+    const float4* bb = reinterpret_cast<const float4*>(g.bary + __float_as_uint(b.w));
+    return test_rec_uv(a, b, __ldg(bb), __ldg(bb + 1), ox, oy, oz, dx, dy, dz, h);
+}
+
+// a 64-byte record already in registers (no dependent load)
+__device__ __forceinline__ bool test_full(const AccelRecFull& r, uint32_t excl, float ox, float oy, float oz,
+                                          float dx, float dy, float dz, FastHit& h) {
+    if (__float_as_uint(r.b.w) == excl) return false;
+    return test_rec_uv(make_float4(r.a.x, r.a.y, r.a.z, r.b.x), make_float4(r.b.y, r.b.z, r.a.w, r.b.w), r.c, r.d,
+                       ox, oy, oz, dx, dy, dz, h);
+}
+
+__device__ __forceinline__ AccelRecFull load_full(const AccelRecFull* p) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+    AccelRecFull r;
+    r.a = __ldg(q); r.b = __ldg(q + 1); r.c = __ldg(q + 2); r.d = __ldg(q + 3);
+    return r;
 }
 
 
@@ -136,6 +162,7 @@ __device__ __forceinline__ bool test_split(const MeshDev& g, float4 q, float4 pt
 __device__ __forceinline__ bool test_entry(const MeshDev& g, const AccelDev& acc, uint32_t k,
                                            uint32_t excl, float ox, float oy, float oz, float dx,
                                            float dy, float dz, FastHit& h) {
+    if (acc.wide == 2) return test_full(load_full(acc.recf + k), excl, ox, oy, oz, dx, dy, dz, h);
     if (acc.wide) {
         const float4 q = __ldg(&acc.recw[k].q);
         if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
@@ -232,6 +259,12 @@ __device__ __forceinline__ bool test_entry_mode(const MeshDev& g, const AccelDev
                                                 float ox, float oy, float oz, float dx, float dy, float dz,
                                                 FastHit& h, PrecCount& pc) {
     if (!PREC) return test_entry(g, acc, k, excl, ox, oy, oz, dx, dy, dz, h);
+    if (acc.wide == 2) {
+        const AccelRecFull r = load_full(acc.recf + k);
+        const uint32_t t = __float_as_uint(r.b.w);
+        if (t == excl) return false;
+        return test_prec(g, r.a.x, r.a.y, r.a.z, r.b.x, r.b.y, r.b.z, t, ox, oy, oz, dx, dy, dz, h, pc);
+    }
     const float4 q = __ldg(&acc.recw[k].q);
     if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
     const float4 pt = __ldg(&acc.recw[k].pt);

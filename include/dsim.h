@@ -77,7 +77,8 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 /* fine-grid record size: 32 (default) holds the plane data for the exact
  * plane test; 16 holds a prefilter record only (half the bytes, one more
- * dependent load for records that pass) */
+ * dependent load for records that pass); 64 holds everything the exact
+ * triangle test reads (no dependent load) */
 int dsim_mesh_set_records(dsim_mesh* m, uint32_t bytesPerRecord);
 int dsim_mesh_accel_info(const dsim_mesh* m, uint64_t info[3]);
 /* Compartment and fiber of every spin of `s` from its position (the

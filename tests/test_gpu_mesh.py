@@ -53,7 +53,9 @@ def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
     ("AM", 0.05, 37, 7, None, 16), ("AM", 0.05, 300, 0, None, None), ("G", 0.3, 13, 1, None, 16),
     ("AM", 0.05, None, 20, 1, None), ("AM", 0.05, None, 20, 2, 16), ("AM", 0.05, 75, 20, 3, None),
     ("AM", 0.05, None, 20, 5, None), ("G", 0.3, 37, 7, 6, 16), ("AM", 0.05, 300, 0, 5, None),
-    ("G", 0.0, 75, 20, 5, 16), ("G", 0.3, None, 7, 4, None), ("AM", 0.05, 100, 20, 7, None)])
+    ("G", 0.0, 75, 20, 5, 16), ("G", 0.3, None, 7, 4, None), ("AM", 0.05, 100, 20, 7, None),
+    ("AM", 0.05, None, 20, None, 64), ("G", 0.3, 37, 7, 5, 64), ("AM", 0.05, 300, 0, 4, 64),
+    ("G", 0.3, 13, 1, 1, 64)])
 def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort, kernel, records):
     """accel None: default fine grid; 0: reference-grid scan; other: fine
     cells per axis (coarser and finer than the reference grid).  sort: steps
