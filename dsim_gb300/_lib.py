@@ -166,6 +166,7 @@ def _declare_batch(L):
         "dsim_batch_counts": (i32, [VP, u32, U64]),
         "dsim_batch_status": (u32, [VP]),
         "dsim_batch_precision_counts": (i32, [VP, u32, U64]),
+        "dsim_batch_get_precise": (i32, [VP, u32, F64, F64]),
         "dsim_batch_retire": (i32, [VP, u32]),
         "dsim_batch_compact": (i32, [VP]),
         "dsim_batch_info": (i32, [VP, U64]),

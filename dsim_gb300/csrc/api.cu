@@ -63,6 +63,7 @@ struct dsim_mesh {
     TriBary* bary = nullptr;
     uint32_t* cell_start = nullptr;
     uint32_t* cell_tri = nullptr;
+    Tri64* tri64 = nullptr;  // FP64 helpers, built for the first precision-form job
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
     uint32_t kernel = 6;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened (8, 6, 4)
@@ -77,6 +78,7 @@ struct dsim_mesh {
     MeshDev dev() const {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
+        g.tri64 = tri64;
         g.n = n; g.L = L;
         return g;
     }
@@ -161,6 +163,17 @@ int mesh_views(const dsim_mesh* m, MeshDev* g, AccelDev* a) {
     *a = m->acc();
     return kOk;
 }
+int mesh_tri64(dsim_mesh* m) {
+    if (!m) return kErrInvalid;
+    if (m->tri64 || m->nT == 0) return kOk;
+    Tri64* t = nullptr;
+    int rc = dev_alloc(&t, m->nT, &m->bytes);
+    if (rc) return rc;
+    if ((rc = launch_tri64(m->nT, m->V, m->trgls, t, 0))) { cudaFree(t); return rc; }
+    DSIM_CUDA_TRY(cudaDeviceSynchronize());
+    m->tri64 = t;
+    return kOk;
+}
 int cyl_view(const dsim_cyl* c, CylDev* g) {
     if (!c || !g) return kErrInvalid;
     *g = c->dev();
@@ -227,7 +240,7 @@ struct dsim_spins {
 static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
-    cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri);
+    cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri); cudaFree(m->tri64);
     cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw); cudaFree(m->acc_recf);
     delete m;
 }

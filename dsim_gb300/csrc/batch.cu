@@ -30,6 +30,7 @@
 #include "cyl_common.cuh"
 #include "engine.h"
 #include "flat_round.cuh"
+#include "prec_round.cuh"
 
 namespace dsim {
 
@@ -51,7 +52,7 @@ struct JobDev {
     const float* wave;            // w[steps]
     uint32_t key0, key1;
     uint32_t flags;               // DSIM_JOB_PRECISE
-    uint32_t pad_;
+    float spinR;                  // spin radius (the precision form clamps to +-(1 - spinR) in FP64)
 };
 
 static_assert(sizeof(JobDev) % 4 == 0 && sizeof(SubDev) % 4 == 0, "records are copied by 32-bit words");
@@ -59,13 +60,16 @@ static_assert(sizeof(JobDev) % 4 == 0 && sizeof(SubDev) % 4 == 0, "records are c
 // packed spin state; meta = compartment | fiber << 8 (cylinders: imo | nearest << 8)
 static constexpr int kBF = 10;  // float fields: x y z mx my mz cx cy cz mag
 static constexpr int kBU = 3;   // uint fields: meta job id
+static constexpr int kBD = 4;   // double fields of precision-form jobs: x y z mag (null until the first one)
 struct BatchSpins {
     float* f[kBF];
     uint32_t* u[kBU];
+    double* d[kBD];
     uint32_t N;
 };
 enum { F_X, F_Y, F_Z, F_MX, F_MY, F_MZ, F_CX, F_CY, F_CZ, F_MAG };
 enum { U_META, U_JOB, U_ID };
+enum { D_X, D_Y, D_Z, D_MAG };
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     float y = v - c;
@@ -74,13 +78,16 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
     s = t;
 }
 
-// PREC: the instantiation for precision-form jobs (FP64 re-test of
-// near-degenerate intersections); each instantiation skips the other's warps
-template <int MINB, bool PREC>
+// The plain form has one instantiation per fine-grid record layout (LAYOUT 1:
+// 32-byte, 2: 64-byte records), each advancing only the mesh jobs whose
+// substrate uses it, so no kernel carries the registers of a record path it
+// does not run; cylinder jobs run in the one launch given cylHere.
+// Precision-form jobs run in k_batch_step64.
+template <int MINB, int LAYOUT>
 __global__ void __launch_bounds__(kFlatThreads, MINB)
 k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
              const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
-             unsigned long long* jobCounts) {
+             unsigned long long* jobCounts, uint32_t cylHere) {
     __shared__ FlatWarp wh[kFlatWarps];
     // gradient moments and their compensation live in shared memory (touched
     // once per step), which keeps the collision loop's registers free
@@ -108,7 +115,8 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
-    if (((J.flags & DSIM_JOB_PRECISE) != 0) != PREC) return;  // warp-uniform
+    if (J.flags & DSIM_JOB_PRECISE) return;  // warp-uniform
+    if (subS[wi].kind == kSubMesh ? subS[wi].acc.wide != (uint32_t)LAYOUT : !cylHere) return;
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;  // not started or finished (warp-uniform)
@@ -125,7 +133,6 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     const uint32_t k0 = J.key0, k1 = J.key1;
     const float* __restrict__ wave = J.wave;
     uint32_t nrefl = 0, nperm = 0, st = 0;
-    PrecCount pc;
     const SubDev& sub = subS[wi];
     if (sub.kind == kSubMesh) {
         const MeshDev& g = sub.g;
@@ -154,7 +161,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
             const bool open = active;
             bool found;
             FastHit best;
-            flat_round_mode<PREC>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pc);
+            flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -216,22 +223,152 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
         S.f[F_MAG][i] = mag;
         S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
     }
-    // per-job counters {reflections, permeations, exact tests, FP64 re-tests}: one atomic per warp
-    unsigned long long r = nrefl, p = nperm, te = pc.tests, re = pc.retests;
+    // per-job counters {reflections, permeations}: one atomic per warp
+    unsigned long long r = nrefl, p = nperm;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         r += __shfl_down_sync(FULL, r, o);
         p += __shfl_down_sync(FULL, p, o);
-        if (PREC) {
-            te += __shfl_down_sync(FULL, te, o);
-            re += __shfl_down_sync(FULL, re, o);
-        }
     }
     if (lane == 0) {
         if (r) atomicAdd(jobCounts + 4 * jb, r);
         if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
-        if (PREC && te) atomicAdd(jobCounts + 4 * jb + 2, te);
-        if (PREC && re) atomicAdd(jobCounts + 4 * jb + 3, re);
+    }
+    if (st) atomicOr(status, st);
+}
+
+// Precision-form mesh jobs (DSIM_JOB_PRECISE): the step of cpuIntegrate
+// (dSim3/src/spinKernelCpu.cpp:430-499) in FP64 -- position, sub-segments,
+// hits and reflections (prec_round.cuh), the clamp to +-(1 - spinRadius), the
+// T2 decay and the gradient moments M += w(t) pos(t) -- on the same Philox
+// draws as the plain form.  Positions and magnitudes persist in the double
+// fields; the float fields receive their rounded values (sort keys, float
+// readers) and the moment pair (m, c) holds M as m - c.
+__global__ void __launch_bounds__(kFlatThreads, 2)
+k_batch_step64(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
+               const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
+               unsigned long long* jobCounts) {
+    __shared__ FlatWarp wh[kFlatWarps];
+    __shared__ PrecWarp wp[kFlatWarps];
+    __shared__ JobDev jobS[kFlatWarps];
+    __shared__ SubDev subS[kFlatWarps];
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t wi = threadIdx.x >> 5;
+    FlatWarp& H = wh[wi];
+    PrecWarp& P = wp[wi];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
+    const uint32_t jb = S.u[U_JOB][i & ~31u];
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(jobS + wi);
+        for (uint32_t k = lane; k < sizeof(JobDev) / 4; k += 32) dst[k] = __ldg(src + k);
+        __syncwarp();
+        const uint32_t* s2 = reinterpret_cast<const uint32_t*>(subs + jobS[wi].sub);
+        uint32_t* d2 = reinterpret_cast<uint32_t*>(subS + wi);
+        for (uint32_t k = lane; k < sizeof(SubDev) / 4; k += 32) d2[k] = __ldg(s2 + k);
+        __syncwarp();
+    }
+    const JobDev& J = jobS[wi];
+    if (!(J.flags & DSIM_JOB_PRECISE)) return;  // warp-uniform
+    const uint32_t now = *stepNow;
+    const uint32_t start = J.start, steps = J.steps;
+    if (now < start || now - start >= steps) return;
+    const uint32_t ls0 = now - start;
+    const uint32_t nsteps = min(chunk, steps - ls0);
+    const uint32_t id = S.u[U_ID][i];
+    const bool valid = id != 0xFFFFFFFFu;
+    double x = 0.0, y = 0.0, z = 0.0, mag = 0.0, Mx = 0.0, My = 0.0, Mz = 0.0;
+    uint32_t comp = 0, fiber = 0;
+    if (valid) {
+        x = S.d[D_X][i]; y = S.d[D_Y][i]; z = S.d[D_Z][i]; mag = S.d[D_MAG][i];
+        Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
+        My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
+        Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
+        const uint32_t meta = S.u[U_META][i];
+        comp = meta & 0xFFu; fiber = meta >> 8;
+    }
+    const MeshDev& g = subS[wi].g;
+    const AccelDev& acc = subS[wi].acc;
+    const double perm = (double)J.perm;
+    const double hiC = 1.0 - (double)J.spinR, loC = -1.0 + (double)J.spinR;
+    const uint32_t reflType = J.reflType, maxSub = J.maxSub;
+    const uint32_t k0 = J.key0, k1 = J.key1;
+    const float* __restrict__ wave = J.wave;
+    uint32_t nrefl = 0, nperm = 0, st = 0, it = 0, excluded = 0xFFFFFFFFu, sub_n = 0;
+    PrecCount pc;
+    bool active = valid && nsteps > 0;
+    bool fresh = active;
+    double u = 1.0, umax = 1.0, umin = 0.0;
+    double ox = x, oy = y, oz = z, px = x, py = y, pz = z;
+    while (__any_sync(FULL, active)) {
+        if (fresh) {
+            const Draw d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+            ox = x; oy = y; oz = z;
+            const double sd = (double)J.sd[comp & 3u];
+            px = x + (double)d.nx * sd; py = y + (double)d.ny * sd; pz = z + (double)d.nz * sd;
+            u = (double)d.u;
+            excluded = 0xFFFFFFFFu;
+            umax = 1.0; umin = 0.0;
+            sub_n = 0;
+            fresh = false;
+        }
+        const bool open = active;
+        bool found;
+        uint32_t ht = 0, htype = 0;
+        double hx = 0.0, hy = 0.0, hz = 0.0;
+        prec_round(H, P, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, ht, htype, hx, hy, hz, pc);
+        if (open) {
+            bool finish = !found;
+            if (found) {
+                apply_hit64(g, ht, htype, hx, hy, hz, u, perm, reflType, umax, umin, ox, oy, oz, px, py, pz, comp,
+                            fiber, excluded, nrefl, nperm);
+                if (++sub_n >= maxSub) {
+                    st |= kStatusSubsegCap;
+                    finish = true;
+                }
+            }
+            if (finish) {
+                if (px > hiC) px = hiC; else if (px < loC) px = loC;
+                if (py > hiC) py = hiC; else if (py < loC) py = loC;
+                if (pz > hiC) pz = hiC; else if (pz < loC) pz = loC;
+                x = px; y = py; z = pz;
+                const float T2 = J.T2[comp & 3u];
+                if (T2 > 0.0f) mag += -mag / (double)T2 * (double)J.dt;
+                const double w = (double)__ldg(wave + ls0 + it);
+                Mx += w * x; My += w * y; Mz += w * z;
+                if (++it >= nsteps) active = false;
+                else fresh = true;
+            }
+        }
+        __syncwarp();
+    }
+    if (valid) {
+        S.d[D_X][i] = x; S.d[D_Y][i] = y; S.d[D_Z][i] = z; S.d[D_MAG][i] = mag;
+        S.f[F_X][i] = (float)x; S.f[F_Y][i] = (float)y; S.f[F_Z][i] = (float)z;
+        S.f[F_MAG][i] = (float)mag;
+        const float mx = (float)Mx, my = (float)My, mz = (float)Mz;
+        S.f[F_MX][i] = mx; S.f[F_MY][i] = my; S.f[F_MZ][i] = mz;
+        S.f[F_CX][i] = (float)((double)mx - Mx);
+        S.f[F_CY][i] = (float)((double)my - My);
+        S.f[F_CZ][i] = (float)((double)mz - Mz);
+        S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
+    }
+    // per-job counters {reflections, permeations, records examined, FP64 triangle tests}
+    unsigned long long r = nrefl, p = nperm, te = pc.records, ex = pc.exact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        p += __shfl_down_sync(FULL, p, o);
+        te += __shfl_down_sync(FULL, te, o);
+        ex += __shfl_down_sync(FULL, ex, o);
+    }
+    if (lane == 0) {
+        if (r) atomicAdd(jobCounts + 4 * jb, r);
+        if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+        if (te) atomicAdd(jobCounts + 4 * jb + 2, te);
+        if (ex) atomicAdd(jobCounts + 4 * jb + 3, ex);
     }
     if (st) atomicOr(status, st);
 }
@@ -270,6 +407,10 @@ __global__ void k_batch_scatter(BatchSpins S, BatchSpins D, const uint32_t* __re
     for (int f = 0; f < kBF; f++) D.f[f][j] = S.f[f][i];
 #pragma unroll
     for (int u = 0; u < kBU; u++) D.u[u][j] = S.u[u][i];
+    if (S.d[0]) {
+#pragma unroll
+        for (int f = 0; f < kBD; f++) D.d[f][j] = S.d[f][i];
+    }
 }
 
 // compaction: slot i of a kept job moves to remapped slot; job index remapped
@@ -286,6 +427,10 @@ __global__ void k_batch_compact(BatchSpins S, BatchSpins D, const int32_t* __res
     D.u[U_META][j] = S.u[U_META][i];
     D.u[U_JOB][j] = (uint32_t)nj;
     D.u[U_ID][j] = S.u[U_ID][i];
+    if (S.d[0]) {
+#pragma unroll
+        for (int f = 0; f < kBD; f++) D.d[f][j] = S.d[f][i];
+    }
 }
 
 // a job's spins in spin order
@@ -301,6 +446,17 @@ __global__ void k_batch_gather(BatchSpins S, uint32_t slot0, uint32_t len, float
     mom6[6 * id] = S.f[F_MX][i]; mom6[6 * id + 1] = S.f[F_MY][i]; mom6[6 * id + 2] = S.f[F_MZ][i];
     mom6[6 * id + 3] = S.f[F_CX][i]; mom6[6 * id + 4] = S.f[F_CY][i]; mom6[6 * id + 5] = S.f[F_CZ][i];
     meta[id] = S.u[U_META][i];
+}
+
+// a precision-form job's FP64 positions and magnitudes in spin order
+__global__ void k_batch_gather64(BatchSpins S, uint32_t slot0, uint32_t len, double* pos3, double* mag) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= len) return;
+    const uint32_t i = slot0 + k;
+    const uint32_t id = S.u[U_ID][i];
+    if (id == 0xFFFFFFFFu) return;
+    pos3[3 * id] = S.d[D_X][i]; pos3[3 * id + 1] = S.d[D_Y][i]; pos3[3 * id + 2] = S.d[D_Z][i];
+    mag[id] = S.d[D_MAG][i];
 }
 
 // FP64 signal of one job for nG gradients: partial records per (block, g)
@@ -369,6 +525,7 @@ using namespace dsim;
 struct BatchBuf {
     float* f[kBF] = {};
     uint32_t* u[kBU] = {};
+    double* d[kBD] = {};
 };
 
 struct BatchJob {
@@ -429,6 +586,7 @@ BatchSpins view(dsim_batch* b, int which) {
     BatchSpins S;
     for (int f = 0; f < kBF; f++) S.f[f] = b->buf[which].f[f];
     for (int u = 0; u < kBU; u++) S.u[u] = b->buf[which].u[u];
+    for (int f = 0; f < kBD; f++) S.d[f] = b->buf[which].d[f];
     S.N = (uint32_t)b->N;
     return S;
 }
@@ -477,6 +635,41 @@ int upload_jobs(dsim_batch* b) {
     return kOk;
 }
 
+// which plain step instantiations a chunk launches: bit 1 / 2 for mesh jobs
+// on 32- / 64-byte fine-grid records, kHasCyl for cylinder jobs (run by the
+// first launched instantiation; LAYOUT 1 when there is no plain mesh job)
+constexpr uint32_t kHasCyl = 1u << 4;
+uint32_t step_layouts(const dsim_batch* b) {
+    uint32_t mask = 0;
+    for (const auto& j : b->jobs) {
+        const SubDev& s = b->subs[j.d.sub];
+        if (s.kind == kSubCyl) mask |= kHasCyl;
+        else if (!(j.d.flags & DSIM_JOB_PRECISE)) mask |= 1u << (s.acc.wide == 2 ? 2u : 1u);
+    }
+    if ((mask & kHasCyl) && !(mask & 6u)) mask |= 1u << 1;
+    return mask;
+}
+
+// kernels one chunk launches: keys, scan (3), scatter, the step
+// instantiations, advance
+uint64_t chunk_launches(const dsim_batch* b) {
+    const uint32_t mask = step_layouts(b);
+    return 5ull + (uint64_t)__builtin_popcount(mask & 6u) + (b->anyPrecise ? 1ull : 0ull) + 1ull;
+}
+
+template <int LAYOUT>
+void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D, uint32_t cylHere) {
+    if (b->occupancy >= 8)
+        k_batch_step<8, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                 b->d_status, b->d_counts, cylHere);
+    else if (b->occupancy >= 6)
+        k_batch_step<6, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                 b->d_status, b->d_counts, cylHere);
+    else
+        k_batch_step<4, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                 b->d_status, b->d_counts, cylHere);
+}
+
 // one chunk: sort into the other buffer, step, advance the step counter
 int enqueue_chunk(dsim_batch* b) {
     const uint32_t N = (uint32_t)b->N;
@@ -490,17 +683,17 @@ int enqueue_chunk(dsim_batch* b) {
     k_batch_scatter<<<nb, 256, 0, b->st>>>(S, D, b->keys, b->hstart, b->hist);
     b->cur = 1 - b->cur;
     const uint32_t grid = (N + kFlatThreads - 1) / kFlatThreads;
-    if (b->occupancy >= 8)
-        k_batch_step<8, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
-    else if (b->occupancy >= 6)
-        k_batch_step<6, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
-    else
-        k_batch_step<4, false><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+    const uint32_t mask = step_layouts(b);
+    // the first plain launch also runs the cylinder jobs
+    uint32_t cylHere = (mask & kHasCyl) ? 1u : 0u;
+    if (mask & (1u << 1)) { launch_step_layout<1>(b, grid, D, cylHere); cylHere = 0; }
+    if (mask & (1u << 2)) launch_step_layout<2>(b, grid, D, cylHere);
     if (b->anyPrecise)
-        k_batch_step<4, true><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status, b->d_counts);
+        k_batch_step64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status,
+                                                         b->d_counts);
     k_batch_advance<<<1, 1, 0, b->st>>>(b->d_stepNow, b->chunk);
     DSIM_CUDA_TRY(cudaGetLastError());
-    b->launches += b->anyPrecise ? 8 : 7;  // keys, scan (3), scatter, step (x2), advance
+    b->launches += chunk_launches(b);  // keys, scan (3), scatter, step (per layout), advance
     return kOk;
 }
 
@@ -602,6 +795,7 @@ void dsim_batch_free(dsim_batch* b) {
     for (int k = 0; k < 2; k++) {
         for (int f = 0; f < kBF; f++) cudaFree(b->buf[k].f[f]);
         for (int u = 0; u < kBU; u++) cudaFree(b->buf[k].u[u]);
+        for (int f = 0; f < kBD; f++) cudaFree(b->buf[k].d[f]);
     }
     for (auto& j : b->jobs) cudaFree(j.wave);
     cudaFree(b->keys); cudaFree(b->hist); cudaFree(b->hstart); cudaFree(b->scratch);
@@ -641,6 +835,27 @@ int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate) {
     return add_sub(b, s, nullptr, substrate);
 }
 
+// first precision-form job on a substrate: the mesh's FP64 triangle table, and
+// for the batch the FP64 state fields of both spin buffers
+static int ensure_precise(dsim_batch* b, uint32_t substrate) {
+    dsim_mesh* m = const_cast<dsim_mesh*>(b->meshes[substrate]);
+    int rc = mesh_tri64(m);
+    if (rc) return rc;
+    SubDev& sd = b->subs[substrate];
+    if (!sd.g.tri64) {
+        if ((rc = mesh_views(m, &sd.g, &sd.acc))) return rc;
+        DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_subs + substrate, &sd, sizeof(SubDev), cudaMemcpyHostToDevice, b->st));
+        invalidate_graph(b);
+    }
+    if (!b->buf[0].d[0]) {
+        for (int k = 0; k < 2; k++)
+            for (int f = 0; f < kBD; f++)
+                if ((rc = balloc(b, (void**)&b->buf[k].d[f], b->cap * 8))) return rc;
+        invalidate_graph(b);
+    }
+    return kOk;
+}
+
 int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, const uint8_t* comp,
                       const uint32_t* fiber, uint32_t* jobId) {
     if (!b || !d || !pos3 || !comp || !jobId || d->nSpins == 0 || d->steps == 0 || d->substrate >= b->subs.size() ||
@@ -677,9 +892,14 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     J.key0 = (uint32_t)d->seed;
     J.key1 = (uint32_t)(d->seed >> 32);
     J.flags = d->flags & DSIM_JOB_PRECISE;
+    J.spinR = d->spinRadius;
     if (J.flags && cyl) {
         set_last_error(kErrInvalid, "dsim_batch_submit: the precision form applies to mesh jobs");
         return kErrInvalid;
+    }
+    if (J.flags) {
+        int rc = ensure_precise(b, d->substrate);
+        if (rc) return rc;
     }
     std::vector<float> w = make_wave(d);
     int rc = balloc(b, (void**)&j.wave, w.size() * 4);
@@ -718,6 +938,18 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].f[f] + b->N, hf[f].data(), (size_t)pad * 4, cudaMemcpyHostToDevice, b->st));
     for (int u = 0; u < kBU; u++)
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].u[u] + b->N, hu[u].data(), (size_t)pad * 4, cudaMemcpyHostToDevice, b->st));
+    if (J.flags) {
+        // the precision form's FP64 state: the given positions, magnitude 1
+        std::vector<double> hd[kBD];
+        for (int f = 0; f < kBD; f++) hd[f].assign(pad, 0.0);
+        for (uint32_t k = 0; k < d->nSpins; k++) {
+            hd[D_X][k] = pos3[3 * k]; hd[D_Y][k] = pos3[3 * k + 1]; hd[D_Z][k] = pos3[3 * k + 2];
+            hd[D_MAG][k] = 1.0;
+        }
+        for (int f = 0; f < kBD; f++)
+            DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].d[f] + b->N, hd[f].data(), (size_t)pad * 8, cudaMemcpyHostToDevice, b->st));
+        DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
+    }
     b->jobs.push_back(j);
     b->nextId++;
     b->N += pad;
@@ -765,7 +997,7 @@ int dsim_batch_advance(dsim_batch* b, uint32_t steps) {
             }
             DSIM_CUDA_TRY(cudaGraphLaunch(b->exec, b->st));
             b->graphLaunches++;
-            b->launches += (b->anyPrecise ? 8ull : 7ull) * G;
+            b->launches += chunk_launches(b) * G;
             b->stepNow += G * b->chunk;
             chunks -= G;
         } else {
@@ -857,6 +1089,33 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
         if (compartment) compartment[k] = (uint8_t)(hme[k] & 0xFFu);
         if (fiber) fiber[k] = hme[k] >> 8;
     }
+    return kOk;
+}
+
+int dsim_batch_get_precise(dsim_batch* b, uint32_t jobId, double* pos3, double* mag) {
+    BatchJob* j = b ? find_job(b, jobId) : nullptr;
+    if (!j || !(j->d.flags & DSIM_JOB_PRECISE)) {
+        set_last_error(kErrInvalid, "dsim_batch_get_precise: %u is not a precision-form job", jobId);
+        return kErrInvalid;
+    }
+    const uint32_t n = j->nSpins;
+    double *dp = nullptr, *dm = nullptr;
+    int rc;
+    if ((rc = balloc(b, (void**)&dp, (size_t)n * 24)) || (rc = balloc(b, (void**)&dm, (size_t)n * 8))) {
+        cudaFree(dp); cudaFree(dm);
+        return rc;
+    }
+    b->bytes -= (size_t)n * 32;
+    k_batch_gather64<<<(j->pad + 255) / 256, 256, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dp, dm);
+    cudaError_t e = cudaGetLastError();
+    std::vector<double> hp(3 * (size_t)n), hm(n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), dp, (size_t)n * 24, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hm.data(), dm, (size_t)n * 8, cudaMemcpyDeviceToHost, b->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
+    cudaFree(dp); cudaFree(dm);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "dsim_batch_get_precise", __FILE__, __LINE__); return kErrCuda; }
+    if (pos3) memcpy(pos3, hp.data(), hp.size() * 8);
+    if (mag) memcpy(mag, hm.data(), hm.size() * 8);
     return kOk;
 }
 
@@ -965,7 +1224,8 @@ int dsim_batch_compact(dsim_batch* b) {
 int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], float* bestMs) {
     if (!b || !best || trialSteps == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: bad argument"); return kErrInvalid; }
     if (b->N == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: no jobs"); return kErrInvalid; }
-    const size_t words = (size_t)(kBF + kBU) * b->N;
+    const bool hasD = b->buf[0].d[0] != nullptr;
+    const size_t words = (size_t)(kBF + kBU + (hasD ? 2 * kBD : 0)) * b->N;
     uint32_t* snap = nullptr;
     int rc = balloc(b, (void**)&snap, words * 4);
     if (rc) return rc;
@@ -978,6 +1238,9 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
             e = cudaMemcpyAsync(snap + (size_t)f * b->N, b->buf[b->cur].f[f], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
         for (int u = 0; u < kBU && e == cudaSuccess; u++)
             e = cudaMemcpyAsync(snap + (size_t)(kBF + u) * b->N, b->buf[b->cur].u[u], b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        for (int f = 0; hasD && f < kBD && e == cudaSuccess; f++)
+            e = cudaMemcpyAsync(snap + (size_t)(kBF + kBU + 2 * f) * b->N, b->buf[b->cur].d[f], b->N * 8,
+                                cudaMemcpyDeviceToDevice, b->st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(counts0.data(), b->d_counts, 32 * nj, cudaMemcpyDeviceToHost, b->st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(b->st);
         return e;
@@ -991,6 +1254,9 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
             e = cudaMemcpyAsync(b->buf[b->cur].f[f], snap + (size_t)f * b->N, b->N * 4, cudaMemcpyDeviceToDevice, b->st);
         for (int u = 0; u < kBU && e == cudaSuccess; u++)
             e = cudaMemcpyAsync(b->buf[b->cur].u[u], snap + (size_t)(kBF + u) * b->N, b->N * 4, cudaMemcpyDeviceToDevice, b->st);
+        for (int f = 0; hasD && f < kBD && e == cudaSuccess; f++)
+            e = cudaMemcpyAsync(b->buf[b->cur].d[f], snap + (size_t)(kBF + kBU + 2 * f) * b->N, b->N * 8,
+                                cudaMemcpyDeviceToDevice, b->st);
         b->stepNow = step0;
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_stepNow, &b->stepNow, 4, cudaMemcpyHostToDevice, b->st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_counts, counts0.data(), 32 * nj, cudaMemcpyHostToDevice, b->st);

@@ -16,11 +16,19 @@ enum Layout : int { kLayoutSoA = 0, kLayoutAoS = 1 };
 enum Rng : int { kRngPhilox = 0, kRngReplay = 1, kRngPhiloxPerSpinKey = 2 };
 
 // device view of a mesh substrate (CSR cell lists over per-triangle records)
+// per-triangle FP64 helpers of the precision form: unit normal, first vertex,
+// u = p3 - p1, v = p2 - p1, u.v, u.u, v.v, evaluated in double from the FP32
+// vertices with the formulas of dSim3/src/spinSystem.cpp:612-648
+struct __align__(16) Tri64 {
+    double nx, ny, nz, p1x, p1y, p1z, ux, uy, uz, vx, vy, vz, uv, uu, vv, pad;
+};
+
 struct MeshDev {
     const uint32_t* cell_start;  // ncells + 1
     const uint32_t* cell_tri;    // triangle index per entry, ascending in a cell
     const TriPlane* plane;       // per triangle
     const TriBary* bary;         // per triangle
+    const Tri64* tri64;          // per triangle, precision form only (else null)
     uint32_t n;                  // cells per axis
     float L;                     // cell edge, normalised units (2 / n)
 };
@@ -121,6 +129,7 @@ int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* sp
 int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
                              const uint32_t* membrane, const uint32_t* fiber, TriPlane* plane,
                              TriBary* bary, cudaStream_t st);
+int launch_tri64(uint32_t nT, const float* V, const uint32_t* trgls, Tri64* out, cudaStream_t st);
 int launch_records_from_helpers(uint32_t nT, const float* V, const float* H,
                                 const uint32_t* triInfo, TriPlane* plane, TriBary* bary,
                                 cudaStream_t st);
@@ -198,6 +207,8 @@ int launch_cyl_step(const CylDev& g, const CylStepArgs& a, const CylSpinsDev& S,
 const char* last_error_message();
 // api.cu: device views of native substrate handles (for batch.cu)
 int mesh_views(const ::dsim_mesh* m, MeshDev* g, AccelDev* a);
+// builds the mesh's FP64 triangle table on first use (kept until the mesh is freed)
+int mesh_tri64(::dsim_mesh* m);
 int cyl_view(const ::dsim_cyl* c, CylDev* g);
 int mesh_rebuild_accel(::dsim_mesh* m, uint32_t nf);
 

@@ -93,8 +93,7 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
         {
             bool found;
             FastHit best;
-            PrecCount pcnt;
-            flat_round_mode<false, LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pcnt);
+            flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
             if (open) {
                 bool finish = !found;
                 if (found) {

@@ -78,30 +78,16 @@ __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, flo
     return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
 }
 
-// the same in the plain (reference FP32) or the precision form
-template <bool PREC>
-__device__ __forceinline__ bool test_wide_mode(const MeshDev& g, float4 q, float4 pt, uint32_t excl, float ox,
-                                               float oy, float oz, float dx, float dy, float dz, FastHit& h,
-                                               PrecCount& pc) {
-    if (!PREC) return test_wide_loaded(g, q, pt, excl, ox, oy, oz, dx, dy, dz, h);
-    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
-    const uint32_t t = __float_as_uint(pt.w);
-    if (t == excl) return false;
-    return test_prec(g, q.x, q.y, q.z, pt.x, pt.y, pt.z, t, ox, oy, oz, dx, dy, dz, h, pc);
-}
-
 // One round for every lane of the warp (all 32 lanes call it).  open: the lane
 // has a sub-segment (o -> p, `excluded` = last-hit triangle) to test.  On
-// return, for open lanes, found / best hold the reference's collision result.
-// PREC selects the precision form's FP64 re-test of near-degenerate
-// intersections (counted in pc); the plain form is the reference's FP32 test.
-// LAYOUT: 1 or 2 compile only the 32- or 64-byte record path; 0 dispatches
-// on acc.wide at run time (every layout)
-template <bool PREC, int LAYOUT = 0>
+// return, for open lanes, found / best hold the reference's collision result
+// (its FP32 tests).  LAYOUT: 1 or 2 compile only the 32- or 64-byte record
+// path; 0 dispatches on acc.wide at run time (every layout)
+template <int LAYOUT = 0>
 __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
                                                 uint32_t lane, bool open, float ox, float oy, float oz,
                                                 float px, float py, float pz, uint32_t excluded,
-                                                bool& found, FastHit& best, PrecCount& pc) {
+                                                bool& found, FastHit& best) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
@@ -161,21 +147,10 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                 if (v0) f0 = load_full(acc.recf + e0);
                 if (v1) f1 = load_full(acc.recf + e1);
                 FastHit h;
-                if (PREC) {
-                    if (v0 && __float_as_uint(f0.b.w) != H.excl[o0] &&
-                        test_prec(g, f0.a.x, f0.a.y, f0.a.z, f0.b.x, f0.b.y, f0.b.z, __float_as_uint(f0.b.w),
-                                  H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h, pc))
-                        flat_file_hit(H, o0, h);
-                    if (v1 && __float_as_uint(f1.b.w) != H.excl[o1] &&
-                        test_prec(g, f1.a.x, f1.a.y, f1.a.z, f1.b.x, f1.b.y, f1.b.z, __float_as_uint(f1.b.w),
-                                  H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h, pc))
-                        flat_file_hit(H, o1, h);
-                } else {
-                    if (v0 && test_full(f0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h))
-                        flat_file_hit(H, o0, h);
-                    if (v1 && test_full(f1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h))
-                        flat_file_hit(H, o1, h);
-                }
+                if (v0 && test_full(f0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h))
+                    flat_file_hit(H, o0, h);
+                if (v1 && test_full(f1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h))
+                    flat_file_hit(H, o1, h);
             }
         } else if (LAYOUT == 1 || (LAYOUT == 0 && acc.wide)) {
             for (uint32_t rb = 0; rb < rtotal; rb += 64) {
@@ -191,11 +166,11 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                 if (v0) { q0 = __ldg(&acc.recw[e0].q); t0 = __ldg(&acc.recw[e0].pt); }
                 if (v1) { q1 = __ldg(&acc.recw[e1].q); t1 = __ldg(&acc.recw[e1].pt); }
                 FastHit h;
-                if (v0 && test_wide_mode<PREC>(g, q0, t0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
-                                           H.dx[o0], H.dy[o0], H.dz[o0], h, pc))
+                if (v0 && test_wide_loaded(g, q0, t0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
+                                           H.dx[o0], H.dy[o0], H.dz[o0], h))
                     flat_file_hit(H, o0, h);
-                if (v1 && test_wide_mode<PREC>(g, q1, t1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1],
-                                           H.dx[o1], H.dy[o1], H.dz[o1], h, pc))
+                if (v1 && test_wide_loaded(g, q1, t1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1],
+                                           H.dx[o1], H.dy[o1], H.dz[o1], h))
                     flat_file_hit(H, o1, h);
             }
         } else if (LAYOUT == 0) {
@@ -205,8 +180,8 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                 const uint32_t e0 = __shfl_sync(FULL, rbase, j0) + r0;
                 const uint32_t o0 = __shfl_sync(FULL, ow, j0);
                 FastHit h;
-                if (r0 < rtotal && test_entry(g, acc, e0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
-                                              H.dx[o0], H.dy[o0], H.dz[o0], h))
+                if (r0 < rtotal && test_narrow(g, acc, e0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
+                                               H.dx[o0], H.dy[o0], H.dz[o0], h))
                     flat_file_hit(H, o0, h);
             }
         }
@@ -219,9 +194,7 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
             uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
             for (uint32_t k = b0; k < b1; k++) {
                 FastHit h;
-                const bool hit = (PREC && acc.wide) ? test_entry_mode<true>(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h, pc)
-                                                    : test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h);
-                if (hit) flat_file_hit(H, lane, h);
+                if (test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h)) flat_file_hit(H, lane, h);
             }
         }
     }
@@ -230,7 +203,7 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
     if (!open) return;
     const uint32_t n = H.n[lane];
     if (n > (uint32_t)kFlatSlots) {
-        ref_scan_mode<PREC>(g, ox, oy, oz, px, py, pz, excluded, best, found, pc);
+        ref_scan(g, ox, oy, oz, px, py, pz, excluded, best, found);
     } else if (n > 0) {
         // the reference's traversal of its grid over the hits filed in
         // this lane's slots (a triangle filed twice from two fine cells
@@ -272,12 +245,11 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
     }
 }
 
-// plain form (the reference's FP32 tests)
+// every record layout
 __device__ __forceinline__ void flat_round(FlatWarp& H, const MeshDev& g, const AccelDev& acc, uint32_t lane,
                                            bool open, float ox, float oy, float oz, float px, float py, float pz,
                                            uint32_t excluded, bool& found, FastHit& best) {
-    PrecCount pc;
-    flat_round_mode<false>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best, pc);
+    flat_round_mode<0>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
 }
 
 // Reflection or permeation at the round's hit `best`: the permeation interval

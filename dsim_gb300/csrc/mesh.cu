@@ -65,6 +65,33 @@ __global__ void k_records_from_mesh(uint32_t nT, const float* __restrict__ V,
     bary[t] = B;
 }
 
+// FP64 helpers from the FP32 vertices: the reference's helper formulas
+// (dSim3/src/spinSystem.cpp:612-648) evaluated in double, in the order the
+// FP64 oracle evaluates them
+__global__ void k_tri64(uint32_t nT, const float* __restrict__ V, const uint32_t* __restrict__ trgls,
+                        Tri64* out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nT) return;
+    const uint32_t ia = trgls[3 * t], ib = trgls[3 * t + 1], ic = trgls[3 * t + 2];
+    const double ax = V[3 * ia], ay = V[3 * ia + 1], az = V[3 * ia + 2];
+    const double bx = V[3 * ib], by = V[3 * ib + 1], bz = V[3 * ib + 2];
+    const double cx = V[3 * ic], cy = V[3 * ic + 1], cz = V[3 * ic + 2];
+    const double nx = (by - ay) * (cz - az) - (bz - az) * (cy - ay);
+    const double ny = (bz - az) * (cx - ax) - (bx - ax) * (cz - az);
+    const double nz = (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+    const double len = sqrt(nx * nx + ny * ny + nz * nz);
+    Tri64 r;
+    r.nx = nx / len; r.ny = ny / len; r.nz = nz / len;
+    r.p1x = ax; r.p1y = ay; r.p1z = az;
+    r.ux = cx - ax; r.uy = cy - ay; r.uz = cz - az;
+    r.vx = bx - ax; r.vy = by - ay; r.vz = bz - az;
+    r.uv = r.ux * r.vx + r.uy * r.vy + r.uz * r.vz;
+    r.uu = r.ux * r.ux + r.uy * r.uy + r.uz * r.uz;
+    r.vv = r.vx * r.vx + r.vy * r.vy + r.vz * r.vz;
+    r.pad = 0.0;
+    out[t] = r;
+}
+
 // records from the reference's own helper arrays (compat path: helpers[12T],
 // triInfo[3T] = {fiber, membrane, firstVertex}, vertices[3V])
 __global__ void k_records_from_helpers(uint32_t nT, const float* __restrict__ V,
@@ -440,6 +467,13 @@ int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
                              TriBary* bary, cudaStream_t st) {
     if (nT == 0) return kOk;
     k_records_from_mesh<<<(nT + 255) / 256, 256, 0, st>>>(nT, V, trgls, membrane, fiber, plane, bary);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+int launch_tri64(uint32_t nT, const float* V, const uint32_t* trgls, Tri64* out, cudaStream_t st) {
+    if (nT == 0) return kOk;
+    k_tri64<<<(nT + 255) / 256, 256, 0, st>>>(nT, V, trgls, out);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

@@ -158,7 +158,17 @@ __device__ __forceinline__ bool test_split(const MeshDev& g, float4 q, float4 pt
                     dx, dy, dz, h);
 }
 
-// one fine-grid entry k against a sub-segment (either record layout)
+// a 16-byte record k (plane in the record, triangle index beside it)
+__device__ __forceinline__ bool test_narrow(const MeshDev& g, const AccelDev& acc, uint32_t k, uint32_t excl,
+                                            float ox, float oy, float oz, float dx, float dy, float dz, FastHit& h) {
+    const float4 q = __ldg(&acc.rec[k].q);
+    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
+    const uint32_t t = __ldg(acc.tri + k);
+    if (t == excl) return false;
+    return test_tri(g, t, ox, oy, oz, dx, dy, dz, h);
+}
+
+// one fine-grid entry k against a sub-segment (any record layout)
 __device__ __forceinline__ bool test_entry(const MeshDev& g, const AccelDev& acc, uint32_t k,
                                            uint32_t excl, float ox, float oy, float oz, float dx,
                                            float dy, float dz, FastHit& h) {
@@ -170,114 +180,12 @@ __device__ __forceinline__ bool test_entry(const MeshDev& g, const AccelDev& acc
         if (__float_as_uint(pt.w) == excl) return false;
         return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
     }
-    const float4 q = __ldg(&acc.rec[k].q);
-    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
-    const uint32_t t = __ldg(acc.tri + k);
-    if (t == excl) return false;
-    return test_tri(g, t, ox, oy, oz, dx, dy, dz, h);
-}
-
-// ---- precision form -------------------------------------------------------
-// Intersections whose FP32 outcome lies within the FP32 error band of a
-// decision boundary -- the crossing parameter r near 0 or 1 (a segment end on
-// the plane) or a barycentric coordinate near a triangle edge -- are decided
-// again in FP64 from the same triangle data; all others keep the FP32 result.
-// The band on r is 16 float ulps of the numerator's and denominator's terms
-// over |den|; on s and t it is kRetestEpsST.
-struct PrecCount {
-    uint32_t tests = 0, retests = 0;
-};
-static constexpr float kRetestEpsST = 1e-5f;
-
-__device__ __forceinline__ bool test_prec(const MeshDev& g, float nx, float ny, float nz, float p1x, float p1y,
-                                          float p1z, uint32_t t, float ox, float oy, float oz, float dx, float dy,
-                                          float dz, FastHit& h, PrecCount& pc) {
-    pc.tests++;
-    const float ax = p1x - ox, ay = p1y - oy, az = p1z - oz;
-    const float num = nx * ax + ny * ay + nz * az;
-    const float den = nx * dx + ny * dy + nz * dz;
-    if (den == 0.0f) return false;
-    const float aden = fabsf(den);
-    const float mag = fabsf(nx * ax) + fabsf(ny * ay) + fabsf(nz * az) + fabsf(nx * dx) + fabsf(ny * dy) +
-                      fabsf(nz * dz);
-    const float band = 16.0f * 1.1920929e-7f * mag;  // in numerator units
-    // clearly outside the segment: num < -band or num > den + band (den > 0; mirrored for den < 0)
-    const float sn = (den > 0.0f) ? num : -num;
-    if (sn < -band || sn > aden + band) return false;
-    bool near = (sn <= band) || (sn >= aden - band);
-    const float r = num / den;
-    const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
-    const float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);
-    const float vv = __ldg(&g.plane[t].vv);
-    const float uv = v4.z, uu = v4.w;
-    const float wx = ox + r * dx - p1x, wy = oy + r * dy - p1y, wz = oz + r * dz - p1z;
-    const float wu = wx * u4.x + wy * u4.y + wz * u4.z;
-    const float wv = wx * u4.w + wy * v4.x + wz * v4.y;
-    const float s = (uv * wv - vv * wu) / (uv * uv - uu * vv);
-    const float tt = (uv * wu - uu * wv) / (uv * uv - uu * vv);
-    if (!((s >= -kRetestEpsST) & (tt >= -kRetestEpsST) & (s + tt <= 1.0f + kRetestEpsST))) return false;
-    near |= (s <= kRetestEpsST) | (tt <= kRetestEpsST) | (s + tt >= 1.0f - kRetestEpsST);
-    if (!near) {
-        h.t = t;
-        h.x = ox + dx * r; h.y = oy + dy * r; h.z = oz + dz * r;
-        h.d2 = (ox - h.x) * (ox - h.x) + (oy - h.y) * (oy - h.y) + (oz - h.z) * (oz - h.z);
-        h.type = 1;
-        return true;
-    }
-    pc.retests++;
-    const double Nx = nx, Ny = ny, Nz = nz;
-    const double Ax = (double)p1x - ox, Ay = (double)p1y - oy, Az = (double)p1z - oz;
-    const double num64 = Nx * Ax + Ny * Ay + Nz * Az;
-    const double den64 = Nx * dx + Ny * (double)dy + Nz * (double)dz;
-    if (den64 == 0.0 || num64 == 0.0) return false;
-    const double r64 = num64 / den64;
-    if (!(r64 > 0.0 && r64 < 1.0)) return false;
-    const double Wx = (double)ox + r64 * dx - p1x, Wy = (double)oy + r64 * dy - p1y, Wz = (double)oz + r64 * dz - p1z;
-    const double Wu = Wx * u4.x + Wy * u4.y + Wz * u4.z;
-    const double Wv = Wx * u4.w + Wy * v4.x + Wz * v4.y;
-    const double dd = (double)uv * uv - (double)uu * vv;
-    const double s64 = ((double)uv * Wv - (double)vv * Wu) / dd;
-    const double t64 = ((double)uv * Wu - (double)uu * Wv) / dd;
-    if (!(s64 >= 0.0 && t64 >= 0.0 && s64 + t64 <= 1.0)) return false;
-    const double hx = (double)ox + dx * r64, hy = (double)oy + dy * r64, hz = (double)oz + dz * r64;
-    h.t = t;
-    h.x = (float)hx; h.y = (float)hy; h.z = (float)hz;
-    h.d2 = (float)((ox - hx) * (ox - hx) + (oy - hy) * (oy - hy) + (oz - hz) * (oz - hz));
-    uint32_t type = 1;
-    if (s64 == 0.0 || t64 == 0.0 || s64 + t64 == 1.0) {
-        type = 2;
-        if ((s64 == 0.0 && t64 == 0.0) || (s64 == 0.0 && t64 == 1.0) || (s64 == 1.0 && t64 == 0.0)) type = 3;
-    }
-    h.type = type;
-    return true;
-}
-
-// exact test of a fine-grid entry in the plain (reference FP32) or the
-// precision form
-template <bool PREC>
-__device__ __forceinline__ bool test_entry_mode(const MeshDev& g, const AccelDev& acc, uint32_t k, uint32_t excl,
-                                                float ox, float oy, float oz, float dx, float dy, float dz,
-                                                FastHit& h, PrecCount& pc) {
-    if (!PREC) return test_entry(g, acc, k, excl, ox, oy, oz, dx, dy, dz, h);
-    if (acc.wide == 2) {
-        const AccelRecFull r = load_full(acc.recf + k);
-        const uint32_t t = __float_as_uint(r.b.w);
-        if (t == excl) return false;
-        return test_prec(g, r.a.x, r.a.y, r.a.z, r.b.x, r.b.y, r.b.z, t, ox, oy, oz, dx, dy, dz, h, pc);
-    }
-    const float4 q = __ldg(&acc.recw[k].q);
-    if (!plane_may_cross(q, ox, oy, oz, dx, dy, dz)) return false;
-    const float4 pt = __ldg(&acc.recw[k].pt);
-    const uint32_t t = __float_as_uint(pt.w);
-    if (t == excl) return false;
-    return test_prec(g, q.x, q.y, q.z, pt.x, pt.y, pt.z, t, ox, oy, oz, dx, dy, dz, h, pc);
+    return test_narrow(g, acc, k, excl, ox, oy, oz, dx, dy, dz, h);
 }
 
 // cubeCollDetect over the reference grid (dSim3/src/spinKernelCpu.cpp:311-337)
-template <bool PREC>
-static __device__ __noinline__ void ref_scan_mode(const MeshDev& g, float ox, float oy, float oz, float px,
-                                                  float py, float pz, uint32_t excluded, FastHit& best,
-                                                  bool& found, PrecCount& pc) {
+static __device__ __noinline__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px, float py,
+                                             float pz, uint32_t excluded, FastHit& best, bool& found) {
     const uint32_t n = g.n;
     const float L = g.L;
     float dx = px - ox, dy = py - oy, dz = pz - oz;
@@ -303,11 +211,7 @@ static __device__ __noinline__ void ref_scan_mode(const MeshDev& g, float ox, fl
                     float4 ra = __ldg(pp), rc = __ldg(pp + 1);
                     float4 rb = make_float4(rc.x, rc.y, rc.z, __uint_as_float(t));
                     FastHit h;
-                    if (PREC) {
-                        if (!test_prec(g, ra.x, ra.y, ra.z, ra.w, rc.x, rc.y, t, ox, oy, oz, dx, dy, dz, h, pc)) continue;
-                    } else if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) {
-                        continue;
-                    }
+                    if (!test_rec(g, ra, rb, ox, oy, oz, dx, dy, dz, h)) continue;
                     if (h.d2 < bd2) { bd2 = h.d2; best = h; found = true; }
                 }
                 cz += iz;
@@ -317,12 +221,5 @@ static __device__ __noinline__ void ref_scan_mode(const MeshDev& g, float ox, fl
         cx += ix;
     } while ((cx != tx + ix) && !found);
 }
-
-static __device__ __forceinline__ void ref_scan(const MeshDev& g, float ox, float oy, float oz, float px,
-                                                float py, float pz, uint32_t excluded, FastHit& best, bool& found) {
-    PrecCount pc;
-    ref_scan_mode<false>(g, ox, oy, oz, px, py, pz, excluded, best, found, pc);
-}
-
 
 }  // namespace dsim

@@ -410,10 +410,16 @@ class Batch:
         return int(native().dsim_batch_status(self.h))
 
     def precision_counts(self, job):
-        """{exact tests, FP64 re-tests} of a precision-form job."""
+        """{fine-grid records examined, FP64 triangle tests} of a precision-form job."""
         c = np.zeros(2, np.uint64)
         check(native().dsim_batch_precision_counts(self.h, int(job), c))
         return int(c[0]), int(c[1])
+
+    def get_precise(self, job, n):
+        """FP64 positions (n x 3) and magnitudes of a precision-form job, in spin order."""
+        pos = np.zeros(3 * n, np.float64); mag = np.zeros(n, np.float64)
+        check(native().dsim_batch_get_precise(self.h, int(job), pos, mag))
+        return pos.reshape(n, 3), mag
 
     def retire(self, job):
         check(native().dsim_batch_retire(self.h, int(job)))

@@ -10,7 +10,7 @@
  *
  * Per spin the batch keeps the gradient moment M = sum_t w(t) pos(t) (w: the
  * job's waveform, pos: normalised position after step t) with compensated
- * (Kahan) FP32 summation, instead of one phase.  Every gradient G that shares
+ * (Kahan) FP32 summation (FP64 in the precision form), instead of one phase.  Every gradient G that shares
  * the waveform then has phase phi = phaseConstant * (gradScaled(G) . M),
  * evaluated in FP64 at readout, so one walk serves all directions and
  * magnitudes of a gradient table.  The mesh step rules, random draws and
@@ -57,10 +57,13 @@ typedef struct {
     uint32_t reserved;
 } dsim_job_desc;
 
-/* Precision form: intersections whose FP32 outcome lies within the FP32 error
- * band of a decision boundary (segment end on the plane, triangle edge) are
- * decided again in FP64; the others keep the reference's FP32 result.  Phase
- * moments are Kahan-compensated in every form. */
+/* Precision form: the job's step is the reference algorithm evaluated in FP64
+ * -- positions, sub-segments, triangle tests on FP64 triangle helpers (the
+ * formulas of dSim3/src/spinSystem.cpp:612-648 in double), reflections, the
+ * clamp, T2 decay and the gradient moments -- on the same draws as the plain
+ * form; FP32 only prunes fine-grid records whose plane lies clearly off the
+ * sub-segment.  Positions and magnitudes persist in FP64
+ * (dsim_batch_get_precise); dsim_batch_get returns them rounded to float. */
 #define DSIM_JOB_PRECISE 1u
 
 /* spinCapacity: packed spin slots (each job is padded to a multiple of 32) */
@@ -97,8 +100,11 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
                    uint8_t* compartment, uint32_t* fiber);
 /* per-job {reflections or rejections, permeations} and status bits */
 int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]);
-/* precision form: {exact intersection tests, of which re-tested in FP64} */
+/* precision form: {fine-grid records examined, FP64 triangle tests} */
 int dsim_batch_precision_counts(dsim_batch* b, uint32_t jobId, uint64_t out[2]);
+/* precision form: FP64 positions (3 per spin) and magnitudes in spin order;
+ * DSIM_EINVAL for a job without DSIM_JOB_PRECISE.  Synchronous. */
+int dsim_batch_get_precise(dsim_batch* b, uint32_t jobId, double* pos3, double* mag);
 uint32_t dsim_batch_status(dsim_batch* b);
 /* drop finished jobs whose results were read and repack the others */
 int dsim_batch_retire(dsim_batch* b, uint32_t jobId);
