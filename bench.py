@@ -590,8 +590,12 @@ def run_forms(args, W, m):
     subs, mix = build_mix(W, m, n_jobs, 11, spins_range, steps_range)
     work = sum(j["n"] * j["steps"] for j in mix)
     grad_work = sum(j["n"] * j["steps"] * len(j["grads"]) for j in mix)
-    best, tune_ms = tune_mix(subs, mix)
-    log("autotune: %s (%.1f ms for 60 steps of 8 jobs)" % (best, tune_ms))
+    if args.mix_config:
+        occ, chunk = args.mix_config
+        best = {"occupancy": occ, "chunk": chunk, "fine_per_ref": None, "fixed": True}
+    else:
+        best, tune_ms = tune_mix(subs, mix)
+        log("autotune: %s (%.1f ms for 60 steps of 8 jobs)" % (best, tune_ms))
     cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
     per = run_plain_mix(mix)
     plain_s = sum(per)
@@ -880,6 +884,8 @@ def main():
     ap.add_argument("--mix-min-steps", type=int, default=400)
     ap.add_argument("--mix-max-steps", type=int, default=2000)
     ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0, 1.5])
+    ap.add_argument("--mix-config", type=int, nargs=2, default=None, metavar=("OCCUPANCY", "CHUNK"),
+                    help="fixed batch occupancy and chunk for the job mix instead of autotuning")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision-form comparison")
     ap.add_argument("--no-cylinders", action="store_true", help="skip the cylinder workload")
     ap.add_argument("--c1-spins", type=int, default=10000)

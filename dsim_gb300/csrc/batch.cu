@@ -326,6 +326,7 @@ k_batch_step64(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs,
                             fiber, excluded, nrefl, nperm);
                 if (++sub_n >= maxSub) {
                     st |= kStatusSubsegCap;
+                    px = ox; py = oy; pz = oz;
                     finish = true;
                 }
             }

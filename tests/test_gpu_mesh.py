@@ -179,3 +179,39 @@ def test_mesh_philox_run_is_deterministic_and_in_box(engine, tmp_path):
         assert np.array_equal(a, b)
     pos = outs[0][0]
     assert np.all(np.abs(pos) <= np.float32(0.995))
+
+
+@pytest.mark.parametrize("cap,refl", [(1, 1), (2, 1), (2, 0)])
+def test_mesh_replay_parity_at_the_subsegment_cap(engine, tmp_path, cap, refl):
+    """The reference's sub-segment loop has no bound (a spin caught between
+    two intersecting membranes would loop forever); the engine stops a step
+    after `maxSubsegments` hits, leaves the spin at the start of its current
+    sub-segment (the last hit point) and raises status bit 1.  With a cap of
+    1 or 2 most colliding steps end there: the oracle, given the same cap,
+    agrees bit for bit.  refl 0: the reference's return-to-start reflection."""
+    from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
+    case = MeshCase(tmp_path, membranes="AM", permeability=0.05, N=1500)
+    iters = 40
+    d = draws(iters, case.N, seed=17)
+    mo = O.Mesh(case.path, case.spaceScale)
+    cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, 50)
+    p = O.params3(case.stdDevs, case.T2, case.permeability, case.dt, 50, maxtpc, reflectionType=refl,
+                  maxSubsegments=cap)
+    pos = case.pos.copy(); seed = np.zeros(2 * case.N, np.uint32)
+    mag = case.mag.copy(); ph = case.phase.copy(); comp = case.comp.copy(); fib = case.fiber.copy()
+    cnt = np.zeros(2 * case.N, np.uint32)
+    capped, _ = O.integrate3(p, pos, seed, mag, ph, comp, fib, mo.vertices, mo.helpers, mo.triInfo, cc, tic,
+                             case.g, case.pc, iters, draws=d, counts=cnt)
+    assert capped > 0
+    m = Mesh.load(case.path, case.spaceScale)
+    s = Spins(case.N)
+    s.set(case.pos, case.mag, case.phase, case.comp, case.fiber)
+    gp = mesh_params(case.stdDevs, case.T2, case.permeability, case.dt, case.pc, reflectionType=refl,
+                     maxSubsegments=cap)
+    mesh_run(m, s, gp, g=case.g, iterations=iters, draws=d, count=True)
+    gpos, gmag, gph, gcomp, gfib = s.get()
+    assert s.status() & 1
+    assert np.array_equal(s.counts(), cnt.reshape(-1, 2))
+    assert np.array_equal(gpos.view(np.uint32), pos.view(np.uint32))
+    assert np.array_equal(gph.view(np.uint32), ph.view(np.uint32))
+    assert np.array_equal(gcomp, comp) and np.array_equal(gfib, fib)

@@ -138,3 +138,51 @@ def test_precision_form_signal_matches_fp64_oracle(engine, tmp_path):
     assert b.precision_counts(plain) == (0, 0)
     with pytest.raises(Exception):
         b.get_precise(plain, case.N)
+
+
+def _precise_job(case, steps, seed):
+    return dict(pos=case.pos, comp=case.comp, fiber=case.fiber.astype(np.uint32), steps=steps, dt=case.dt,
+                step_sd=case.stdDevs, T2=case.T2, phase_constant=case.pc, seed=seed,
+                permeability=case.permeability, waveform="pgse", delta=0.1, Delta=0.2, precise=True)
+
+
+def test_precision_form_state_survives_mix_compaction_and_autotune(engine, tmp_path):
+    """The FP64 fields follow the spins through sorts, admission of later
+    jobs, compaction and the autotuner's snapshot: a precision-form job's FP64
+    positions equal the job run alone, bit for bit."""
+    from dsim_gb300.engine import Batch, Mesh
+    am = MeshCase(tmp_path, membranes="AM", permeability=0.05, N=600, dt=0.002)
+    gl = MeshCase(tmp_path, membranes="G", permeability=0.3, N=500, dt=0.002, seed=4)
+    ma, mg = Mesh.load(am.path, am.spaceScale), Mesh.load(gl.path, gl.spaceScale)
+    jp, jq = _precise_job(am, 60, 5), _precise_job(gl, 140, 6)
+    plain = dict(_precise_job(am, 90, 7), precise=False)
+
+    def alone(mesh, kw, n):
+        b = Batch(1 << 14, 2)
+        j = b.submit(b.add_mesh(mesh), **kw)
+        b.run()
+        out = b.get_precise(j, n), b.counts(j)
+        b.close()
+        return out
+
+    want_q = alone(mg, jq, gl.N)
+    b = Batch(1 << 14, 4)
+    b.configure(chunk=10, occupancy=6, graph_chunks=2)
+    sa, sg = b.add_mesh(ma), b.add_mesh(mg)
+    ip = b.submit(sa, **jp)
+    ix = b.submit(sa, **plain)
+    b.advance(30)
+    iq = b.submit(sg, **jq)                 # admitted while the others run
+    best, _ = b.autotune(trial_steps=20)    # snapshot and restore with FP64 fields
+    b.advance(40)
+    assert b.job_status(ip) == (60, True)
+    b.retire(ip)
+    b.compact()                             # the precision-form job q moves slots
+    b.run()
+    assert b.status() == 0
+    (pos, mag), cnt = b.get_precise(iq, gl.N), b.counts(iq)
+    assert np.array_equal(pos.view(np.uint64), want_q[0][0].view(np.uint64))
+    assert np.array_equal(mag.view(np.uint64), want_q[0][1].view(np.uint64))
+    assert np.array_equal(cnt, want_q[1])
+    assert b.job_status(ix) == (90, True)
+    b.close()
