@@ -15,7 +15,6 @@ namespace dsim {
 enum Layout : int { kLayoutSoA = 0, kLayoutAoS = 1 };
 enum Rng : int { kRngPhilox = 0, kRngReplay = 1, kRngPhiloxPerSpinKey = 2 };
 
-// device view of a mesh substrate (CSR cell lists over per-triangle records)
 // per-triangle FP64 helpers of the precision form: unit normal, first vertex,
 // u = p3 - p1, v = p2 - p1, u.v, u.u, v.v, evaluated in double from the FP32
 // vertices with the formulas of dSim3/src/spinSystem.cpp:612-648
@@ -23,6 +22,7 @@ struct __align__(16) Tri64 {
     double nx, ny, nz, p1x, p1y, p1z, ux, uy, uz, vx, vy, vz, uv, uu, vv, pad;
 };
 
+// device view of a mesh substrate (CSR cell lists over per-triangle records)
 struct MeshDev {
     const uint32_t* cell_start;  // ncells + 1
     const uint32_t* cell_tri;    // triangle index per entry, ascending in a cell
@@ -66,9 +66,9 @@ struct MeshStepArgs {
 };
 
 // ---- accel.cu -------------------------------------------------------------
-// Fine acceleration grid: every triangle is listed in each fine cell its
-// bounding box (widened by kAccelEps) overlaps; cells are stored in Morton
-// order.  Per entry a 16-byte plane record {n.x, n.y, n.z, n.p1} for a
+// Fine acceleration grid: every triangle is listed in each fine cell it
+// touches (separating-axis test against the cell widened by kAccelEps); cells
+// are stored in Morton order.  Per entry a 16-byte plane record {n.x, n.y, n.z, n.p1} for a
 // conservative plane-crossing prefilter, and the triangle index beside it.
 static constexpr float kAccelEps = 1e-5f;
 struct __align__(16) AccelRec {
@@ -120,7 +120,8 @@ int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepA
                           const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 6);
 // flat.cu: warp-flattened candidate lists (same results); occupancy 6 or 8
 int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 8);
+                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 8,
+                          bool queue = false);
 int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st);
 int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
                       uint32_t iterations, cudaStream_t st);

@@ -29,11 +29,14 @@
 
 namespace dsim {
 
-template <bool STATS, int MINB, int LAYOUT>
+// QUEUE (32-byte records): records past the plane test are finished 32 at a
+// time from a per-warp queue (flat_round_mode's Q)
+template <bool STATS, int MINB, int LAYOUT, bool QUEUE = false>
 __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g, AccelDev acc,
                                                                        MeshStepArgs a, SpinsSorted S,
                                                                        int rng) {
     __shared__ FlatWarp wh[kFlatWarps];
+    __shared__ FlatQueue wq[QUEUE ? kFlatWarps : 1];
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     FlatWarp& H = wh[threadIdx.x >> 5];
@@ -93,7 +96,8 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
         {
             bool found;
             FastHit best;
-            flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
+            flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best,
+                                    QUEUE ? &wq[threadIdx.x >> 5] : nullptr);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -132,7 +136,7 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
 }
 
 int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy) {
+                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy, bool queue) {
     if (S.N == 0 || a.iterations == 0) return kOk;
     dim3 block(kFlatThreads), grid((S.N + kFlatThreads - 1) / kFlatThreads);
     // one instantiation per record layout keeps each kernel's registers to its own path
@@ -141,6 +145,8 @@ int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepA
         if (occupancy >= 8) k_mesh_step_flat<false, 8, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
         else if (occupancy >= 6) k_mesh_step_flat<false, 6, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
         else k_mesh_step_flat<false, 4, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    } else if (acc.wide == 1 && queue) {
+        k_mesh_step_flat<false, 6, 1, true><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     } else if (acc.wide == 1) {
         if (occupancy >= 8) k_mesh_step_flat<false, 8, 1><<<grid, block, 0, st>>>(g, acc, a, S, rng);
         else if (occupancy >= 6) k_mesh_step_flat<false, 6, 1><<<grid, block, 0, st>>>(g, acc, a, S, rng);

@@ -69,6 +69,14 @@ __device__ __forceinline__ uint32_t warp_find(uint32_t incl, uint32_t r) {
     return pos;
 }
 
+// Queue of a warp's 32-byte records that passed the plane test, as (record,
+// owner) pairs: the rest of the exact test (with its dependent loads) runs on
+// 32 of them at a time with every lane busy
+static constexpr uint32_t kFlatQueue = 64;  // at most 31 left over + 32 appended
+struct FlatQueue {
+    uint32_t e[kFlatQueue], o[kFlatQueue];
+};
+
 // one 32-byte record already in registers against a sub-segment
 __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, float4 pt, uint32_t excl,
                                                  float ox, float oy, float oz, float dx, float dy,
@@ -78,16 +86,46 @@ __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, flo
     return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
 }
 
+// the rest of the exact test of queued record e for owner o (plane test passed)
+__device__ __forceinline__ void flat_test_queued(FlatWarp& H, const MeshDev& g, const AccelDev& acc, uint32_t e,
+                                                 uint32_t o) {
+    const float4 q = __ldg(&acc.recw[e].q), pt = __ldg(&acc.recw[e].pt);
+    FastHit h;
+    if (test_split(g, q, pt, H.ox[o], H.oy[o], H.oz[o], H.dx[o], H.dy[o], H.dz[o], h)) flat_file_hit(H, o, h);
+}
+
+// appends the lanes' surviving (e, o) to the queue (qn: warp-uniform length)
+// and tests full groups of 32 from its top; all lanes call it
+__device__ __forceinline__ void flat_enqueue(FlatWarp& H, FlatQueue& Q, const MeshDev& g, const AccelDev& acc,
+                                             uint32_t lane, bool live, uint32_t e, uint32_t o, uint32_t& qn) {
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
+    if (live) {
+        const uint32_t at = qn + __popc(b & ((1u << lane) - 1u));
+        Q.e[at] = e; Q.o[at] = o;
+    }
+    qn += __popc(b);
+    __syncwarp();
+    while (qn >= 32) {
+        const uint32_t at = qn - 32 + lane;
+        const uint32_t eq = Q.e[at], oq = Q.o[at];
+        __syncwarp();
+        qn -= 32;
+        flat_test_queued(H, g, acc, eq, oq);
+    }
+}
+
 // One round for every lane of the warp (all 32 lanes call it).  open: the lane
 // has a sub-segment (o -> p, `excluded` = last-hit triangle) to test.  On
 // return, for open lanes, found / best hold the reference's collision result
 // (its FP32 tests).  LAYOUT: 1 or 2 compile only the 32- or 64-byte record
-// path; 0 dispatches on acc.wide at run time (every layout)
+// path; 0 dispatches on acc.wide at run time (every layout).  Q (32-byte
+// records only): records past the plane test are queued and finished 32 at a
+// time (null: finished in place)
 template <int LAYOUT = 0>
 __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
                                                 uint32_t lane, bool open, float ox, float oy, float oz,
                                                 float px, float py, float pz, uint32_t excluded,
-                                                bool& found, FastHit& best) {
+                                                bool& found, FastHit& best, FlatQueue* Q = nullptr) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
@@ -113,6 +151,7 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
     const uint32_t iincl = warp_incl_scan(ncw, lane);
     const uint32_t iexcl = iincl - ncw;
     const uint32_t itotal = __shfl_sync(FULL, iincl, 31);
+    uint32_t qn = 0;  // queue length (warp-uniform)
     __syncwarp();
     // pass 1: 32 items at a time, one cell-range load per lane
     for (uint32_t ib = 0; ib < itotal; ib += 32) {
@@ -165,6 +204,15 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                 float4 q0 = make_float4(0.f, 0.f, 0.f, 0.f), t0 = q0, q1 = q0, t1 = q0;
                 if (v0) { q0 = __ldg(&acc.recw[e0].q); t0 = __ldg(&acc.recw[e0].pt); }
                 if (v1) { q1 = __ldg(&acc.recw[e1].q); t1 = __ldg(&acc.recw[e1].pt); }
+                if (Q) {
+                    const bool s0 = v0 && __float_as_uint(t0.w) != H.excl[o0] &&
+                                    plane_may_cross(q0, H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0]);
+                    const bool s1 = v1 && __float_as_uint(t1.w) != H.excl[o1] &&
+                                    plane_may_cross(q1, H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1]);
+                    flat_enqueue(H, *Q, g, acc, lane, s0, e0, o0, qn);
+                    flat_enqueue(H, *Q, g, acc, lane, s1, e1, o1, qn);
+                    continue;
+                }
                 FastHit h;
                 if (v0 && test_wide_loaded(g, q0, t0, H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0],
                                            H.dx[o0], H.dy[o0], H.dz[o0], h))
@@ -186,6 +234,7 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
             }
         }
     }
+    if (Q && lane < qn) flat_test_queued(H, g, acc, Q->e[lane], Q->o[lane]);  // the queue's remainder
     // boxes of more than kFlatMaxItems cells (long sub-segments): the owner alone
     if (solo) {
         for (uint32_t q = 0; q < nc; q++) {

@@ -25,17 +25,22 @@ struct PrecCount {
 };
 
 // FP64 sub-segment table of a warp, by owner lane (the FP32 copies in
-// FlatWarp drive the cell boxes and the plane pruning)
+// FlatWarp drive the cell boxes and the plane pruning), and the queue of
+// records that passed the pruning: (triangle, owner) pairs tested in FP64
+// 32 at a time, so the FP64 test runs with every lane busy
+static constexpr uint32_t kPrecQueue = 64;  // at most 31 left over + 32 appended
 struct PrecWarp {
     double ox[32], oy[32], oz[32], dx[32], dy[32], dz[32];
+    uint32_t qt[kPrecQueue], qo[kPrecQueue];
 };
 
 // May the plane (n, w = n.p1) meet the sub-segment o -> o + d?  The FP32
 // value of n.p1 - n.o differs from the FP64 numerator of the exact test by
 // less than ~3e-6 for points of the box (rounding of o to float <= 6e-8 per
 // axis, FP32 against FP64 unit normal <= ~3e-7 relative, a few roundings of
-// terms <= 3.5), and the FP32 denominator from the FP64 one by far less, so a
-// record whose FP64 crossing parameter lies in (0, 1) always passes.  A
+// terms <= 3.5), and the FP32 denominator (from the difference of the rounded
+// end points) from the FP64 one by far less, so a record whose FP64 crossing
+// parameter lies in (0, 1) always passes.  A
 // segment parallel to the plane in FP32 passes when its start lies within
 // the margin.
 static constexpr float kPrecMargin = 1e-5f;
@@ -87,6 +92,24 @@ __device__ __forceinline__ uint32_t ref_coord64(double p, double L, uint32_t n) 
     return (uint32_t)mx;
 }
 
+// The same cell from an FP32 estimate: fp is p rounded to float and invL the
+// float of 1 / L.  The estimate (fp + 1) invL differs from (p + 1) / L by less
+// than 1e-5 (1 + |estimate|) for |p| <= 4 (three float roundings and the
+// rounding of p and 1 / L, a few 1e-7 relative each), and the FP64 quotient
+// from (p + 1) / L by far less; away from an integer by more than that bound
+// both have the same floor, and only near a cell boundary is the FP64
+// quotient evaluated.
+__device__ __forceinline__ uint32_t ref_coord64_est(double p, float fp, double L, float invL, uint32_t n) {
+    const float e = (fp + 1.0f) * invL;
+    const float fl = floorf(e);
+    const float margin = 1e-4f * (1.0f + fabsf(e));
+    if (!((e - fl > margin) & (fl + 1.0f - e > margin)) || !(fabsf(fp) <= 4.0f)) return ref_coord64(p, L, n);
+    const float hi = (float)(n - 1);
+    const float mn = (hi < fl) ? hi : fl;
+    const float mx = (0.0f < mn) ? mn : 0.0f;
+    return (uint32_t)mx;
+}
+
 // FP32 plane and triangle of fine-grid record k (32- or 64-byte layout)
 __device__ __forceinline__ void record_plane(const AccelDev& acc, uint32_t k, bool full, float4& q, uint32_t& t) {
     if (full) {
@@ -111,21 +134,49 @@ __device__ __forceinline__ void prec_file_hit(FlatWarp& H, uint32_t owner, uint3
     }
 }
 
-// record k against owner o's FP64 sub-segment; files a hit
-__device__ __forceinline__ void prec_test_record(FlatWarp& H, const PrecWarp& P, const MeshDev& g,
-                                                 const AccelDev& acc, uint32_t k, bool full, uint32_t o,
-                                                 PrecCount& pc) {
+// FP32 pruning of record k for owner o: returns the triangle to test in
+// FP64, or 0xFFFFFFFF
+__device__ __forceinline__ uint32_t prec_prune(const FlatWarp& H, const AccelDev& acc, uint32_t k, bool full,
+                                               uint32_t o, PrecCount& pc) {
     float4 q;
     uint32_t t;
     record_plane(acc, k, full, q, t);
     pc.records++;
-    if (t == H.excl[o]) return;
-    if (!plane_near(q.x, q.y, q.z, q.w, H.ox[o], H.oy[o], H.oz[o], H.dx[o], H.dy[o], H.dz[o])) return;
+    if (t == H.excl[o]) return 0xFFFFFFFFu;
+    if (!plane_near(q.x, q.y, q.z, q.w, H.ox[o], H.oy[o], H.oz[o], H.dx[o], H.dy[o], H.dz[o])) return 0xFFFFFFFFu;
+    return t;
+}
+
+// FP64 test of triangle t against owner o's sub-segment; files a hit
+__device__ __forceinline__ void prec_test(FlatWarp& H, const PrecWarp& P, const MeshDev& g, uint32_t t, uint32_t o,
+                                          PrecCount& pc) {
     pc.exact++;
     double r;
     uint32_t type;
     if (tri_test64(g.tri64, t, P.ox[o], P.oy[o], P.oz[o], P.dx[o], P.dy[o], P.dz[o], r, type))
         prec_file_hit(H, o, t, type, r);
+}
+
+// appends the lanes' surviving (t, o) to the warp's queue (qn: warp-uniform
+// length) and tests full groups of 32 from its top; all lanes call it
+__device__ __forceinline__ void prec_enqueue(FlatWarp& H, PrecWarp& P, const MeshDev& g, uint32_t lane,
+                                             uint32_t t, uint32_t o, uint32_t& qn, PrecCount& pc) {
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const bool live = t != 0xFFFFFFFFu;
+    const uint32_t b = __ballot_sync(FULL, live);
+    if (live) {
+        const uint32_t at = qn + __popc(b & ((1u << lane) - 1u));
+        P.qt[at] = t; P.qo[at] = o;
+    }
+    qn += __popc(b);
+    __syncwarp();
+    while (qn >= 32) {
+        const uint32_t at = qn - 32 + lane;
+        const uint32_t tq = P.qt[at], oq = P.qo[at];
+        __syncwarp();
+        qn -= 32;
+        prec_test(H, P, g, tq, oq, pc);
+    }
 }
 
 // collDetectRectGrid's cell walk over the reference grid with cubeCollDetect
@@ -200,7 +251,7 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
     const bool solo = open && nc > (uint32_t)kFlatMaxItems;
     const uint32_t ncw = (open && !solo) ? nc : 0u;
     H.ox[lane] = fox; H.oy[lane] = foy; H.oz[lane] = foz;
-    H.dx[lane] = (float)dx; H.dy[lane] = (float)dy; H.dz[lane] = (float)dz;
+    H.dx[lane] = fpx - fox; H.dy[lane] = fpy - foy; H.dz[lane] = fpz - foz;
     P.ox[lane] = ox; P.oy[lane] = oy; P.oz[lane] = oz;
     P.dx[lane] = dx; P.dy[lane] = dy; P.dz[lane] = dz;
     H.excl[lane] = excluded;
@@ -210,6 +261,7 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
     const uint32_t iincl = warp_incl_scan(ncw, lane);
     const uint32_t iexcl = iincl - ncw;
     const uint32_t itotal = __shfl_sync(FULL, iincl, 31);
+    uint32_t qn = 0;  // queue length (warp-uniform)
     __syncwarp();
     for (uint32_t ib = 0; ib < itotal; ib += 32) {
         const uint32_t m = ib + lane;
@@ -228,20 +280,31 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
         const uint32_t rincl = warp_incl_scan(cnt, lane);
         const uint32_t rtotal = __shfl_sync(FULL, rincl, 31);
         const uint32_t rbase = b0 - (rincl - cnt);
-        for (uint32_t rb = 0; rb < rtotal; rb += 32) {
-            const uint32_t r0 = rb + lane;
+        for (uint32_t rb = 0; rb < rtotal; rb += 64) {
+            const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
             const uint32_t j0 = min(warp_find(rincl, r0), 31u);
+            const uint32_t j1 = min(warp_find(rincl, r1), 31u);
             const uint32_t e0 = __shfl_sync(FULL, rbase, j0) + r0;
+            const uint32_t e1 = __shfl_sync(FULL, rbase, j1) + r1;
             const uint32_t o0 = __shfl_sync(FULL, ow, j0);
-            if (r0 < rtotal) prec_test_record(H, P, g, acc, e0, full, o0, pc);
+            const uint32_t o1 = __shfl_sync(FULL, ow, j1);
+            const uint32_t t0 = (r0 < rtotal) ? prec_prune(H, acc, e0, full, o0, pc) : 0xFFFFFFFFu;
+            const uint32_t t1 = (r1 < rtotal) ? prec_prune(H, acc, e1, full, o1, pc) : 0xFFFFFFFFu;
+            prec_enqueue(H, P, g, lane, t0, o0, qn, pc);
+            prec_enqueue(H, P, g, lane, t1, o1, qn, pc);
         }
     }
+    // the queue's remainder (fewer than 32)
+    if (lane < qn) prec_test(H, P, g, P.qt[lane], P.qo[lane], pc);
     if (solo) {
         for (uint32_t q = 0; q < nc; q++) {
             const uint32_t iz = q % w2, r = q / w2, iy = r % w1, ix = r / w1;
             const uint32_t key = morton3(lo0 + ix, lo1 + iy, lo2 + iz);
             const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
-            for (uint32_t k = b0; k < b1; k++) prec_test_record(H, P, g, acc, k, full, lane, pc);
+            for (uint32_t k = b0; k < b1; k++) {
+                const uint32_t t = prec_prune(H, acc, k, full, lane, pc);
+                if (t != 0xFFFFFFFFu) prec_test(H, P, g, t, lane, pc);
+            }
         }
     }
     __syncwarp();
@@ -257,8 +320,11 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
     // hit, the lowest triangle index on ties (its cell lists ascend)
     const uint32_t gn = g.n;
     const double L = (double)g.L;
-    const uint32_t sx = ref_coord64(ox, L, gn), sy = ref_coord64(oy, L, gn), sz = ref_coord64(oz, L, gn);
-    const uint32_t tx = ref_coord64(px, L, gn), ty = ref_coord64(py, L, gn), tz = ref_coord64(pz, L, gn);
+    const float invL = 1.0f / g.L;
+    const uint32_t sx = ref_coord64_est(ox, fox, L, invL, gn), sy = ref_coord64_est(oy, foy, L, invL, gn),
+                   sz = ref_coord64_est(oz, foz, L, invL, gn);
+    const uint32_t tx = ref_coord64_est(px, fpx, L, invL, gn), ty = ref_coord64_est(py, fpy, L, invL, gn),
+                   tz = ref_coord64_est(pz, fpz, L, invL, gn);
     const uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
     const uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
     const uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));

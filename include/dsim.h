@@ -63,7 +63,7 @@ int dsim_mesh_create(const float* vertices_um, uint32_t nVertices, const uint32_
  *              max entries in one cell, device bytes, nonempty cells */
 int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
 /* The step kernels find candidate triangles in a finer acceleration grid
- * (each triangle listed in every fine cell its bounding box overlaps) and
+ * (each triangle listed in every fine cell it touches) and
  * apply the reference grid's first-cell-with-hit rule only to the hits, which
  * gives the same results.  Built with 2.5 * numCubes cells per axis by default;
  * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
@@ -73,7 +73,8 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
  * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
  * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM; 5, 6, 7 the
  * warp's candidate records flattened into one list, lanes stepping
- * independently (8, 6, 4 blocks per SM) */
+ * independently (8, 6, 4 blocks per SM); 8 as 6, with the records that pass
+ * the plane test queued and finished 32 at a time (32-byte records) */
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 /* fine-grid record size: 32 (default) holds the plane data for the exact
  * plane test; 16 holds a prefilter record only (half the bytes, one more
