@@ -165,6 +165,9 @@ int mesh_views(const dsim_mesh* m, MeshDev* g, AccelDev* a) {
 }
 int mesh_tri64(dsim_mesh* m) {
     if (!m) return kErrInvalid;
+    // batches on several host threads may share the mesh: one builds the table
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
     if (m->tri64 || m->nT == 0) return kOk;
     Tri64* t = nullptr;
     int rc = dev_alloc(&t, m->nT, &m->bytes);
