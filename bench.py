@@ -759,12 +759,13 @@ def run_precision(args, W, m):
     pos0 = W.pos.reshape(-1, 3)[sel].reshape(-1).copy()
     comp0, fib0 = W.comp[sel].copy(), W.fiber[sel].astype(np.uint32)
     seed = 77
-    b = Batch(1 << 16, 2 * len(waves))
+    b = Batch(1 << 16, 3 * len(waves))
     sid = b.add_mesh(m)
     common = dict(pos=pos0, comp=comp0, fiber=fib0, steps=steps, dt=dt, step_sd=sd, T2=W.T2, phase_constant=pc,
                   seed=seed, waveform="table")
     t0 = time.time()
     prec = [b.submit(sid, table=w, precise=True, **common) for w in waves]
+    local = [b.submit(sid, table=w, local=True, **common) for w in waves]
     plain = [b.submit(sid, table=w, precise=False, **common) for w in waves]
     b.run()
     gpu_s = time.time() - t0
@@ -789,15 +790,16 @@ def run_precision(args, W, m):
     oracle_s = time.time() - t0
     dirs = fibonacci_dirs(32)
     bvals = [1.0, 3.0, 5.0, 10.0]
-    err = {"precise": [], "plain": []}
-    rms_dz = {"precise": [], "plain": []}
+    err = {"precise": [], "local": [], "plain": []}
+    rms_dz = {"precise": [], "local": [], "plain": []}
     diverged = {}
     exact_pos = True
     for k in range(len(waves)):
-        for form, ids in (("precise", prec), ("plain", plain)):
+        for form, ids in (("precise", prec), ("local", local), ("plain", plain)):
             bpos, bmag, mom, _, _ = b.get(ids[k], n)
-            if form == "precise":
+            if form != "plain":
                 bpos, bmag = b.get_precise(ids[k], n)
+            if form == "precise":
                 exact_pos &= bool(np.array_equal(bpos.reshape(-1).view(np.uint64), pos.view(np.uint64)))
             if k == 0:
                 dp = np.abs(bpos.reshape(-1, 3).astype(np.float64) - pos.reshape(-1, 3)).max(1)
@@ -813,14 +815,16 @@ def run_precision(args, W, m):
                 err[form].extend(np.abs(S32 - S64).tolist())
                 rms_dz[form].extend(np.sqrt(np.mean(np.abs(z32 - z64) ** 2, 0)).tolist())
     records, exact = b.precision_counts(prec[0])
+    l_records, l_retests = b.precision_counts(local[0])
     b.close()
     # throughput of the precision form vs the plain form at full spin count
     rates = {}
-    for form in ("plain", "precise"):
+    for form in ("plain", "local", "precise"):
         bb = Batch(W.N + 64, 1)
         sid = bb.add_mesh(m)
         jid = bb.submit(sid, W.pos, W.comp, W.fiber.astype(np.uint32), args.c5_rate_steps, dt, sd, W.T2, pc, 5,
-                        waveform="table", table=waves[1][:args.c5_rate_steps], precise=(form == "precise"))
+                        waveform="table", table=waves[1][:args.c5_rate_steps], precise=(form == "precise"),
+                        local=(form == "local"))
         bb.sync()
         t0 = time.time()
         bb.run()
@@ -830,9 +834,12 @@ def run_precision(args, W, m):
                       "x 32 directions x b %s ms/um2 (|G| <= 300 mT/m)" % (n, steps, [int(f) for f in freqs], bvals),
             "max_abs_dS_precise": float(np.max(err["precise"])), "median_abs_dS_precise": float(np.median(err["precise"])),
             "max_abs_dS_plain": float(np.max(err["plain"])), "median_abs_dS_plain": float(np.median(err["plain"])),
+            "max_abs_dS_local": float(np.max(err["local"])), "median_abs_dS_local": float(np.median(err["local"])),
             "spins_diverged_precise": diverged["precise"], "spins_diverged_plain": diverged["plain"],
+            "spins_diverged_local": diverged["local"],
             "max_abs_dS_at_full_spins_precise": float(np.max(rms_dz["precise"])) / np.sqrt(W.N),
             "max_abs_dS_at_full_spins_plain": float(np.max(rms_dz["plain"])) / np.sqrt(W.N),
+            "max_abs_dS_at_full_spins_local": float(np.max(rms_dz["local"])) / np.sqrt(W.N),
             "positions_bit_exact_precise": exact_pos,
             "dS_note": ("the precision form walks the FP64 algorithm (positions equal the FP64 oracle's bit for bit; "
                         "|dS| is rounding of the stored moments); the plain form's |dS| is set by the few spins whose "
@@ -840,7 +847,13 @@ def run_precision(args, W, m):
                         "zero-mean, so at the full spin count the expected |dS| is rms(z - z64) / sqrt(N), reported "
                         "per gradient as max over gradients"),
             "fp64_test_fraction": exact / max(records, 1), "records_examined": records, "fp64_tests": exact,
+            "local_fp64_retest_fraction": l_retests / max(l_records, 1),
+            "forms": {"precise": "the step in FP64 (DSIM_JOB_PRECISE)",
+                      "local": "FP32 offsets from a 1/16 lattice, FP64 re-tests of near-degenerate intersections, "
+                               "Kahan moments (DSIM_JOB_LOCAL)",
+                      "plain": "the reference's FP32 step with Kahan moments"},
             "spin_steps_per_s_precise": rates["precise"], "spin_steps_per_s_plain_batch": rates["plain"],
+            "spin_steps_per_s_local": rates["local"],
             "rate_workload": "%d spins x %d steps, one job" % (W.N, args.c5_rate_steps),
             "gpu_s": gpu_s, "oracle_s": oracle_s, "oracle": "FP64 restatement of the reference step (oracle), same draws"}
 

@@ -30,6 +30,7 @@
 #include "cyl_common.cuh"
 #include "engine.h"
 #include "flat_round.cuh"
+#include "local_round.cuh"
 #include "prec_round.cuh"
 
 namespace dsim {
@@ -51,7 +52,7 @@ struct JobDev {
     float inR;                    // cylinders: (inner radius proportion)^2
     const float* wave;            // w[steps]
     uint32_t key0, key1;
-    uint32_t flags;               // DSIM_JOB_PRECISE
+    uint32_t flags;               // DSIM_JOB_PRECISE or DSIM_JOB_LOCAL
     float spinR;                  // spin radius (the precision form clamps to +-(1 - spinR) in FP64)
 };
 
@@ -115,7 +116,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
-    if (J.flags & DSIM_JOB_PRECISE) return;  // warp-uniform
+    if (J.flags & (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL)) return;  // warp-uniform
     if (subS[wi].kind == kSubMesh ? subS[wi].acc.wide != (uint32_t)LAYOUT : !cylHere) return;
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
@@ -233,6 +234,154 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     if (lane == 0) {
         if (r) atomicAdd(jobCounts + 4 * jb, r);
         if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+    }
+    if (st) atomicOr(status, st);
+}
+
+// Cell-local FP32 mesh jobs (DSIM_JOB_LOCAL): the plain step with positions
+// as FP32 offsets from a lattice origin (local_round.cuh), FP64 re-tests of
+// near-degenerate intersections, Kahan moments.  Between chunks the position
+// is kept in the double fields as origin + offset; the float fields get its
+// rounded value (sort keys, float readers).
+__global__ void __launch_bounds__(kFlatThreads, 4)
+k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
+                   const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
+                   unsigned long long* jobCounts) {
+    __shared__ FlatWarp wh[kFlatWarps];
+    __shared__ LocalWarp wl[kFlatWarps];
+    __shared__ float mom[6][kFlatThreads];
+    __shared__ JobDev jobS[kFlatWarps];
+    __shared__ SubDev subS[kFlatWarps];
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tx = threadIdx.x;
+    const uint32_t wi = threadIdx.x >> 5;
+    FlatWarp& H = wh[wi];
+    LocalWarp& Lw = wl[wi];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
+    const uint32_t jb = S.u[U_JOB][i & ~31u];
+    {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(jobS + wi);
+        for (uint32_t k = lane; k < sizeof(JobDev) / 4; k += 32) dst[k] = __ldg(src + k);
+        __syncwarp();
+        const uint32_t* s2 = reinterpret_cast<const uint32_t*>(subs + jobS[wi].sub);
+        uint32_t* d2 = reinterpret_cast<uint32_t*>(subS + wi);
+        for (uint32_t k = lane; k < sizeof(SubDev) / 4; k += 32) d2[k] = __ldg(s2 + k);
+        __syncwarp();
+    }
+    const JobDev& J = jobS[wi];
+    if (!(J.flags & DSIM_JOB_LOCAL)) return;  // warp-uniform
+    const uint32_t now = *stepNow;
+    const uint32_t start = J.start, steps = J.steps;
+    if (now < start || now - start >= steps) return;
+    const uint32_t ls0 = now - start;
+    const uint32_t nsteps = min(chunk, steps - ls0);
+    const uint32_t id = S.u[U_ID][i];
+    const bool valid = id != 0xFFFFFFFFu;
+    // position = lattice origin (multiple of 1/16) + FP32 offset in [0, 1/16)
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f, x = 0.0f, y = 0.0f, z = 0.0f, mag = 0.0f;
+    uint32_t comp = 0, fiber = 0;
+    mom[0][tx] = 0.0f; mom[1][tx] = 0.0f; mom[2][tx] = 0.0f;
+    mom[3][tx] = 0.0f; mom[4][tx] = 0.0f; mom[5][tx] = 0.0f;
+    if (valid) {
+        const double X = S.d[D_X][i], Y = S.d[D_Y][i], Z = S.d[D_Z][i];
+        const double Gx = floor(X * 16.0) * 0.0625, Gy = floor(Y * 16.0) * 0.0625, Gz = floor(Z * 16.0) * 0.0625;
+        gx = (float)Gx; gy = (float)Gy; gz = (float)Gz;
+        x = (float)(X - Gx); y = (float)(Y - Gy); z = (float)(Z - Gz);
+        mag = S.f[F_MAG][i];
+        mom[0][tx] = S.f[F_MX][i]; mom[1][tx] = S.f[F_MY][i]; mom[2][tx] = S.f[F_MZ][i];
+        mom[3][tx] = S.f[F_CX][i]; mom[4][tx] = S.f[F_CY][i]; mom[5][tx] = S.f[F_CZ][i];
+        const uint32_t meta = S.u[U_META][i];
+        comp = meta & 0xFFu; fiber = meta >> 8;
+    }
+    const MeshDev& g = subS[wi].g;
+    const AccelDev& acc = subS[wi].acc;
+    const float perm = J.perm;
+    const uint32_t reflType = J.reflType, maxSub = J.maxSub;
+    const uint32_t k0 = J.key0, k1 = J.key1;
+    const float* __restrict__ wave = J.wave;
+    uint32_t nrefl = 0, nperm = 0, st = 0, it = 0, excluded = 0xFFFFFFFFu, sub_n = 0;
+    PrecCount pc;
+    bool active = valid && nsteps > 0;
+    bool fresh = active;
+    Draw d;
+    d.nx = d.ny = d.nz = 0.0f; d.u = 1.0f;
+    float umax = 1.0f, umin = 0.0f;
+    float ox = x, oy = y, oz = z, px = x, py = y, pz = z;
+    while (__any_sync(FULL, active)) {
+        if (fresh) {
+            d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+            ox = x; oy = y; oz = z;
+            const float sd = J.sd[comp & 3u];
+            px = x + d.nx * sd; py = y + d.ny * sd; pz = z + d.nz * sd;
+            excluded = 0xFFFFFFFFu;
+            umax = 1.0f; umin = 0.0f;
+            sub_n = 0;
+            fresh = false;
+        }
+        const bool open = active;
+        bool found;
+        FastHit best;
+        local_round(H, Lw, g, acc, lane, open, gx, gy, gz, ox, oy, oz, px, py, pz, excluded, found, best, pc);
+        if (open) {
+            bool finish = !found;
+            if (found) {
+                apply_hit(g, best, d.u, perm, reflType, umax, umin, ox, oy, oz, px, py, pz, comp, fiber, excluded,
+                          nrefl, nperm);
+                if (++sub_n >= maxSub) {
+                    st |= kStatusSubsegCap;
+                    px = ox; py = oy; pz = oz;
+                    finish = true;
+                }
+            }
+            if (finish) {
+                // clamp in absolute coordinates, then move the origin so the
+                // offset is back in [0, 1/16)
+                float ax = gx + px, ay = gy + py, az = gz + pz;
+                if (ax > J.clampHi) px = J.clampHi - gx; else if (ax < J.clampLo) px = J.clampLo - gx;
+                if (ay > J.clampHi) py = J.clampHi - gy; else if (ay < J.clampLo) py = J.clampLo - gy;
+                if (az > J.clampHi) pz = J.clampHi - gz; else if (az < J.clampLo) pz = J.clampLo - gz;
+                const float sx = floorf(px * 16.0f) * kLatticeH, sy = floorf(py * 16.0f) * kLatticeH,
+                            sz = floorf(pz * 16.0f) * kLatticeH;
+                gx += sx; gy += sy; gz += sz;
+                x = px - sx; y = py - sy; z = pz - sz;
+                const float T2 = J.T2[comp & 3u];
+                if (T2 > 0.0f) mag += -mag / T2 * J.dt;
+                const float w = __ldg(wave + ls0 + it);
+                kahan_add(mom[0][tx], mom[3][tx], w * (gx + x));
+                kahan_add(mom[1][tx], mom[4][tx], w * (gy + y));
+                kahan_add(mom[2][tx], mom[5][tx], w * (gz + z));
+                if (++it >= nsteps) active = false;
+                else fresh = true;
+            }
+        }
+        __syncwarp();
+    }
+    if (valid) {
+        const double X = (double)gx + (double)x, Y = (double)gy + (double)y, Z = (double)gz + (double)z;
+        S.d[D_X][i] = X; S.d[D_Y][i] = Y; S.d[D_Z][i] = Z; S.d[D_MAG][i] = (double)mag;
+        S.f[F_X][i] = (float)X; S.f[F_Y][i] = (float)Y; S.f[F_Z][i] = (float)Z;
+        S.f[F_MAG][i] = mag;
+        S.f[F_MX][i] = mom[0][tx]; S.f[F_MY][i] = mom[1][tx]; S.f[F_MZ][i] = mom[2][tx];
+        S.f[F_CX][i] = mom[3][tx]; S.f[F_CY][i] = mom[4][tx]; S.f[F_CZ][i] = mom[5][tx];
+        S.u[U_META][i] = (comp & 0xFFu) | (fiber << 8);
+    }
+    // per-job counters {reflections, permeations, records examined, FP64 re-tests}
+    unsigned long long r = nrefl, p = nperm, te = pc.records, ex = pc.exact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        p += __shfl_down_sync(FULL, p, o);
+        te += __shfl_down_sync(FULL, te, o);
+        ex += __shfl_down_sync(FULL, ex, o);
+    }
+    if (lane == 0) {
+        if (r) atomicAdd(jobCounts + 4 * jb, r);
+        if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+        if (te) atomicAdd(jobCounts + 4 * jb + 2, te);
+        if (ex) atomicAdd(jobCounts + 4 * jb + 3, ex);
     }
     if (st) atomicOr(status, st);
 }
@@ -562,7 +711,7 @@ struct dsim_batch {
     uint32_t *hist = nullptr, *hstart = nullptr, *scratch = nullptr;
     uint64_t keyCap = 0, K = 0;
     uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
-    bool anyPrecise = false;
+    bool anyPrecise = false, anyLocal = false;
     cudaGraphExec_t exec = nullptr;
     bool graphValid = false;
     int graphCur = -1;
@@ -645,7 +794,7 @@ uint32_t step_layouts(const dsim_batch* b) {
     for (const auto& j : b->jobs) {
         const SubDev& s = b->subs[j.d.sub];
         if (s.kind == kSubCyl) mask |= kHasCyl;
-        else if (!(j.d.flags & DSIM_JOB_PRECISE)) mask |= 1u << (s.acc.wide == 2 ? 2u : 1u);
+        else if (!j.d.flags) mask |= 1u << (s.acc.wide == 2 ? 2u : 1u);
     }
     if ((mask & kHasCyl) && !(mask & 6u)) mask |= 1u << 1;
     return mask;
@@ -655,7 +804,8 @@ uint32_t step_layouts(const dsim_batch* b) {
 // instantiations, advance
 uint64_t chunk_launches(const dsim_batch* b) {
     const uint32_t mask = step_layouts(b);
-    return 5ull + (uint64_t)__builtin_popcount(mask & 6u) + (b->anyPrecise ? 1ull : 0ull) + 1ull;
+    return 5ull + (uint64_t)__builtin_popcount(mask & 6u) + (b->anyPrecise ? 1ull : 0ull) + (b->anyLocal ? 1ull : 0ull) +
+           1ull;
 }
 
 template <int LAYOUT>
@@ -689,6 +839,9 @@ int enqueue_chunk(dsim_batch* b) {
     uint32_t cylHere = (mask & kHasCyl) ? 1u : 0u;
     if (mask & (1u << 1)) { launch_step_layout<1>(b, grid, D, cylHere); cylHere = 0; }
     if (mask & (1u << 2)) launch_step_layout<2>(b, grid, D, cylHere);
+    if (b->anyLocal)
+        k_batch_step_local<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                             b->d_status, b->d_counts);
     if (b->anyPrecise)
         k_batch_step64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status,
                                                          b->d_counts);
@@ -892,10 +1045,14 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     J.inR = d->innerRadiusProportion * d->innerRadiusProportion;
     J.key0 = (uint32_t)d->seed;
     J.key1 = (uint32_t)(d->seed >> 32);
-    J.flags = d->flags & DSIM_JOB_PRECISE;
+    J.flags = d->flags & (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL);
+    if (J.flags == (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL)) {
+        set_last_error(kErrInvalid, "dsim_batch_submit: DSIM_JOB_PRECISE and DSIM_JOB_LOCAL exclude each other");
+        return kErrInvalid;
+    }
     J.spinR = d->spinRadius;
     if (J.flags && cyl) {
-        set_last_error(kErrInvalid, "dsim_batch_submit: the precision form applies to mesh jobs");
+        set_last_error(kErrInvalid, "dsim_batch_submit: the precision and cell-local forms apply to mesh jobs");
         return kErrInvalid;
     }
     if (J.flags) {
@@ -940,7 +1097,7 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     for (int u = 0; u < kBU; u++)
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->buf[b->cur].u[u] + b->N, hu[u].data(), (size_t)pad * 4, cudaMemcpyHostToDevice, b->st));
     if (J.flags) {
-        // the precision form's FP64 state: the given positions, magnitude 1
+        // the FP64 state of the precision and cell-local forms: the given positions, magnitude 1
         std::vector<double> hd[kBD];
         for (int f = 0; f < kBD; f++) hd[f].assign(pad, 0.0);
         for (uint32_t k = 0; k < d->nSpins; k++) {
@@ -957,7 +1114,8 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
     DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 4 * jobIndex, 0, 32, b->st));
     DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
-    if (J.flags) b->anyPrecise = true;
+    if (J.flags & DSIM_JOB_PRECISE) b->anyPrecise = true;
+    if (J.flags & DSIM_JOB_LOCAL) b->anyLocal = true;
     invalidate_graph(b);
     *jobId = j.id;
     return kOk;
@@ -1095,8 +1253,8 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
 
 int dsim_batch_get_precise(dsim_batch* b, uint32_t jobId, double* pos3, double* mag) {
     BatchJob* j = b ? find_job(b, jobId) : nullptr;
-    if (!j || !(j->d.flags & DSIM_JOB_PRECISE)) {
-        set_last_error(kErrInvalid, "dsim_batch_get_precise: %u is not a precision-form job", jobId);
+    if (!j || !j->d.flags) {
+        set_last_error(kErrInvalid, "dsim_batch_get_precise: %u is neither a precision-form nor a cell-local job", jobId);
         return kErrInvalid;
     }
     const uint32_t n = j->nSpins;
@@ -1208,8 +1366,11 @@ int dsim_batch_compact(dsim_batch* b) {
     b->cur = 1 - b->cur;
     b->jobs = kept;
     b->N = slot;
-    b->anyPrecise = false;
-    for (const auto& j : b->jobs) b->anyPrecise |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
+    b->anyPrecise = b->anyLocal = false;
+    for (const auto& j : b->jobs) {
+        b->anyPrecise |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
+        b->anyLocal |= (j.d.flags & DSIM_JOB_LOCAL) != 0;
+    }
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
     if (!newCounts.empty())
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_counts, newCounts.data(), newCounts.size() * 8, cudaMemcpyHostToDevice, b->st));

@@ -359,12 +359,14 @@ class Batch:
 
     def submit(self, substrate, pos, comp, fiber, steps, dt, step_sd, T2, phase_constant, seed,
                permeability=0.0, waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None,
-               reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0, precise=False):
+               reflection_type=1, spin_radius=0.005, inner_radius_proportion=1.0, precise=False, local=False):
+        """precise: the FP64 step (DSIM_JOB_PRECISE); local: FP32 cell-local
+        offsets with FP64 re-tests (DSIM_JOB_LOCAL)."""
         pos = np.ascontiguousarray(pos, F).reshape(-1)
         n = len(pos) // 3
         d, tab = _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability, waveform,
                            delta, Delta, frequency, table, reflection_type, spin_radius,
-                           inner_radius_proportion, precise)
+                           inner_radius_proportion, precise, local)
         jid = C.c_uint32()
         comp = np.ascontiguousarray(comp, np.uint8)
         fib = None if fiber is None else np.ascontiguousarray(fiber, np.uint32)
@@ -416,7 +418,8 @@ class Batch:
         return int(c[0]), int(c[1])
 
     def get_precise(self, job, n):
-        """FP64 positions (n x 3) and magnitudes of a precision-form job, in spin order."""
+        """FP64 positions (n x 3) and magnitudes of a precision-form or
+        cell-local job, in spin order."""
         pos = np.zeros(3 * n, np.float64); mag = np.zeros(n, np.float64)
         check(native().dsim_batch_get_precise(self.h, int(job), pos, mag))
         return pos.reshape(n, 3), mag
@@ -453,7 +456,7 @@ def pgse_table(steps, dt, delta, Delta):
 
 def _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permeability=0.0,
               waveform="pgse", delta=0.0, Delta=0.0, frequency=0.0, table=None, reflection_type=1,
-              spin_radius=0.005, inner_radius_proportion=1.0, precise=False):
+              spin_radius=0.005, inner_radius_proportion=1.0, precise=False, local=False):
     d = _lib.JobDesc()
     d.substrate, d.nSpins, d.steps = int(substrate), int(n), int(steps)
     d.deltaTime = float(dt)
@@ -474,7 +477,7 @@ def _job_desc(substrate, n, steps, dt, step_sd, T2, phase_constant, seed, permea
         assert len(tab) >= steps
         d.table = tab.ctypes.data
     d.seed = int(seed)
-    d.flags = 1 if precise else 0
+    d.flags = (1 if precise else 0) | (2 if local else 0)
     return d, tab
 
 

@@ -53,7 +53,7 @@ typedef struct {
     float frequency;               /* Hz (OGSE) */
     const float* table;            /* DSIM_WAVE_TABLE: `steps` values (host) */
     uint64_t seed;                 /* Philox key; counter = (spin, step, 0) */
-    uint32_t flags;                /* DSIM_JOB_PRECISE: precision form (mesh jobs) */
+    uint32_t flags;                /* DSIM_JOB_PRECISE or DSIM_JOB_LOCAL (mesh jobs) */
     uint32_t reserved;
 } dsim_job_desc;
 
@@ -65,6 +65,15 @@ typedef struct {
  * sub-segment.  Positions and magnitudes persist in FP64
  * (dsim_batch_get_precise); dsim_batch_get returns them rounded to float. */
 #define DSIM_JOB_PRECISE 1u
+/* Cell-local form: the plain FP32 step with every position held as an FP32
+ * offset from a lattice origin (a multiple of 1/16 in normalised units), so
+ * positions round about 16x finer than absolute FP32 coordinates; the
+ * intersections whose FP32 outcome lies within the FP32 error band of a
+ * decision boundary (crossing parameter near 0 or 1, a barycentric coordinate
+ * within 1e-5 of an edge) are decided again in FP64 on the FP64 triangle
+ * helpers; moments are Kahan-compensated FP32.  Exclusive with
+ * DSIM_JOB_PRECISE.  dsim_batch_get_precise returns origin + offset. */
+#define DSIM_JOB_LOCAL 2u
 
 /* spinCapacity: packed spin slots (each job is padded to a multiple of 32) */
 int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** out);
@@ -100,10 +109,11 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
                    uint8_t* compartment, uint32_t* fiber);
 /* per-job {reflections or rejections, permeations} and status bits */
 int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]);
-/* precision form: {fine-grid records examined, FP64 triangle tests} */
+/* precision and cell-local forms: {fine-grid records examined, FP64 triangle
+ * tests} */
 int dsim_batch_precision_counts(dsim_batch* b, uint32_t jobId, uint64_t out[2]);
-/* precision form: FP64 positions (3 per spin) and magnitudes in spin order;
- * DSIM_EINVAL for a job without DSIM_JOB_PRECISE.  Synchronous. */
+/* precision and cell-local forms: FP64 positions (3 per spin) and magnitudes
+ * in spin order; DSIM_EINVAL for a plain job.  Synchronous. */
 int dsim_batch_get_precise(dsim_batch* b, uint32_t jobId, double* pos3, double* mag);
 uint32_t dsim_batch_status(dsim_batch* b);
 /* drop finished jobs whose results were read and repack the others */
