@@ -813,7 +813,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
         if (m->kernel == 1) rc = launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st);
         else if (m->kernel >= 5)
             rc = launch_mesh_step_flat(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
-                                       m->kernel == 5 ? 8 : (m->kernel == 7 ? 4 : 6), m->kernel == 8);
+                                       m->kernel == 5 ? 8 : (m->kernel == 7 ? 4 : 6), m->kernel == 8, m->kernel == 9);
         else
             rc = launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
                                        m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
@@ -824,7 +824,7 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
 }
 
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant) {
-    if (!m || variant < 1 || variant > 8) { set_last_error(kErrInvalid, "kernel variant must be 1..8"); return kErrInvalid; }
+    if (!m || variant < 1 || variant > 9) { set_last_error(kErrInvalid, "kernel variant must be 1..9"); return kErrInvalid; }
     m->kernel = variant;
     return kOk;
 }

@@ -121,7 +121,7 @@ int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepA
 // flat.cu: warp-flattened candidate lists (same results); occupancy 6 or 8
 int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
                           const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 8,
-                          bool queue = false);
+                          bool queue = false, bool stage = false);
 int launch_aos_to_soa(const float* pos, const void* spin, const SpinsSorted& D, cudaStream_t st);
 int launch_soa_to_aos(const SpinsSorted& S, float* pos, void* spin, uint32_t* spinKeys,
                       uint32_t iterations, cudaStream_t st);

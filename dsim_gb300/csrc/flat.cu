@@ -30,13 +30,15 @@
 namespace dsim {
 
 // QUEUE (32-byte records): records past the plane test are finished 32 at a
-// time from a per-warp queue (flat_round_mode's Q)
-template <bool STATS, int MINB, int LAYOUT, bool QUEUE = false>
+// time from a per-warp queue (flat_round_mode's Q); STAGE: records staged in
+// shared memory by double-buffered asynchronous copies (flat_round_mode's P)
+template <bool STATS, int MINB, int LAYOUT, bool QUEUE = false, bool STAGE = false>
 __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g, AccelDev acc,
                                                                        MeshStepArgs a, SpinsSorted S,
                                                                        int rng) {
     __shared__ FlatWarp wh[kFlatWarps];
     __shared__ FlatQueue wq[QUEUE ? kFlatWarps : 1];
+    __shared__ FlatStage ws[STAGE ? kFlatWarps : 1];
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     FlatWarp& H = wh[threadIdx.x >> 5];
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
             bool found;
             FastHit best;
             flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best,
-                                    QUEUE ? &wq[threadIdx.x >> 5] : nullptr);
+                                    QUEUE ? &wq[threadIdx.x >> 5] : nullptr, STAGE ? &ws[threadIdx.x >> 5] : nullptr);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
 }
 
 int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy, bool queue) {
+                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy, bool queue, bool stage) {
     if (S.N == 0 || a.iterations == 0) return kOk;
     dim3 block(kFlatThreads), grid((S.N + kFlatThreads - 1) / kFlatThreads);
     // one instantiation per record layout keeps each kernel's registers to its own path
@@ -145,6 +147,8 @@ int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepA
         if (occupancy >= 8) k_mesh_step_flat<false, 8, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
         else if (occupancy >= 6) k_mesh_step_flat<false, 6, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
         else k_mesh_step_flat<false, 4, 2><<<grid, block, 0, st>>>(g, acc, a, S, rng);
+    } else if (acc.wide == 1 && stage) {
+        k_mesh_step_flat<false, 6, 1, false, true><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     } else if (acc.wide == 1 && queue) {
         k_mesh_step_flat<false, 6, 1, true><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     } else if (acc.wide == 1) {

@@ -86,6 +86,23 @@ __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, flo
     return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
 }
 
+// Double-buffered staging of 32-byte records in shared memory: while a warp
+// tests one 64-record window, each lane's two records of the next window are
+// already in flight by asynchronous copies (cp.async, 16 bytes each), so the
+// load latency of a window overlaps the tests of the previous one.  A lane
+// reads back only the copies it issued itself.
+struct FlatStage {
+    float4 rec[2][32][4];  // [buffer][lane][q0, pt0, q1, pt1]
+};
+
+__device__ __forceinline__ void stage_copy16(float4* dst, const float4* src) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // the rest of the exact test of queued record e for owner o (plane test passed)
 __device__ __forceinline__ void flat_test_queued(FlatWarp& H, const MeshDev& g, const AccelDev& acc, uint32_t e,
                                                  uint32_t o) {
@@ -125,7 +142,8 @@ template <int LAYOUT = 0>
 __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, const AccelDev& acc,
                                                 uint32_t lane, bool open, float ox, float oy, float oz,
                                                 float px, float py, float pz, uint32_t excluded,
-                                                bool& found, FastHit& best, FlatQueue* Q = nullptr) {
+                                                bool& found, FastHit& best, FlatQueue* Q = nullptr,
+                                                FlatStage* P = nullptr) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
@@ -190,6 +208,59 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                     flat_file_hit(H, o0, h);
                 if (v1 && test_full(f1, H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1], H.dz[o1], h))
                     flat_file_hit(H, o1, h);
+            }
+        } else if (LAYOUT == 1 && P) {
+            // windows of 64 records, the next one staged while this one is tested
+            uint32_t e0 = 0, e1 = 0, o0 = 0, o1 = 0;
+            bool v0 = false, v1 = false;
+            auto locate = [&](uint32_t rb, uint32_t& a0, uint32_t& a1, uint32_t& w0_, uint32_t& w1_, bool& u0,
+                              bool& u1) {
+                const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
+                const uint32_t j0 = min(warp_find(rincl, r0), 31u);
+                const uint32_t j1 = min(warp_find(rincl, r1), 31u);
+                a0 = __shfl_sync(FULL, rbase, j0) + r0;
+                a1 = __shfl_sync(FULL, rbase, j1) + r1;
+                w0_ = __shfl_sync(FULL, ow, j0);
+                w1_ = __shfl_sync(FULL, ow, j1);
+                u0 = r0 < rtotal;
+                u1 = r1 < rtotal;
+            };
+            auto stage = [&](uint32_t buf, uint32_t a0, uint32_t a1, bool u0, bool u1) {
+                float4* d = P->rec[buf][lane];
+                if (u0) {
+                    stage_copy16(d, &acc.recw[a0].q);
+                    stage_copy16(d + 1, &acc.recw[a0].pt);
+                }
+                if (u1) {
+                    stage_copy16(d + 2, &acc.recw[a1].q);
+                    stage_copy16(d + 3, &acc.recw[a1].pt);
+                }
+                stage_commit();
+            };
+            if (rtotal > 0) {
+                locate(0, e0, e1, o0, o1, v0, v1);
+                stage(0, e0, e1, v0, v1);
+            }
+            for (uint32_t rb = 0, buf = 0; rb < rtotal; rb += 64, buf ^= 1u) {
+                uint32_t n0 = 0, n1 = 0, p0 = 0, p1 = 0;
+                bool u0 = false, u1 = false;
+                const bool more = rb + 64 < rtotal;  // warp-uniform
+                if (more) {
+                    locate(rb + 64, n0, n1, p0, p1, u0, u1);
+                    stage(buf ^ 1u, n0, n1, u0, u1);
+                    stage_wait<1>();
+                } else {
+                    stage_wait<0>();
+                }
+                const float4* d = P->rec[buf][lane];
+                FastHit h;
+                if (v0 && test_wide_loaded(g, d[0], d[1], H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0],
+                                           H.dy[o0], H.dz[o0], h))
+                    flat_file_hit(H, o0, h);
+                if (v1 && test_wide_loaded(g, d[2], d[3], H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1],
+                                           H.dy[o1], H.dz[o1], h))
+                    flat_file_hit(H, o1, h);
+                e0 = n0; e1 = n1; o0 = p0; o1 = p1; v0 = u0; v1 = u1;
             }
         } else if (LAYOUT == 1 || (LAYOUT == 0 && acc.wide)) {
             for (uint32_t rb = 0; rb < rtotal; rb += 64) {

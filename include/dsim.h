@@ -74,7 +74,9 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
  * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM; 5, 6, 7 the
  * warp's candidate records flattened into one list, lanes stepping
  * independently (8, 6, 4 blocks per SM); 8 as 6, with the records that pass
- * the plane test queued and finished 32 at a time (32-byte records) */
+ * the plane test queued and finished 32 at a time; 9 as 6, with each 64-record
+ * window staged in shared memory by asynchronous copies while the previous
+ * one is tested (8 and 9: 32-byte records) */
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 /* fine-grid record size: 32 (default) holds the plane data for the exact
  * plane test; 16 holds a prefilter record only (half the bytes, one more

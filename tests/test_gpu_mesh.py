@@ -56,14 +56,15 @@ def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
     ("G", 0.0, 75, 20, 5, 16), ("G", 0.3, None, 7, 4, None), ("AM", 0.05, 100, 20, 7, None),
     ("AM", 0.05, None, 20, None, 64), ("G", 0.3, 37, 7, 5, 64), ("AM", 0.05, 300, 0, 4, 64),
     ("G", 0.3, 13, 1, 1, 64), ("AM", 0.05, None, 20, 8, None), ("G", 0.3, 37, 7, 8, None),
-    ("G", 0.0, 300, 0, 8, None)])
+    ("G", 0.0, 300, 0, 8, None), ("AM", 0.05, None, 20, 9, None), ("G", 0.3, 37, 7, 9, None),
+    ("AM", 0.05, 300, 0, 9, None)])
 def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort, kernel, records):
     """accel None: default fine grid; 0: reference-grid scan; other: fine
     cells per axis (coarser and finer than the reference grid).  sort: steps
     between spin reorderings (0 = never).  kernel: step kernel variant;
     records: fine-grid record bytes (kernel 8 queues the records that pass
-    the plane test on 32-byte records and falls back to kernel 6's path on
-    the others)."""
+    the plane test, kernel 9 stages records in shared memory by asynchronous
+    copies; both on 32-byte records, kernel 6's path on the others)."""
     from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
     case = MeshCase(tmp_path, membranes=membranes, permeability=perm, N=1500)
     iters = 60
