@@ -64,6 +64,7 @@ struct dsim_mesh {
     uint32_t* cell_start = nullptr;
     uint32_t* cell_tri = nullptr;
     Tri64* tri64 = nullptr;  // FP64 helpers, built for the first precision-form job
+    uint4* tri_cells = nullptr;  // each triangle's reference cells (up to 4)
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
     uint32_t kernel = 6;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened (8, 6, 4)
@@ -79,6 +80,7 @@ struct dsim_mesh {
         MeshDev g;
         g.cell_start = cell_start; g.cell_tri = cell_tri; g.plane = plane; g.bary = bary;
         g.tri64 = tri64;
+        g.tri_cells = tri_cells;
         g.n = n; g.L = L;
         return g;
     }
@@ -244,6 +246,7 @@ static void mesh_release(dsim_mesh* m) {
     if (!m) return;
     cudaFree(m->V); cudaFree(m->trgls); cudaFree(m->membrane); cudaFree(m->fiber);
     cudaFree(m->plane); cudaFree(m->bary); cudaFree(m->cell_start); cudaFree(m->cell_tri); cudaFree(m->tri64);
+    cudaFree(m->tri_cells);
     cudaFree(m->acc_start); cudaFree(m->acc_rec); cudaFree(m->acc_tri); cudaFree(m->acc_recw); cudaFree(m->acc_recf);
     delete m;
 }
@@ -297,6 +300,17 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
         if (cudaMemsetAsync(counter, 0, ncells * 4, st) != cudaSuccess) { rc = kErrCuda; break; }
         if ((rc = launch_tri_cells(true, m->nT, m->V, m->trgls, m->n, m->L, counter, m->cell_start, m->cell_tri, st))) break;
         if ((rc = launch_sort_cells(ncells, m->cell_start, m->cell_tri, st))) break;
+        if ((rc = dev_alloc(&m->tri_cells, m->nT, &m->bytes))) break;
+        if (m->nT > ncells) {  // the scan scratch is sized for ncells; use a count of its own
+            uint32_t* tcount = nullptr;
+            if ((rc = dev_alloc(&tcount, m->nT))) break;
+            rc = launch_tri_cell_lists(ncells, m->nT, m->cell_start, m->cell_tri, tcount, m->tri_cells, st);
+            if (!rc && cudaStreamSynchronize(st) != cudaSuccess) rc = kErrCuda;
+            cudaFree(tcount);
+            if (rc) break;
+        } else if ((rc = launch_tri_cell_lists(ncells, m->nT, m->cell_start, m->cell_tri, counter, m->tri_cells, st))) {
+            break;
+        }
         std::vector<uint32_t> cs(ncells + 1);
         if (cudaMemcpyAsync(cs.data(), m->cell_start, cs.size() * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) { rc = kErrCuda; break; }

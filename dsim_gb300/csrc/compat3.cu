@@ -313,6 +313,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
     MeshDev g;
     g.cell_start = s.cell_start; g.cell_tri = s.cell_tri; g.plane = s.plane; g.bary = s.bary;
     g.tri64 = nullptr;
+    g.tri_cells = nullptr;
     g.n = s.numCubes; g.L = s.cubeLength;
     MeshStepArgs a;
     memset(&a, 0, sizeof(a));

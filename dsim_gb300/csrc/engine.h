@@ -29,6 +29,7 @@ struct MeshDev {
     const TriPlane* plane;       // per triangle
     const TriBary* bary;         // per triangle
     const Tri64* tri64;          // per triangle, precision form only (else null)
+    const uint4* tri_cells;      // per triangle: its reference cells (up to 4; else null)
     uint32_t n;                  // cells per axis
     float L;                     // cell edge, normalised units (2 / n)
 };
@@ -131,6 +132,11 @@ int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
                              const uint32_t* membrane, const uint32_t* fiber, TriPlane* plane,
                              TriBary* bary, cudaStream_t st);
 int launch_tri64(uint32_t nT, const float* V, const uint32_t* trgls, Tri64* out, cudaStream_t st);
+// every triangle's reference cells from the cell lists: up to 4 in a uint4
+// (unused entries kCellNone), kCellMany in every entry when there are more
+static constexpr uint32_t kCellNone = 0xFFFFFFFFu, kCellMany = 0xFFFFFFFEu;
+int launch_tri_cell_lists(uint32_t ncells, uint32_t nT, const uint32_t* cell_start, const uint32_t* cell_tri,
+                          uint32_t* count, uint4* out, cudaStream_t st);
 int launch_records_from_helpers(uint32_t nT, const float* V, const float* H,
                                 const uint32_t* triInfo, TriPlane* plane, TriBary* bary,
                                 cudaStream_t st);

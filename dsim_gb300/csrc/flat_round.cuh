@@ -336,6 +336,11 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
         uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
         uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
         uint32_t bq = 0;
+        // each hit's reference cells, loaded together before the walk
+        uint4 hc[kFlatSlots];
+#pragma unroll
+        for (int q = 0; q < kFlatSlots; q++)
+            hc[q] = ((uint32_t)q < n) ? hit_cells(g, H.t[q][lane]) : make_uint4(kCellNone, kCellNone, kCellNone, kCellNone);
         uint32_t cx = sx;
         do {
             uint32_t cy = sy;
@@ -343,9 +348,11 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                 uint32_t cz = sz;
                 do {
                     uint32_t c = gn * gn * cz + gn * cy + cx;
-                    for (uint32_t q = 0; q < n; q++) {
+#pragma unroll
+                    for (uint32_t q = 0; q < (uint32_t)kFlatSlots; q++) {
+                        if (q >= n) break;
                         const uint32_t t = H.t[q][lane];
-                        if (!in_ref_cell(g, c, t)) continue;
+                        if (!hit_in_cell(g, hc[q], c, t)) continue;
                         const float d2 = H.d2[q][lane];
                         if (!found || d2 < H.d2[bq][lane] || (d2 == H.d2[bq][lane] && t < H.t[bq][lane])) {
                             bq = q;

@@ -471,6 +471,34 @@ int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
     return kOk;
 }
 
+// every triangle's reference cells: one thread per cell appends the cell to
+// each of its triangles' records (order within a record is irrelevant)
+__global__ void k_tri_cell_lists(uint32_t ncells, const uint32_t* __restrict__ cell_start,
+                                 const uint32_t* __restrict__ cell_tri, uint32_t* count, uint4* out) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    for (uint32_t k = cell_start[c]; k < cell_start[c + 1]; k++) {
+        const uint32_t t = cell_tri[k];
+        const uint32_t slot = atomicAdd(count + t, 1u);
+        if (slot < 4) reinterpret_cast<uint32_t*>(out + t)[slot] = c;
+    }
+}
+__global__ void k_tri_cell_many(uint32_t nT, const uint32_t* __restrict__ count, uint4* out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nT && count[t] > 4) out[t] = make_uint4(kCellMany, kCellMany, kCellMany, kCellMany);
+}
+
+int launch_tri_cell_lists(uint32_t ncells, uint32_t nT, const uint32_t* cell_start, const uint32_t* cell_tri,
+                          uint32_t* count, uint4* out, cudaStream_t st) {
+    if (nT == 0) return kOk;
+    DSIM_CUDA_TRY(cudaMemsetAsync(count, 0, (size_t)nT * 4, st));
+    DSIM_CUDA_TRY(cudaMemsetAsync(out, 0xFF, (size_t)nT * sizeof(uint4), st));
+    k_tri_cell_lists<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, cell_start, cell_tri, count, out);
+    k_tri_cell_many<<<(nT + 255) / 256, 256, 0, st>>>(nT, count, out);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
 int launch_tri64(uint32_t nT, const float* V, const uint32_t* trgls, Tri64* out, cudaStream_t st) {
     if (nT == 0) return kOk;
     k_tri64<<<(nT + 255) / 256, 256, 0, st>>>(nT, V, trgls, out);

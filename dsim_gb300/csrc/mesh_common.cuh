@@ -48,6 +48,18 @@ __device__ __forceinline__ bool in_ref_cell(const MeshDev& g, uint32_t c, uint32
     return false;
 }
 
+// Membership of triangle t in reference cell c from the triangle's own cell
+// record (loaded once per hit): the same answer as in_ref_cell with no
+// dependent loads; a triangle in more than four cells keeps the search.
+__device__ __forceinline__ bool hit_in_cell(const MeshDev& g, uint4 cells, uint32_t c, uint32_t t) {
+    if (cells.x == kCellMany) return in_ref_cell(g, c, t);
+    return (cells.x == c) | (cells.y == c) | (cells.z == c) | (cells.w == c);
+}
+__device__ __forceinline__ uint4 hit_cells(const MeshDev& g, uint32_t t) {
+    if (!g.tri_cells) return make_uint4(kCellMany, kCellMany, kCellMany, kCellMany);
+    return __ldg(g.tri_cells + t);
+}
+
 __device__ __forceinline__ uint32_t ref_coord(float p, float L, uint32_t n) {
     float f = floorf((p + 1.0f) / L);
     float hi = (float)(n - 1);
