@@ -312,6 +312,10 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
     }
     if (n == 0) return;
     uint32_t bq = 0;
+    uint4 hc[kFlatSlots];  // each hit's reference cells, loaded together before the walk
+#pragma unroll
+    for (int q = 0; q < kFlatSlots; q++)
+        hc[q] = ((uint32_t)q < n) ? hit_cells(g, H.t[q][lane]) : make_uint4(kCellNone, kCellNone, kCellNone, kCellNone);
     uint32_t cx = sx;
     do {
         uint32_t cy = sy;
@@ -319,9 +323,11 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
             uint32_t cz = sz;
             do {
                 const uint32_t c = gn * gn * cz + gn * cy + cx;
-                for (uint32_t q = 0; q < n; q++) {
+#pragma unroll
+                for (uint32_t q = 0; q < (uint32_t)kFlatSlots; q++) {
+                    if (q >= n) break;
                     const uint32_t t = H.t[q][lane];
-                    if (!in_ref_cell(g, c, t)) continue;
+                    if (!hit_in_cell(g, hc[q], c, t)) continue;
                     const float d2 = H.d2[q][lane];
                     if (!found || d2 < H.d2[bq][lane] || (d2 == H.d2[bq][lane] && t < H.t[bq][lane])) {
                         bq = q;

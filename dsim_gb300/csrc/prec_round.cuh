@@ -329,6 +329,10 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
     const uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
     const uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
     double bd2 = 0.0;
+    uint4 hc[kFlatSlots];  // each hit's reference cells, loaded together before the walk
+#pragma unroll
+    for (int q = 0; q < kFlatSlots; q++)
+        hc[q] = ((uint32_t)q < n) ? hit_cells(g, H.t[q][lane]) : make_uint4(kCellNone, kCellNone, kCellNone, kCellNone);
     uint32_t cx = sx;
     do {
         uint32_t cy = sy;
@@ -336,9 +340,11 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
             uint32_t cz = sz;
             do {
                 const uint32_t c = gn * gn * cz + gn * cy + cx;
-                for (uint32_t q = 0; q < n; q++) {
+#pragma unroll
+                for (uint32_t q = 0; q < (uint32_t)kFlatSlots; q++) {
+                    if (q >= n) break;
                     const uint32_t t = H.t[q][lane];
-                    if (!in_ref_cell(g, c, t)) continue;
+                    if (!hit_in_cell(g, hc[q], c, t)) continue;
                     const double r = __hiloint2double(__float_as_int(H.y[q][lane]), __float_as_int(H.x[q][lane]));
                     double x, y, z;
                     const double d2 = hit_point64(ox, oy, oz, dx, dy, dz, r, x, y, z);
