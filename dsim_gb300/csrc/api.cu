@@ -143,10 +143,11 @@ struct dsim_cyl {
     float4* fibers = nullptr;
     uint32_t* cc = nullptr;
     uint32_t* cubes = nullptr;
+    float4* cubeF = nullptr;  // each grid entry's fiber record
     uint64_t bytes = 0;
     CylDev dev() const {
         CylDev g;
-        g.fibers = fibers; g.cube_count = cc; g.cubes = cubes;
+        g.fibers = fibers; g.cube_count = cc; g.cubes = cubes; g.cube_fibers = cubeF;
         g.n = host.numCubes; g.maxFPC = host.maxFPC; g.L = host.cubeLength;
         g.nF = host.nF;
         return g;
@@ -440,7 +441,7 @@ void dsim_mesh_free(dsim_mesh* m) { mesh_release(m); }
 // ---------------------------------------------------------------------------
 static void cyl_release(dsim_cyl* c) {
     if (!c) return;
-    cudaFree(c->fibers); cudaFree(c->cc); cudaFree(c->cubes);
+    cudaFree(c->fibers); cudaFree(c->cc); cudaFree(c->cubes); cudaFree(c->cubeF);
     delete c;
 }
 
@@ -454,6 +455,22 @@ static int cyl_upload(dsim_cyl* c) {
     DSIM_CUDA_TRY(cudaMemcpy(c->cc, h.cubeCounter.data(), h.cubeCounter.size() * 4, cudaMemcpyHostToDevice));
     if (!h.cubes.empty())
         DSIM_CUDA_TRY(cudaMemcpy(c->cubes, h.cubes.data(), h.cubes.size() * 4, cudaMemcpyHostToDevice));
+    // the fiber records inline in the grid, so a cell scan reads no index
+    // first; only for a grid whose listed entries all name a fiber
+    const size_t ncells = h.cubeCounter.size();
+    std::vector<float> inl(h.cubes.size() * 4, 0.0f);
+    bool ok = !h.cubes.empty();
+    for (size_t cell = 0; cell < ncells && ok; cell++)
+        for (uint32_t j = 0; j < h.cubeCounter[cell] && ok; j++) {
+            const size_t k = cell * h.maxFPC + j;
+            const uint32_t fi = h.cubes[k];
+            if (fi >= h.nF) { ok = false; break; }
+            for (int q = 0; q < 4; q++) inl[4 * k + q] = h.fiberPos[4 * (size_t)fi + q];
+        }
+    if (ok) {
+        if ((rc = dev_alloc(&c->cubeF, h.cubes.size(), &c->bytes))) return rc;
+        DSIM_CUDA_TRY(cudaMemcpy(c->cubeF, inl.data(), inl.size() * 4, cudaMemcpyHostToDevice));
+    }
     return kOk;
 }
 

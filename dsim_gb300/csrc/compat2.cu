@@ -128,6 +128,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, float deltaTime, float*
         }
     }
     CylDev g;
+    g.cube_fibers = nullptr;  // the reference's own grid arrays: fiber indices only
     g.fibers = fiberPos ? reinterpret_cast<const float4*>(fiberPos) : s.fibers;
     g.cube_count = cubeCounters;
     g.cubes = cubeList ? cubeList : s.boundList;

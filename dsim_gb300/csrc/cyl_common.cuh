@@ -65,33 +65,49 @@ __device__ __forceinline__ void cyl_membranes(const CylDev& g, float ox, float o
             else if (endD < inR * radSq) imo = 0;
             else imo = 1;
         } else {
+            // a cell's entries: the inline record when the grid has them (the
+            // index is read only when the spin changes region), else the index
+            // and then the fiber
             uint32_t cube = cyl_cell(px, py, pz, g.L, g.n);
             uint32_t cnt = __ldg(g.cube_count + cube);
             const uint32_t* list = g.cubes + (size_t)cube * g.maxFPC;
+            const float4* inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
             for (uint32_t j = 0; j < cnt; j++) {
-                uint32_t fi = __ldg(list + j);
-                if (fi >= g.nF) { status |= kStatusBadCell; continue; }
-                float4 f = __ldg(g.fibers + fi);
+                float4 f;
+                uint32_t fi = 0;
+                if (inl) {
+                    f = __ldg(inl + j);
+                } else {
+                    fi = __ldg(list + j);
+                    if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+                    f = __ldg(g.fibers + fi);
+                }
                 float radSq = f.w;
                 float cur = cyl_dist_sq(px, py, pz, f);
                 if ((cur <= radSq) & (cur > inR * radSq)) {
                     if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
-                    else { imo = 1; nearest = fi; nperm++; }
+                    else { imo = 1; nearest = inl ? __ldg(list + j) : fi; nperm++; }
                 } else if (cur < inR * radSq) {
                     if (u < 1.0f - perm) { px = ox; py = oy; pz = oz; nrej++; }
                     else if ((1.0f - perm < u) & (u < 1.0f - perm * perm)) {
-                        px = ox; py = oy; pz = oz; nearest = fi; imo = 1; nrej++;
-                    } else { imo = 0; nearest = fi; nperm++; }
+                        px = ox; py = oy; pz = oz; nearest = inl ? __ldg(list + j) : fi; imo = 1; nrej++;
+                    } else { imo = 0; nearest = inl ? __ldg(list + j) : fi; nperm++; }
                 }
             }
             if (imo == 2) {
                 cube = cyl_cell(px, py, pz, g.L, g.n);
                 cnt = __ldg(g.cube_count + cube);
                 list = g.cubes + (size_t)cube * g.maxFPC;
+                inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
                 for (uint32_t j = 0; j < cnt; j++) {
-                    uint32_t fi = __ldg(list + j);
-                    if (fi >= g.nF) { status |= kStatusBadCell; continue; }
-                    float4 f = __ldg(g.fibers + fi);
+                    float4 f;
+                    if (inl) {
+                        f = __ldg(inl + j);
+                    } else {
+                        const uint32_t fi = __ldg(list + j);
+                        if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+                        f = __ldg(g.fibers + fi);
+                    }
                     float nd = cyl_dist_sq(px, py, pz, f);
                     if (nd < inR * f.w) { px = ox; py = oy; pz = oz; nrej++; }
                     else if (nd < f.w) { px = ox; py = oy; pz = oz; nrej++; }

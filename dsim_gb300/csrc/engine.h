@@ -179,6 +179,7 @@ struct CylDev {
     const float4* fibers;       // {x, y, z, r^2}; the axis coordinate is 2.0
     const uint32_t* cube_count; // dense reference grid (dSim2 addEntities)
     const uint32_t* cubes;
+    const float4* cube_fibers;  // per grid entry, its fiber's record inline (or null)
     uint32_t n, maxFPC;
     float L;
     uint32_t nF;                // number of fibers (index bound)
