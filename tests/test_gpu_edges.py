@@ -6,6 +6,8 @@ property at the full mesh size.
   fine-cell boundaries, where the cell of a point and the first cell of the
   reference's walk are decided by floor of an exact multiple.
 * Spins at the clamp (+-0.995) with steps pushing them out of the box.
+* Cylinders: spins on grid-cell boundaries, on cylinder surfaces and at the
+  clamp, bit for bit against the dSim2 oracle.
 * At the full C2 size (2.56M triangles, 1M spins), every step kernel variant
   gives the same positions, phases and collision counts bit for bit, every
   position stays within the clamp, and the counts are nonzero.
@@ -113,3 +115,51 @@ def test_full_size_variants_agree(engine):
         assert np.array_equal(ph.view(np.uint32), ph6.view(np.uint32)), k
         assert np.array_equal(comp, comp6) and np.array_equal(cnt, cnt6), k
     m.set_kernel(6)
+
+
+def test_cylinder_edges(engine, tmp_path):
+    """Cylinders: spins on the grid's cell boundaries, on cylinder surfaces
+    (centre + r (cos, sin), in float) and at the clamp, with permeable
+    myelin; replay parity with the dSim2 oracle."""
+    from dsim_gb300.engine import Cylinders, Spins, cyl_params, cyl_run
+    from scenarios import CylCase
+    from test_gpu_cyl import _oracle, _setup
+    case = CylCase(tmp_path, permeability=0.05, inner=0.7, N=3000)
+    fp, maxR = O.load_fibers2(case.path, case.spaceScale)
+    _, _, n, _, L = O.build_grid2(fp, maxR)
+    rng = np.random.default_rng(8)
+    k = rng.integers(0, n + 1, (1000, 3))
+    on_cells = (F(-1.0) + k.astype(F) * F(L)).astype(F)
+    on_cells = np.clip(on_cells, F(-0.995), F(0.995))
+    f4 = fp.reshape(-1, 4)
+    sel = rng.integers(0, len(f4), 1000)
+    ang = rng.uniform(0, 2 * np.pi, 1000)
+    r = np.sqrt(f4[sel, 3]).astype(F)
+    surf = np.zeros((1000, 3), F)
+    surf[:, 0] = f4[sel, 0] + r * np.cos(ang).astype(F)
+    surf[:, 1] = f4[sel, 1] + r * np.sin(ang).astype(F)
+    surf[:, 2] = rng.uniform(-0.9, 0.9, 1000).astype(F)
+    surf = np.clip(surf, F(-0.995), F(0.995))
+    clamp = rng.uniform(-0.9, 0.9, (1000, 3)).astype(F)
+    for i in range(1000):
+        for a in rng.integers(0, 3, rng.integers(1, 4)):
+            clamp[i, a] = F(0.995) if rng.random() < 0.5 else F(-0.995)
+    case.pos = np.concatenate([on_cells, surf, clamp]).astype(F).reshape(-1)
+    case.N = 3000
+    fp, maxR, cc, cubes, n, maxfpc, L, near, imo = _setup(case)
+    iters = 60
+    d = draws(iters, case.N, seed=23)
+    rpos, rpar, rcnt = _oracle(case, fp, cc, cubes, n, maxfpc, L, iters, d, near, imo)
+    c = Cylinders.load(case.path, case.spaceScale)
+    s = Spins(case.N)
+    s.set_cyl(case.pos, None, None, imo, near)
+    p = cyl_params(case.D, case.D, 0.1 * case.D, case.spaceScale, 70.0, 8.0, 80.0, case.permeability,
+                   case.inner, case.dt, case.pc)
+    cyl_run(c, s, p, g=case.g, iterations=iters, draws=d, count=True)
+    pos, mag, ph, gimo, gnear = s.get_cyl()
+    assert s.status() == 0
+    assert s.counts().sum() > 0
+    assert np.array_equal(s.counts(), rcnt)
+    assert np.array_equal(pos.reshape(-1, 3).view(np.uint32), rpos[:, :3].view(np.uint32))
+    assert np.array_equal(ph.view(np.uint32), rpar[:, 1].view(np.uint32))
+    assert np.array_equal(gimo, rpar[:, 3].astype(np.uint32))
