@@ -27,6 +27,7 @@ namespace dsim {
 
 static constexpr float kLatticeH = 0.0625f;
 static constexpr float kLocalEpsST = 1e-5f;
+static constexpr uint32_t kLocalRefine = 0x100u;  // hit type flag: point from FP32, refine if chosen
 
 // per-warp table of the local form: each owner's lattice origin and the queue
 // of records past the plane test
@@ -96,22 +97,12 @@ __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWa
         if (!((s >= -kLocalEpsST) & (tt >= -kLocalEpsST) & (s + tt <= 1.0f + kLocalEpsST))) return false;
         near = (s <= kLocalEpsST) | (tt <= kLocalEpsST) | (s + tt >= 1.0f - kLocalEpsST);
         if (!near) {
-            // The hit point in FP64 from the same FP32 operands, rounded once
-            // to the local frame: the float nearest the exact crossing.  In
-            // FP32 the point o + d r would carry an error comparable to the
-            // local coordinates' finer ulp, so a spin leaving a hit could
-            // start off a plane it lies on (an axis-aligned plane, or a
-            // coincident membrane) and meet that plane again at r ~ 1e-7.
-            const double n64 = (double)q.x * ((double)ax - (double)ox) + (double)q.y * ((double)ay - (double)oy) +
-                               (double)q.z * ((double)az - (double)oz);
-            const double d64 = (double)q.x * dx + (double)q.y * dy + (double)q.z * dz;
-            const double r64 = n64 / d64;
+            // FP32 point for choosing the nearest hit; the chosen one gets its
+            // point again from FP64 (local_refine)
             h.t = t;
-            h.x = (float)((double)ox + (double)dx * r64);
-            h.y = (float)((double)oy + (double)dy * r64);
-            h.z = (float)((double)oz + (double)dz * r64);
+            h.x = ox + dx * r; h.y = oy + dy * r; h.z = oz + dz * r;
             h.d2 = (ox - h.x) * (ox - h.x) + (oy - h.y) * (oy - h.y) + (oz - h.z) * (oz - h.z);
-            h.type = 1;
+            h.type = 1u | kLocalRefine;
             return true;
         }
     }
@@ -128,6 +119,27 @@ __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWa
     h.d2 = (float)d2;
     h.type = type;
     return true;
+}
+
+// The chosen hit's point in FP64 from the same FP32 operands, rounded once to
+// the local frame: the float nearest the exact crossing.  In FP32 the point o
+// + d r would carry an error comparable to the local coordinates' finer ulp,
+// so a spin leaving a hit could start off a plane it lies on (an axis-aligned
+// plane, or a coincident membrane) and meet that plane again at r ~ 1e-7.
+// Hits decided in FP64 carry their point already (no kLocalRefine).
+__device__ __forceinline__ void local_refine(const MeshDev& g, float gx, float gy, float gz, float ox, float oy,
+                                             float oz, float dx, float dy, float dz, FastHit& h) {
+    if (!(h.type & kLocalRefine)) return;
+    h.type &= ~kLocalRefine;
+    const float4* pp = reinterpret_cast<const float4*>(g.plane + h.t);
+    const float4 a = __ldg(pp), c = __ldg(pp + 1);  // {n, p1.x}, {p1.y, p1.z, vv, info}
+    const double n64 = (double)a.x * ((double)(a.w - gx) - (double)ox) + (double)a.y * ((double)(c.x - gy) - (double)oy) +
+                       (double)a.z * ((double)(c.y - gz) - (double)oz);
+    const double d64 = (double)a.x * dx + (double)a.y * dy + (double)a.z * dz;
+    const double r64 = n64 / d64;
+    h.x = (float)((double)ox + (double)dx * r64);
+    h.y = (float)((double)oy + (double)dy * r64);
+    h.z = (float)((double)oz + (double)dz * r64);
 }
 
 // record k of the fine grid
@@ -308,6 +320,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
             } while ((cy != ty + iy) && !found);
             cx += ix;
         } while ((cx != tx + ix) && !found);
+        if (found) local_refine(g, gx, gy, gz, ox, oy, oz, dx, dy, dz, best);
         return;
     }
     if (n == 0) return;
@@ -343,6 +356,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
     if (found) {
         best.t = H.t[bq][lane]; best.type = H.type[bq][lane]; best.d2 = H.d2[bq][lane];
         best.x = H.x[bq][lane]; best.y = H.y[bq][lane]; best.z = H.z[bq][lane];
+        local_refine(g, gx, gy, gz, ox, oy, oz, dx, dy, dz, best);
     }
 }
 
