@@ -33,7 +33,8 @@ static constexpr uint32_t kLocalRefine = 0x100u;  // hit type flag: point from F
 // of records past the plane test
 struct LocalWarp {
     float gx[32], gy[32], gz[32];
-    uint32_t qe[kPrecQueue], qo[kPrecQueue];
+    uint32_t qe[kPrecQueue], qo[kPrecQueue];  // records past the plane test
+    uint32_t ft[kPrecQueue], fo[kPrecQueue];  // (triangle, owner) pairs for the FP64 re-test
 };
 
 // FP32 plane {n, n.p1}, first vertex and triangle of fine-grid record k
@@ -65,10 +66,33 @@ __device__ __forceinline__ bool local_plane(const FlatWarp& H, const LocalWarp& 
                               ((den == 0.0f) & (fabsf(na) < kPlaneMargin));
 }
 
+// the FP64 re-test of triangle t for owner o from the exact position origin +
+// offset; a hit point is local to o's origin
+__device__ __forceinline__ bool local_fp64(const FlatWarp& H, const LocalWarp& Lw, const MeshDev& g, uint32_t t,
+                                           uint32_t o, FastHit& h, PrecCount& pc) {
+    pc.exact++;
+    const float gx = Lw.gx[o], gy = Lw.gy[o], gz = Lw.gz[o];
+    const float dx = H.dx[o], dy = H.dy[o], dz = H.dz[o];
+    const double Ox = (double)gx + (double)H.ox[o], Oy = (double)gy + (double)H.oy[o], Oz = (double)gz + (double)H.oz[o];
+    double r64;
+    uint32_t type;
+    if (!tri_test64(g.tri64, t, Ox, Oy, Oz, (double)dx, (double)dy, (double)dz, r64, type)) return false;
+    double hx, hy, hz;
+    const double d2 = hit_point64(Ox, Oy, Oz, (double)dx, (double)dy, (double)dz, r64, hx, hy, hz);
+    h.t = t;
+    h.x = (float)(hx - (double)gx); h.y = (float)(hy - (double)gy); h.z = (float)(hz - (double)gz);
+    h.d2 = (float)d2;
+    h.type = type;
+    return true;
+}
+
 // the exact test of triangle t (unit normal q.xyz, first vertex p1) for owner
-// o in o's local frame; a hit point is local to o's origin
+// o in o's local frame; a hit point is local to o's origin.  A case near a
+// decision boundary is decided by local_fp64 here, or (defer) left to the
+// caller with `deferred` set.
 __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWarp& Lw, const MeshDev& g, float4 q,
-                                                float3 p1, uint32_t t, uint32_t o, FastHit& h, PrecCount& pc) {
+                                                float3 p1, uint32_t t, uint32_t o, FastHit& h, PrecCount& pc,
+                                                bool defer, bool& deferred) {
     const float gx = Lw.gx[o], gy = Lw.gy[o], gz = Lw.gz[o];
     const float ox = H.ox[o], oy = H.oy[o], oz = H.oz[o], dx = H.dx[o], dy = H.dy[o], dz = H.dz[o];
     const float ax = p1.x - gx, ay = p1.y - gy, az = p1.z - gz;
@@ -107,18 +131,11 @@ __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWa
         }
     }
     // near a decision boundary: FP64 on the exact position
-    pc.exact++;
-    const double Ox = (double)gx + (double)ox, Oy = (double)gy + (double)oy, Oz = (double)gz + (double)oz;
-    double r64;
-    uint32_t type;
-    if (!tri_test64(g.tri64, t, Ox, Oy, Oz, (double)dx, (double)dy, (double)dz, r64, type)) return false;
-    double hx, hy, hz;
-    const double d2 = hit_point64(Ox, Oy, Oz, (double)dx, (double)dy, (double)dz, r64, hx, hy, hz);
-    h.t = t;
-    h.x = (float)(hx - (double)gx); h.y = (float)(hy - (double)gy); h.z = (float)(hz - (double)gz);
-    h.d2 = (float)d2;
-    h.type = type;
-    return true;
+    if (defer) {
+        deferred = true;
+        return false;
+    }
+    return local_fp64(H, Lw, g, t, o, h, pc);
 }
 
 // The chosen hit's point in FP64 from the same FP32 operands, rounded once to
@@ -150,7 +167,23 @@ __device__ __forceinline__ bool local_test(const FlatWarp& H, const LocalWarp& L
     float3 p1;
     uint32_t t;
     record_load(acc, k, full, q, p1, t);
-    return local_test_core(H, Lw, g, q, p1, t, o, h, pc);
+    bool deferred = false;
+    return local_test_core(H, Lw, g, q, p1, t, o, h, pc, false, deferred);
+}
+
+// the same, leaving a near case to the FP64 queue: returns its triangle in
+// *tdef (else 0xFFFFFFFF)
+__device__ __forceinline__ bool local_test_defer(const FlatWarp& H, const LocalWarp& Lw, const MeshDev& g,
+                                                 const AccelDev& acc, uint32_t k, bool full, uint32_t o, FastHit& h,
+                                                 PrecCount& pc, uint32_t& tdef) {
+    float4 q;
+    float3 p1;
+    uint32_t t;
+    record_load(acc, k, full, q, p1, t);
+    bool deferred = false;
+    const bool hit = local_test_core(H, Lw, g, q, p1, t, o, h, pc, true, deferred);
+    tdef = deferred ? t : 0xFFFFFFFFu;
+    return hit;
 }
 
 // triangle t from its per-triangle records
@@ -158,14 +191,39 @@ __device__ __forceinline__ bool local_test_tri(const FlatWarp& H, const LocalWar
                                                uint32_t t, uint32_t o, FastHit& h, PrecCount& pc) {
     const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
     const float4 a = __ldg(pp), c = __ldg(pp + 1);  // {n, p1.x}, {p1.y, p1.z, vv, info}
-    return local_test_core(H, Lw, g, make_float4(a.x, a.y, a.z, 0.0f), make_float3(a.w, c.x, c.y), t, o, h, pc);
+    bool deferred = false;
+    return local_test_core(H, Lw, g, make_float4(a.x, a.y, a.z, 0.0f), make_float3(a.w, c.x, c.y), t, o, h, pc, false,
+                           deferred);
+}
+
+// appends the lanes' deferred (t, o) to the FP64 queue (fn: warp-uniform
+// length) and re-tests full groups of 32 in FP64; all lanes call it
+__device__ __forceinline__ void local_enqueue64(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, uint32_t lane,
+                                                uint32_t t, uint32_t o, uint32_t& fn, PrecCount& pc) {
+    const bool live = t != 0xFFFFFFFFu;
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
+    if (live) {
+        const uint32_t at = fn + __popc(b & ((1u << lane) - 1u));
+        Lw.ft[at] = t; Lw.fo[at] = o;
+    }
+    fn += __popc(b);
+    __syncwarp();
+    while (fn >= 32) {
+        const uint32_t at = fn - 32 + lane;
+        const uint32_t tq = Lw.ft[at], oq = Lw.fo[at];
+        __syncwarp();
+        fn -= 32;
+        FastHit h;
+        if (local_fp64(H, Lw, g, tq, oq, h, pc)) flat_file_hit(H, oq, h);
+    }
 }
 
 // appends the lanes' surviving (k, o) to the warp's queue (qn: warp-uniform
-// length) and tests full groups of 32 from its top; all lanes call it
+// length) and tests full groups of 32 from its top, their near cases going to
+// the FP64 queue; all lanes call it
 __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, const AccelDev& acc,
                                               bool full, uint32_t lane, bool live, uint32_t k, uint32_t o,
-                                              uint32_t& qn, PrecCount& pc) {
+                                              uint32_t& qn, uint32_t& fn, PrecCount& pc) {
     const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
     if (live) {
         const uint32_t at = qn + __popc(b & ((1u << lane) - 1u));
@@ -179,7 +237,9 @@ __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const 
         __syncwarp();
         qn -= 32;
         FastHit h;
-        if (local_test(H, Lw, g, acc, kq, full, oq, h, pc)) flat_file_hit(H, oq, h);
+        uint32_t tdef;
+        if (local_test_defer(H, Lw, g, acc, kq, full, oq, h, pc, tdef)) flat_file_hit(H, oq, h);
+        local_enqueue64(H, Lw, g, lane, tdef, oq, fn, pc);
     }
 }
 
@@ -221,7 +281,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
     const uint32_t iincl = warp_incl_scan(ncw, lane);
     const uint32_t iexcl = iincl - ncw;
     const uint32_t itotal = __shfl_sync(FULL, iincl, 31);
-    uint32_t qn = 0;
+    uint32_t qn = 0, fn = 0;  // queue lengths (warp-uniform)
     __syncwarp();
     for (uint32_t ib = 0; ib < itotal; ib += 32) {
         const uint32_t m = ib + lane;
@@ -261,13 +321,18 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
                 pc.records++;
                 s1 = t != H.excl[o1] && local_plane(H, Lw, q, o1);
             }
-            local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, qn, pc);
-            local_enqueue(H, Lw, g, acc, full, lane, s1, e1, o1, qn, pc);
+            local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, qn, fn, pc);
+            local_enqueue(H, Lw, g, acc, full, lane, s1, e1, o1, qn, fn, pc);
         }
     }
-    if (lane < qn) {
+    {
+        // the record queue's remainder, then the FP64 queue's
         FastHit h;
-        if (local_test(H, Lw, g, acc, Lw.qe[lane], full, Lw.qo[lane], h, pc)) flat_file_hit(H, Lw.qo[lane], h);
+        uint32_t tdef = 0xFFFFFFFFu;
+        const uint32_t oq = Lw.qo[lane];
+        if (lane < qn && local_test_defer(H, Lw, g, acc, Lw.qe[lane], full, oq, h, pc, tdef)) flat_file_hit(H, oq, h);
+        local_enqueue64(H, Lw, g, lane, (lane < qn) ? tdef : 0xFFFFFFFFu, oq, fn, pc);
+        if (lane < fn && local_fp64(H, Lw, g, Lw.ft[lane], Lw.fo[lane], h, pc)) flat_file_hit(H, Lw.fo[lane], h);
     }
     if (solo) {
         for (uint32_t q = 0; q < nc; q++) {
