@@ -471,11 +471,12 @@ def run_reference(args, rank, world):
 # --------------------------------------------------------------------------
 # batched and served forms on a seeded job mix
 # --------------------------------------------------------------------------
-def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False):
+def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False, subs=None):
     from dsim_gb300 import jobs as JB
     t0 = time.time()
-    subs = [JB.mesh_substrate(W.axons, 1, mesh=m, tube=W.tube), JB.mesh_substrate(100, 7),
-            JB.cyl_substrate(64, 1), JB.cyl_substrate(256, 2)]
+    if subs is None:
+        subs = [JB.mesh_substrate(W.axons, 1, mesh=m, tube=W.tube), JB.mesh_substrate(100, 7),
+                JB.cyl_substrate(64, 1), JB.cyl_substrate(256, 2)]
     rng = np.random.default_rng(seed)
     mix = [JB.make_job(rng, subs, spins_range=spins_range, steps_range=steps_range, permeable=permeable,
                        seed=1000 + k) for k in range(n_jobs)]
@@ -615,10 +616,20 @@ def run_forms(args, W, m):
                     "autotuned": best, "kernel_launches": info["launches"], "graph_launches": info["graph_launches"],
                     "status": st},
     }
-    cap_jobs = n_jobs / plain_s
-    out["served"] = [run_served_mix(subs, mix, cfg, r * cap_jobs) for r in args.serve_rates]
-    for o, r in zip(out["served"], args.serve_rates):
-        o["rate_x_plain_capacity"] = r
+    # serving: the same substrates and ranges with permeable membranes (per-hit
+    # permeation log-uniform 1e-4 - 1e-2); arrival rates relative to the plain
+    # form's capacity on that mix
+    out["served"] = []
+    if args.serve_rates:
+        _, pmix = build_mix(W, m, n_jobs, 12, spins_range, steps_range, permeable=True, subs=subs)
+        pplain_s = sum(run_plain_mix(pmix))
+        cap_jobs = n_jobs / pplain_s
+        out["served_mix"] = {"jobs": n_jobs, "seed": 12, "permeability": "log-uniform 1e-4 - 1e-2 per hit",
+                             "plain_spin_steps_per_s": sum(j["n"] * j["steps"] for j in pmix) / pplain_s,
+                             "plain_jobs_per_s": cap_jobs}
+        out["served"] = [run_served_mix(subs, pmix, cfg, r * cap_jobs) for r in args.serve_rates]
+        for o, r in zip(out["served"], args.serve_rates):
+            o["rate_x_plain_capacity"] = r
     return out
 
 
