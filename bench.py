@@ -440,6 +440,8 @@ def run_ours(args, rank, world):
         res["forms"] = run_forms(args, W, m)
     if rank == 0 and not args.no_precision:
         res["precision"] = run_precision(args, W, m)
+    if rank == 0 and args.c5_full:
+        res["precision_full"] = run_precision_full(args, W, m)
     if rank == 0 and not args.no_cylinders:
         res["cylinders"] = run_cylinders(args)
     if rank == 0 and not args.no_cpu:
@@ -869,6 +871,50 @@ def run_precision(args, W, m):
             "gpu_s": gpu_s, "oracle_s": oracle_s, "oracle": "FP64 restatement of the reference step (oracle), same draws"}
 
 
+def run_precision_full(args, W, m):
+    """C5 at full size: every spin of the workload, 20,000 steps at dt 2 us,
+    PGSE and OGSE 50 / 200 Hz, in the three forms.  The FP64 form (bit-exact
+    with the FP64 oracle on samples) is the reference; per-gradient |dS| of
+    the cell-local and plain forms against it over 32 directions x b."""
+    from dsim_gb300.engine import Batch, grad_scaled, phase_constant, std_devs
+    from dsim_gb300.jobs import fibonacci_dirs, pgse_gmag
+    dt = 0.002
+    steps = args.c5_steps
+    waves, delta, Delta, freqs = c5_waves(steps, dt)
+    waves = waves[[0, 1, len(waves) - 1]]  # PGSE, OGSE 50 Hz, OGSE 200 Hz
+    sd = std_devs(W.D, W.D, 0.1 * W.D, W.spaceScale, dt)
+    pc = phase_constant(42576.0, dt)
+    dirs = fibonacci_dirs(32)
+    bvals = [1.0, 3.0, 5.0, 10.0]
+    gs = np.concatenate([grad_scaled(min(pgse_gmag(bv, delta, Delta), 300.0) * dirs, W.spaceScale)
+                         for bv in bvals]).astype(F)
+    out = {"workload": "%d spins x %d steps at dt 2 us, waveforms PGSE and OGSE 50 / 200 Hz, 32 directions x b %s "
+                       "ms/um2 (|G| <= 300 mT/m)" % (W.N, steps, bvals)}
+    sig = {}
+    for form in ("precise", "local", "plain"):
+        b = Batch(len(waves) * (W.N + 32), len(waves))
+        sid = b.add_mesh(m)
+        t0 = time.time()
+        ids = [b.submit(sid, W.pos, W.comp, W.fiber.astype(np.uint32), steps, dt, sd, W.T2, pc, 77,
+                        waveform="table", table=w, precise=(form == "precise"), local=(form == "local"))
+               for w in waves]
+        b.run()
+        b.sync()
+        el = time.time() - t0
+        assert b.status() in (0, 1)
+        sig[form] = np.stack([b.signal(j, gs) for j in ids])  # [wave][grad][5][3]
+        out["spin_steps_per_s_" + form] = len(waves) * W.N * steps / el
+        out["status_" + form] = int(b.status())
+        b.close()
+    S = {k: np.hypot(v[:, :, 0, 0], v[:, :, 0, 1]) / v[:, :, 0, 2] for k, v in sig.items()}
+    for form in ("local", "plain"):
+        d = np.abs(S[form] - S["precise"])
+        out["max_abs_dS_" + form] = float(d.max())
+        out["median_abs_dS_" + form] = float(np.median(d))
+    out["reference"] = "the FP64 form (DSIM_JOB_PRECISE), bit-exact with the FP64 oracle on samples"
+    return out
+
+
 # --------------------------------------------------------------------------
 def barrier(world):
     if world > 1:
@@ -917,6 +963,8 @@ def main():
     ap.add_argument("--c5-steps", type=int, default=20000)
     ap.add_argument("--c5-sample", type=int, default=512)
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
+    ap.add_argument("--c5-full", action="store_true",
+                    help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
