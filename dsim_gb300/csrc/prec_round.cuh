@@ -31,7 +31,8 @@ struct PrecCount {
 static constexpr uint32_t kPrecQueue = 64;  // at most 31 left over + 32 appended
 struct PrecWarp {
     double ox[32], oy[32], oz[32], dx[32], dy[32], dz[32];
-    uint32_t qt[kPrecQueue], qo[kPrecQueue];
+    uint32_t qt[kPrecQueue], qo[kPrecQueue];  // past the plane pruning
+    uint32_t ft[kPrecQueue], fo[kPrecQueue];  // past the barycentric pre-test: to the FP64 test
 };
 
 // May the plane (n, w = n.p1) meet the sub-segment o -> o + d?  The FP32
@@ -157,10 +158,61 @@ __device__ __forceinline__ void prec_test(FlatWarp& H, const PrecWarp& P, const 
         prec_file_hit(H, o, t, type, r);
 }
 
+// FP32 barycentric pre-test: false only when the crossing of t's plane lies
+// clearly outside the triangle, so the FP64 test would reject it too.  The
+// FP32 crossing w = o + r d - p1 (from float positions and helpers) is within
+// a few 1e-7 of the FP64 one, i.e. within 2e-4 in barycentric units for edges
+// of 1e-3 or more; with the angle at p1 of about 25 degrees or more and an edge
+// ratio of at most 10 the Gram system amplifies that by at most ~25, far below
+// the margin of 0.05.  Other triangles (and a segment parallel to the plane
+// in FP32) always go to the FP64 test.
+static constexpr float kPreST = 0.05f;
+__device__ __forceinline__ bool prec_pretest(const FlatWarp& H, const MeshDev& g, uint32_t t, uint32_t o) {
+    const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
+    const float4 a = __ldg(pp), c = __ldg(pp + 1);  // {n, p1.x}, {p1.y, p1.z, vv, info}
+    const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
+    const float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);  // {u, v.x}, {v.y, v.z, uv, uu}
+    const float uv = v4.z, uu = v4.w, vv = c.z;
+    const float mn = fminf(uu, vv), mx = fmaxf(uu, vv);
+    if (!((uv * uv <= 0.82f * uu * vv) & (mx <= 100.0f * mn) & (mn >= 1e-6f))) return true;
+    const float ox = H.ox[o], oy = H.oy[o], oz = H.oz[o], dx = H.dx[o], dy = H.dy[o], dz = H.dz[o];
+    const float den = a.x * dx + a.y * dy + a.z * dz;
+    if (den == 0.0f) return true;
+    const float r = (a.x * (a.w - ox) + a.y * (c.x - oy) + a.z * (c.y - oz)) / den;
+    const float wx = ox + r * dx - a.w, wy = oy + r * dy - c.x, wz = oz + r * dz - c.y;
+    const float wu = wx * u4.x + wy * u4.y + wz * u4.z;
+    const float wv = wx * u4.w + wy * v4.x + wz * v4.y;
+    const float D = uv * uv - uu * vv;
+    const float s = (uv * wv - vv * wu) / D, tt = (uv * wu - uu * wv) / D;
+    return (s >= -kPreST) & (tt >= -kPreST) & (s + tt <= 1.0f + kPreST);
+}
+
+// appends the lanes' (t, o) to the FP64 queue (fn: warp-uniform length) and
+// tests full groups of 32 in FP64; all lanes call it
+__device__ __forceinline__ void prec_enqueue64(FlatWarp& H, PrecWarp& P, const MeshDev& g, uint32_t lane,
+                                               uint32_t t, uint32_t o, uint32_t& fn, PrecCount& pc) {
+    const bool live = t != 0xFFFFFFFFu;
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
+    if (live) {
+        const uint32_t at = fn + __popc(b & ((1u << lane) - 1u));
+        P.ft[at] = t; P.fo[at] = o;
+    }
+    fn += __popc(b);
+    __syncwarp();
+    while (fn >= 32) {
+        const uint32_t at = fn - 32 + lane;
+        const uint32_t tq = P.ft[at], oq = P.fo[at];
+        __syncwarp();
+        fn -= 32;
+        prec_test(H, P, g, tq, oq, pc);
+    }
+}
+
 // appends the lanes' surviving (t, o) to the warp's queue (qn: warp-uniform
-// length) and tests full groups of 32 from its top; all lanes call it
+// length) and pre-tests full groups of 32 from its top, passing the
+// survivors to the FP64 queue; all lanes call it
 __device__ __forceinline__ void prec_enqueue(FlatWarp& H, PrecWarp& P, const MeshDev& g, uint32_t lane,
-                                             uint32_t t, uint32_t o, uint32_t& qn, PrecCount& pc) {
+                                             uint32_t t, uint32_t o, uint32_t& qn, uint32_t& fn, PrecCount& pc) {
     const uint32_t FULL = 0xFFFFFFFFu;
     const bool live = t != 0xFFFFFFFFu;
     const uint32_t b = __ballot_sync(FULL, live);
@@ -175,7 +227,7 @@ __device__ __forceinline__ void prec_enqueue(FlatWarp& H, PrecWarp& P, const Mes
         const uint32_t tq = P.qt[at], oq = P.qo[at];
         __syncwarp();
         qn -= 32;
-        prec_test(H, P, g, tq, oq, pc);
+        prec_enqueue64(H, P, g, lane, prec_pretest(H, g, tq, oq) ? tq : 0xFFFFFFFFu, oq, fn, pc);
     }
 }
 
@@ -261,7 +313,7 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
     const uint32_t iincl = warp_incl_scan(ncw, lane);
     const uint32_t iexcl = iincl - ncw;
     const uint32_t itotal = __shfl_sync(FULL, iincl, 31);
-    uint32_t qn = 0;  // queue length (warp-uniform)
+    uint32_t qn = 0, fn = 0;  // queue lengths (warp-uniform)
     __syncwarp();
     for (uint32_t ib = 0; ib < itotal; ib += 32) {
         const uint32_t m = ib + lane;
@@ -290,12 +342,17 @@ __device__ __forceinline__ void prec_round(FlatWarp& H, PrecWarp& P, const MeshD
             const uint32_t o1 = __shfl_sync(FULL, ow, j1);
             const uint32_t t0 = (r0 < rtotal) ? prec_prune(H, acc, e0, full, o0, pc) : 0xFFFFFFFFu;
             const uint32_t t1 = (r1 < rtotal) ? prec_prune(H, acc, e1, full, o1, pc) : 0xFFFFFFFFu;
-            prec_enqueue(H, P, g, lane, t0, o0, qn, pc);
-            prec_enqueue(H, P, g, lane, t1, o1, qn, pc);
+            prec_enqueue(H, P, g, lane, t0, o0, qn, fn, pc);
+            prec_enqueue(H, P, g, lane, t1, o1, qn, fn, pc);
         }
     }
-    // the queue's remainder (fewer than 32)
-    if (lane < qn) prec_test(H, P, g, P.qt[lane], P.qo[lane], pc);
+    // the queues' remainders (fewer than 32 each)
+    {
+        const uint32_t tq = P.qt[lane], oq = P.qo[lane];
+        const bool pass = lane < qn && prec_pretest(H, g, tq, oq);
+        prec_enqueue64(H, P, g, lane, pass ? tq : 0xFFFFFFFFu, oq, fn, pc);
+        if (lane < fn) prec_test(H, P, g, P.ft[lane], P.fo[lane], pc);
+    }
     if (solo) {
         for (uint32_t q = 0; q < nc; q++) {
             const uint32_t iz = q % w2, r = q / w2, iy = r % w1, ix = r / w1;
