@@ -67,7 +67,8 @@ struct dsim_mesh {
     uint4* tri_cells = nullptr;  // each triangle's reference cells (up to 4)
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
-    uint32_t kernel = 6;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened (8, 6, 4)
+    uint32_t kernel = 8;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened
+                          // (8, 6, 4), 8 flattened with queued plane survivors, 9 with staged records
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
     AccelRec* acc_rec = nullptr;
@@ -199,7 +200,7 @@ struct dsim_spins {
     uint32_t *meta2 = nullptr, *id2 = nullptr, *keys = nullptr, *hist = nullptr, *hstart = nullptr,
              *hscratch = nullptr;
     uint32_t sortNb = 0;        // key grid of the allocated sort buffers
-    uint32_t sortEvery = 20;    // steps between reorderings (0 = never)
+    uint32_t sortEvery = 1000;  // steps between reorderings (0 = never): once per call of up to 1000 steps
     uint64_t launches = 0;      // kernels launched by dsim_mesh_run / dsim_cyl_run on this object
     uint32_t spinBase = 0;      // global index of spin 0 in the Philox counter (replica shards)
     bool permuted = false;      // slot i does not hold spin i

@@ -1428,7 +1428,7 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
     // fine-grid resolutions: cells per reference-cell edge x 2
     const uint32_t gridHalves[] = {2, 3, 4, 5};  // 1, 1.5, 2, 2.5 fine cells per reference cell
     const uint32_t occs[] = {4, 6, 8};
-    const uint32_t chunks[] = {10, 20, 40};
+    const uint32_t chunks[] = {20, 40, 100, 200};
     bool haveMesh = false;
     for (auto* m : b->meshes) haveMesh |= (m != nullptr);
     cudaEvent_t e0, e1;

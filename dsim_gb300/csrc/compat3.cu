@@ -83,7 +83,7 @@ struct State {
     uint32_t* keys = nullptr;
     uint32_t *hist = nullptr, *hstart = nullptr, *hscratch = nullptr;
     uint32_t histNf = 0;
-    uint32_t sortEvery = 20;
+    uint32_t sortEvery = 1000;  // reorder by fine cell once per call of up to 1000 steps
     void release() {
         cudaFree(plane); cudaFree(bary); cudaFree(cell_start); cudaFree(cell_tri);
         cudaFree(acc_start); cudaFree(acc_recw);
@@ -355,7 +355,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, dsim_spinData* spinInfo
         b.iterations = n;
         b.step0 = done;
         b.draws = s.replay ? s.replay + (size_t)done * N : nullptr;
-        if ((rc = launch_mesh_step_flat(g, acc, b, s.set(cur, N), rng, 0, 6))) { fail(rc); return; }
+        if ((rc = launch_mesh_step_flat(g, acc, b, s.set(cur, N), rng, 0, 6, true))) { fail(rc); return; }
     }
     rc = launch_soa_to_aos(s.set(cur, N), pos, spinInfo, s.replay ? nullptr : randSeed, iterations, 0);
     if (rc) fail(rc);

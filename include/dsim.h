@@ -69,7 +69,7 @@ int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
  * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
  * info = {cells per axis, entries, device bytes}. */
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
-/* step kernel on the fine grid (all give the same results; default 6): 1 one thread per
+/* step kernel on the fine grid (all give the same results; default 8): 1 one thread per
  * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
  * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM; 5, 6, 7 the
  * warp's candidate records flattened into one list, lanes stepping
@@ -132,8 +132,10 @@ int dsim_spins_counts(dsim_spins* s, uint32_t* counts2N, int reset);
 int dsim_spins_scanned(dsim_spins* s, uint32_t* scannedN, int reset);
 int dsim_spins_status(dsim_spins* s, uint32_t* status, int reset);
 /* Spins are reordered by fine-grid cell every `steps` steps of a mesh run
- * (default 20; 0 = never) so that neighbouring threads read the same cell
- * records.  Each spin keeps its identity (random stream, counters, getters). */
+ * (default 1000, i.e. once at the start of a call of up to 1000 steps; 0 =
+ * never) so that neighbouring threads read the same cell records; one step
+ * kernel launch covers the steps between reorderings.  Each spin keeps its
+ * identity (random stream, counters, getters). */
 int dsim_spins_set_sort_interval(dsim_spins* s, uint32_t steps);
 /* Global index of this object's spin 0 in the Philox counter (default 0).
  * A job split over several GPUs gives each shard the index of its first spin,

@@ -121,7 +121,7 @@ int dsim_batch_retire(dsim_batch* b, uint32_t jobId);
 int dsim_batch_compact(dsim_batch* b);
 /* Autotuner: runs trialSteps steps of the current jobs from a snapshot of the
  * spin state for every candidate -- step-kernel occupancy {4, 6, 8} x chunk
- * {10, 20, 40} x fine-grid cells per reference-cell edge {1, 1.5, 2, 2.5}
+ * {20, 40, 100, 200} x fine-grid cells per reference-cell edge {1, 1.5, 2, 2.5}
  * (every mesh substrate's fine grid is rebuilt; meshes must not be in use
  * elsewhere meanwhile) -- restores the snapshot and keeps the fastest.
  * best = {occupancy, chunk, 2 x fine cells per reference cell edge (0: no
