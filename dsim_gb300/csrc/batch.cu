@@ -81,22 +81,23 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 
 // The plain form has one instantiation per fine-grid record layout (LAYOUT 1:
 // 32-byte, 2: 64-byte records), each advancing only the mesh jobs whose
-// substrate uses it, so no kernel carries the registers of a record path it
-// does not run; cylinder jobs run in the one launch given cylHere.
-// Precision-form jobs run in k_batch_step64.
+// substrate uses it, and one for cylinder jobs (LAYOUT 3), so no kernel
+// carries the registers of a path it does not run.  Precision-form and
+// cell-local jobs run in k_batch_step64 and k_batch_step_local.
 template <int MINB, int LAYOUT>
 __global__ void __launch_bounds__(kFlatThreads, MINB)
 k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
              const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
-             unsigned long long* jobCounts, uint32_t cylHere) {
-    __shared__ FlatWarp wh[kFlatWarps];
+             unsigned long long* jobCounts) {
+    constexpr int MESH = LAYOUT == 3 ? 1 : LAYOUT;  // the record path of the mesh instantiations
+    __shared__ FlatWarp wh[LAYOUT == 3 ? 1 : kFlatWarps];
     // gradient moments and their compensation live in shared memory (touched
     // once per step), which keeps the collision loop's registers free
     __shared__ float mom[6][kFlatThreads];
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t tx = threadIdx.x;
-    FlatWarp& H = wh[threadIdx.x >> 5];
+    FlatWarp& H = wh[LAYOUT == 3 ? 0u : (threadIdx.x >> 5)];  // the cylinder path uses no table
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
     const uint32_t jb = S.u[U_JOB][i & ~31u];
@@ -117,7 +118,8 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     }
     const JobDev& J = jobS[wi];
     if (J.flags & (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL)) return;  // warp-uniform
-    if (subS[wi].kind == kSubMesh ? subS[wi].acc.wide != (uint32_t)LAYOUT : !cylHere) return;
+    if (LAYOUT == 3 ? subS[wi].kind != kSubCyl
+                    : (subS[wi].kind != kSubMesh || subS[wi].acc.wide != (uint32_t)LAYOUT)) return;
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;  // not started or finished (warp-uniform)
@@ -135,7 +137,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     const float* __restrict__ wave = J.wave;
     uint32_t nrefl = 0, nperm = 0, st = 0;
     const SubDev& sub = subS[wi];
-    if (sub.kind == kSubMesh) {
+    if (LAYOUT != 3) {
         const MeshDev& g = sub.g;
         const AccelDev& acc = sub.acc;
         const float perm = J.perm;
@@ -162,7 +164,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
             const bool open = active;
             bool found;
             FastHit best;
-            flat_round_mode<LAYOUT>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
+            flat_round_mode<MESH>(H, g, acc, lane, open, ox, oy, oz, px, py, pz, excluded, found, best);
             if (open) {
                 bool finish = !found;
                 if (found) {
@@ -786,17 +788,14 @@ int upload_jobs(dsim_batch* b) {
 }
 
 // which plain step instantiations a chunk launches: bit 1 / 2 for mesh jobs
-// on 32- / 64-byte fine-grid records, kHasCyl for cylinder jobs (run by the
-// first launched instantiation; LAYOUT 1 when there is no plain mesh job)
-constexpr uint32_t kHasCyl = 1u << 4;
+// on 32- / 64-byte fine-grid records, bit 3 for cylinder jobs
 uint32_t step_layouts(const dsim_batch* b) {
     uint32_t mask = 0;
     for (const auto& j : b->jobs) {
         const SubDev& s = b->subs[j.d.sub];
-        if (s.kind == kSubCyl) mask |= kHasCyl;
+        if (s.kind == kSubCyl) mask |= 1u << 3;
         else if (!j.d.flags) mask |= 1u << (s.acc.wide == 2 ? 2u : 1u);
     }
-    if ((mask & kHasCyl) && !(mask & 6u)) mask |= 1u << 1;
     return mask;
 }
 
@@ -804,21 +803,21 @@ uint32_t step_layouts(const dsim_batch* b) {
 // instantiations, advance
 uint64_t chunk_launches(const dsim_batch* b) {
     const uint32_t mask = step_layouts(b);
-    return 5ull + (uint64_t)__builtin_popcount(mask & 6u) + (b->anyPrecise ? 1ull : 0ull) + (b->anyLocal ? 1ull : 0ull) +
-           1ull;
+    return 5ull + (uint64_t)__builtin_popcount(mask & 0xEu) + (b->anyPrecise ? 1ull : 0ull) +
+           (b->anyLocal ? 1ull : 0ull) + 1ull;
 }
 
 template <int LAYOUT>
-void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D, uint32_t cylHere) {
+void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D) {
     if (b->occupancy >= 8)
         k_batch_step<8, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts, cylHere);
+                                                                 b->d_status, b->d_counts);
     else if (b->occupancy >= 6)
         k_batch_step<6, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts, cylHere);
+                                                                 b->d_status, b->d_counts);
     else
         k_batch_step<4, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts, cylHere);
+                                                                 b->d_status, b->d_counts);
 }
 
 // one chunk: sort into the other buffer, step, advance the step counter
@@ -835,10 +834,9 @@ int enqueue_chunk(dsim_batch* b) {
     b->cur = 1 - b->cur;
     const uint32_t grid = (N + kFlatThreads - 1) / kFlatThreads;
     const uint32_t mask = step_layouts(b);
-    // the first plain launch also runs the cylinder jobs
-    uint32_t cylHere = (mask & kHasCyl) ? 1u : 0u;
-    if (mask & (1u << 1)) { launch_step_layout<1>(b, grid, D, cylHere); cylHere = 0; }
-    if (mask & (1u << 2)) launch_step_layout<2>(b, grid, D, cylHere);
+    if (mask & (1u << 1)) launch_step_layout<1>(b, grid, D);
+    if (mask & (1u << 2)) launch_step_layout<2>(b, grid, D);
+    if (mask & (1u << 3)) launch_step_layout<3>(b, grid, D);
     if (b->anyLocal)
         k_batch_step_local<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
                                                              b->d_status, b->d_counts);
