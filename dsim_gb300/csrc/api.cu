@@ -329,8 +329,8 @@ static int mesh_build(dsim_mesh* m, const std::vector<float>& Vn, const std::vec
     cudaFree(counter);
     cudaFree(scratch);
     if (rc) return rc;
-    // default fine grid: 2.5 fine cells per reference cell edge
-    const uint32_t nf = 5 * m->n / 2;
+    // default fine grid: 2.25 fine cells per reference cell edge (50 -> 112)
+    const uint32_t nf = 9 * m->n / 4;
     return accel_build(m, nf < 1 ? 1 : (nf <= 1024 ? nf : 1024));
 }
 

@@ -149,8 +149,8 @@ int derive(State& s, const uint32_t* tic, const uint32_t* cc) {
         return kErrFormat;
     }
     // fine acceleration grid from the records (triangle corners p1, p1 + v, p1 + u),
-    // 2.5 fine cells per reference cell edge, 32-byte records
-    uint32_t nf = s.numCubes * 5 / 2 <= 1024 ? s.numCubes * 5 / 2 : 1024;
+    // 2.25 fine cells per reference cell edge, 32-byte records
+    uint32_t nf = s.numCubes * 9 / 4 <= 1024 ? s.numCubes * 9 / 4 : 1024;
     if (nf < 1) nf = 1;
     uint32_t nkeys = accel_keys(nf);
     uint32_t* counter = nullptr;

@@ -62,13 +62,13 @@ def test_tiny_and_ragged_spin_counts(engine, tmp_path, N):
 
 def test_spins_on_cell_boundaries(engine, tmp_path):
     """x, y, z exactly on reference-cell boundaries -1 + k (2/50) and on
-    fine-cell boundaries -1 + k (2/125), in float."""
+    fine-cell boundaries -1 + k (2/112), in float."""
     case = MeshCase(tmp_path, membranes="AM", permeability=0.05, N=1500)
     rng = np.random.default_rng(3)
     k = rng.integers(3, 47, (600, 3))
     ref = (F(-1.0) + k.astype(F) * (F(2.0) / F(50))).astype(F)
-    kf = rng.integers(8, 117, (600, 3))
-    fine = (F(-1.0) + kf.astype(F) * (F(2.0) / F(125))).astype(F)
+    kf = rng.integers(8, 105, (600, 3))
+    fine = (F(-1.0) + kf.astype(F) * (F(2.0) / F(112))).astype(F)
     mixed = ref.copy()
     mixed[:, 1] = rng.uniform(-0.9, 0.9, 600).astype(F)   # one coordinate free
     pos = np.concatenate([ref, fine, mixed]).astype(F)
