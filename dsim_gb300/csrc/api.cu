@@ -1,12 +1,15 @@
 // api.cu -- host side of the native engine: substrate loading and grid build,
 // device-resident spin state, launches, and the dsim_* C-ABI (include/dsim.h).
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <cmath>
+#include <limits>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #pragma GCC visibility push(default)
@@ -145,15 +148,28 @@ struct dsim_cyl {
     uint32_t* cc = nullptr;
     uint32_t* cubes = nullptr;
     float4* cubeF = nullptr;  // each grid entry's fiber record
+    uint32_t* fineStart = nullptr;  // fine filter grid (CSR), null when not built
+    float4* fineRec = nullptr;
+    uint32_t* finePos = nullptr;
+    uint32_t fineK = 0;
+    uint64_t fineEntries = 0, fineBytes = 0;
     uint64_t bytes = 0;
     CylDev dev() const {
         CylDev g;
         g.fibers = fibers; g.cube_count = cc; g.cubes = cubes; g.cube_fibers = cubeF;
         g.n = host.numCubes; g.maxFPC = host.maxFPC; g.L = host.cubeLength;
         g.nF = host.nF;
+        g.fine_start = fineK ? fineStart : nullptr; g.fine_rec = fineRec; g.fine_pos = finePos;
+        g.fineK = fineK;
+        g.fineInv = fineK ? (float)fineK / host.cubeLength : 0.0f;
         return g;
     }
 };
+
+// batches holding each cylinder substrate's device view: its fine grid is
+// not rebuilt (freed) while one does
+static std::mutex g_cylHoldMu;
+static std::unordered_map<const dsim_cyl*, int> g_cylHolds;
 
 namespace dsim {
 // device views for the batch module (batch.cu)
@@ -185,6 +201,15 @@ int cyl_view(const dsim_cyl* c, CylDev* g) {
     if (!c || !g) return kErrInvalid;
     *g = c->dev();
     return kOk;
+}
+void cyl_hold(const dsim_cyl* c, int delta) {
+    std::lock_guard<std::mutex> lk(g_cylHoldMu);
+    if (delta > 0) {
+        g_cylHolds[c] += delta;
+    } else {
+        auto it = g_cylHolds.find(c);
+        if (it != g_cylHolds.end() && (it->second += delta) <= 0) g_cylHolds.erase(it);
+    }
 }
 int mesh_rebuild_accel(dsim_mesh* m, uint32_t nf) { return accel_build(m, nf); }
 }  // namespace dsim
@@ -440,10 +465,114 @@ void dsim_mesh_free(dsim_mesh* m) { mesh_release(m); }
 // ---------------------------------------------------------------------------
 // cylinders
 // ---------------------------------------------------------------------------
+static void cyl_fine_release(dsim_cyl* c) {
+    cudaFree(c->fineStart); cudaFree(c->fineRec); cudaFree(c->finePos);
+    c->fineStart = nullptr; c->fineRec = nullptr; c->finePos = nullptr;
+    c->bytes -= c->fineBytes;
+    c->fineK = 0; c->fineEntries = 0; c->fineBytes = 0;
+}
+
+static int cyl_holds(const dsim_cyl* c) {
+    std::lock_guard<std::mutex> lk(g_cylHoldMu);
+    auto it = g_cylHolds.find(c);
+    return it == g_cylHolds.end() ? 0 : it->second;
+}
+
 static void cyl_release(dsim_cyl* c) {
     if (!c) return;
+    {
+        std::lock_guard<std::mutex> lk(g_cylHoldMu);
+        g_cylHolds.erase(c);
+    }
     cudaFree(c->fibers); cudaFree(c->cc); cudaFree(c->cubes); cudaFree(c->cubeF);
+    cyl_fine_release(c);
     delete c;
+}
+
+// Fine filter grid.  A spin outside every fiber tests the entries of its
+// grid cell's list in order, and only an entry whose fiber disk holds the
+// tested point (d^2 <= r^2, or d^2 < inR r^2 with inR <= 1) changes anything.
+// Each grid cell is split k x k x k; a fine cell keeps, in list order and
+// with repeats, the list positions whose disk can reach the cell: in double,
+// d^2 from the axis to the cell's box widened by 1e-5 at most r^2 (1 + 1e-4)
+// (the float distance of a point within the box is far inside that margin),
+// with the boxes of the outermost fine cells reaching to infinity outward
+// (a proposed position can leave the box before the clamp; the grid cell of
+// such a point is the clamped one).  The spin's fine cell is taken inside
+// its grid cell, so the fine list is a subsequence of the list it replaces.
+static uint32_t cyl_fine_default(const CylHost& h) {
+    // fine cells about half the largest radius across, at most 16 per grid
+    // cell edge and 2^22 fine cells in all
+    const uint32_t n = h.numCubes;
+    if (!(h.maxR > 0.0f) || n == 0) return 0;
+    uint32_t k = (uint32_t)std::min(16.0, std::ceil(2.0 * (double)h.cubeLength / (double)h.maxR));
+    while (k >= 2 && (uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 22)) k--;
+    return k >= 2 ? k : 0;
+}
+
+static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
+    cyl_fine_release(c);
+    const CylHost& h = c->host;
+    const uint32_t n = h.numCubes;
+    const double L = (double)h.cubeLength;
+    if (k < 2 || n == 0 || !c->cubeF) return kOk;
+    if ((uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 24)) {
+        set_last_error(kErrTooLarge, "cylinder fine grid: (%u x %u)^3 cells, limit 2^24", n, k);
+        return kErrTooLarge;
+    }
+    const uint32_t nk = n * k;
+    const size_t nfine = (size_t)nk * nk * nk;
+    const double Lf = L / k, eps = 1e-5, inf = std::numeric_limits<double>::infinity();
+    std::vector<uint32_t> start(nfine + 1, 0), pos;
+    std::vector<float> rec;
+    for (size_t fc = 0; fc < nfine; fc++) {
+        const uint32_t gx = (uint32_t)(fc % nk), gy = (uint32_t)((fc / nk) % nk), gz = (uint32_t)(fc / ((size_t)nk * nk));
+        const uint32_t gcoord[3] = {gx, gy, gz};
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+            lo[a] = gcoord[a] == 0 ? -inf : -1.0 + gcoord[a] * Lf - eps;
+            hi[a] = gcoord[a] == nk - 1 ? inf : -1.0 + (gcoord[a] + 1) * Lf + eps;
+        }
+        const size_t cell = ((size_t)(gz / k) * n + gy / k) * n + gx / k;
+        for (uint32_t j = 0; j < h.cubeCounter[cell]; j++) {
+            const uint32_t fi = h.cubes[cell * h.maxFPC + j];
+            const float* f = &h.fiberPos[4 * (size_t)fi];
+            // the axes of the distance, as the step's distance function picks them
+            int a0 = 0, a1 = 2;
+            if (f[0] == 2.0f) { a0 = 1; a1 = 2; }
+            else if (f[2] == 2.0f) { a0 = 0; a1 = 1; }
+            double d2 = 0.0;
+            for (int a : {a0, a1}) {
+                const double x = (double)f[a];
+                const double d = std::max(std::max(lo[a] - x, 0.0), x - hi[a]);
+                d2 += d * d;
+            }
+            if (d2 <= (double)f[3] * (1.0 + 1e-4)) {
+                pos.push_back(j);
+                for (int q = 0; q < 4; q++) rec.push_back(f[q]);
+            }
+        }
+        start[fc + 1] = (uint32_t)pos.size();
+        if (pos.size() > 0xF0000000u) {
+            set_last_error(kErrTooLarge, "cylinder fine grid: too many entries");
+            return kErrTooLarge;
+        }
+    }
+    int rc;
+    if ((rc = dev_alloc(&c->fineStart, nfine + 1, &c->fineBytes)) || (rc = dev_alloc(&c->fineRec, pos.size(), &c->fineBytes)) ||
+        (rc = dev_alloc(&c->finePos, pos.size(), &c->fineBytes))) {
+        cyl_fine_release(c);
+        return rc;
+    }
+    c->bytes += c->fineBytes;
+    DSIM_CUDA_TRY(cudaMemcpy(c->fineStart, start.data(), start.size() * 4, cudaMemcpyHostToDevice));
+    if (!pos.empty()) {
+        DSIM_CUDA_TRY(cudaMemcpy(c->fineRec, rec.data(), rec.size() * 4, cudaMemcpyHostToDevice));
+        DSIM_CUDA_TRY(cudaMemcpy(c->finePos, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice));
+    }
+    c->fineK = k;
+    c->fineEntries = pos.size();
+    return kOk;
 }
 
 static int cyl_upload(dsim_cyl* c) {
@@ -471,6 +600,7 @@ static int cyl_upload(dsim_cyl* c) {
     if (ok) {
         if ((rc = dev_alloc(&c->cubeF, h.cubes.size(), &c->bytes))) return rc;
         DSIM_CUDA_TRY(cudaMemcpy(c->cubeF, inl.data(), inl.size() * 4, cudaMemcpyHostToDevice));
+        if ((rc = cyl_fine_build(c, cyl_fine_default(h)))) return rc;
     }
     return kOk;
 }
@@ -510,6 +640,21 @@ int dsim_cyl_info(const dsim_cyl* c, uint32_t geom[3], float* cubeLength, uint32
     if (cubeCounter) memcpy(cubeCounter, h.cubeCounter.data(), h.cubeCounter.size() * 4);
     if (cubes && !h.cubes.empty()) memcpy(cubes, h.cubes.data(), h.cubes.size() * 4);
     if (fiberPos4 && h.nF) memcpy(fiberPos4, h.fiberPos.data(), (size_t)h.nF * 16);
+    return kOk;
+}
+
+int dsim_cyl_set_fine(dsim_cyl* c, uint32_t k) {
+    if (!c) return kErrInvalid;
+    if (cyl_holds(c) > 0) {
+        set_last_error(kErrInvalid, "dsim_cyl_set_fine: the substrate is in a batch (free the batch first)");
+        return kErrInvalid;
+    }
+    return cyl_fine_build(c, k);
+}
+
+int dsim_cyl_fine_info(const dsim_cyl* c, uint64_t info[3]) {
+    if (!c || !info) return kErrInvalid;
+    info[0] = c->fineK; info[1] = c->fineEntries; info[2] = c->fineBytes;
     return kOk;
 }
 

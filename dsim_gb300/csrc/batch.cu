@@ -54,6 +54,7 @@ struct JobDev {
     uint32_t key0, key1;
     uint32_t flags;               // DSIM_JOB_PRECISE or DSIM_JOB_LOCAL
     float spinR;                  // spin radius (the precision form clamps to +-(1 - spinR) in FP64)
+    uint32_t sortRegion;          // cylinders: spins outside every fiber sort after those inside
 };
 
 static_assert(sizeof(JobDev) % 4 == 0 && sizeof(SubDev) % 4 == 0, "records are copied by 32-bit words");
@@ -537,13 +538,17 @@ __global__ void k_batch_keys(const JobDev* __restrict__ jobs, BatchSpins S, uint
     const uint32_t bits = J.sortBits, n = 1u << bits;
     uint32_t key;
     if (S.u[U_ID][i] == 0xFFFFFFFFu) {
-        key = J.sortBase + (1u << (3 * bits)) - 1u;
+        key = J.sortBase + ((J.sortRegion ? 2u : 1u) << (3 * bits)) - 1u;
     } else {
+        // cylinder jobs: a spin outside every fiber scans its cell's fiber
+        // list (twice), one inside tests its own fiber once, so the two
+        // kinds go to separate warps: region (imo == 2) above the cell code
+        const uint32_t region = J.sortRegion && (S.u[U_META][i] & 0xFFu) >= 2u ? 1u : 0u;
         const float s = 0.5f * (float)n;
         uint32_t a = (uint32_t)fminf(fmaxf(floorf((S.f[F_X][i] + 1.0f) * s), 0.0f), (float)(n - 1));
         uint32_t b = (uint32_t)fminf(fmaxf(floorf((S.f[F_Y][i] + 1.0f) * s), 0.0f), (float)(n - 1));
         uint32_t c = (uint32_t)fminf(fmaxf(floorf((S.f[F_Z][i] + 1.0f) * s), 0.0f), (float)(n - 1));
-        key = J.sortBase + morton3(a, b, c);
+        key = J.sortBase + (region << (3 * bits)) + morton3(a, b, c);
     }
     keys[i] = key;
     atomicAdd(hist + key, 1u);
@@ -700,6 +705,7 @@ struct dsim_batch {
     uint64_t N = 0;
     std::vector<SubDev> subs;
     std::vector<const dsim_mesh*> meshes;  // per substrate (null for cylinders)
+    std::vector<const dsim_cyl*> cylsHeld; // cylinder substrates added (released on free)
     SubDev* d_subs = nullptr;
     uint32_t subCap = 256;
     std::vector<BatchJob> jobs;            // packing order
@@ -761,7 +767,7 @@ int layout_keys(dsim_batch* b) {
     uint64_t K = 0, slot = 0;
     for (auto& j : b->jobs) {
         j.d.sortBase = (uint32_t)K;
-        K += 1ull << (3 * j.d.sortBits);
+        K += (j.d.sortRegion ? 2ull : 1ull) << (3 * j.d.sortBits);
         j.slot0 = slot;
         slot += j.pad;
     }
@@ -954,6 +960,7 @@ void dsim_batch_free(dsim_batch* b) {
     cudaFree(b->d_jobs); cudaFree(b->d_subs); cudaFree(b->d_counts); cudaFree(b->d_status);
     cudaFree(b->d_stepNow);
     if (b->st) cudaStreamDestroy(b->st);
+    for (const dsim_cyl* c : b->cylsHeld) cyl_hold(c, -1);
     delete b;
 }
 
@@ -984,7 +991,10 @@ int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate) {
     s.kind = kSubCyl;
     int rc = cyl_view(c, &s.c);
     if (rc) return rc;
-    return add_sub(b, s, nullptr, substrate);
+    if ((rc = add_sub(b, s, nullptr, substrate))) return rc;
+    cyl_hold(c, 1);
+    b->cylsHeld.push_back(c);
+    return kOk;
 }
 
 // first precision-form job on a substrate: the mesh's FP64 triangle table, and
@@ -1033,6 +1043,7 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     J.steps = d->steps;
     J.start = b->stepNow;
     J.sortBits = sort_bits(d->nSpins);
+    J.sortRegion = cyl ? 1u : 0u;
     for (int k = 0; k < 4; k++) { J.sd[k] = d->stepSd[k]; J.T2[k] = d->T2[k]; }
     J.perm = d->permeability;
     J.dt = d->deltaTime;

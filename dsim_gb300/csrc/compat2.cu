@@ -129,6 +129,8 @@ void integrateSystem(float* pos, unsigned int* randSeed, float deltaTime, float*
     }
     CylDev g;
     g.cube_fibers = nullptr;  // the reference's own grid arrays: fiber indices only
+    g.fine_start = nullptr; g.fine_rec = nullptr; g.fine_pos = nullptr;
+    g.fineK = 0; g.fineInv = 0.0f;
     g.fibers = fiberPos ? reinterpret_cast<const float4*>(fiberPos) : s.fibers;
     g.cube_count = cubeCounters;
     g.cubes = cubeList ? cubeList : s.boundList;

@@ -29,6 +29,39 @@ __device__ __forceinline__ float cyl_dist_sq(float px, float py, float pz, float
     return (px - f.x) * (px - f.x) + (pz - f.z) * (pz - f.z);
 }
 
+// The spin's fine cell inside its grid cell `cube` (the grid's own cell of
+// the point): the fine coordinate, clamped to the grid cell's fineK cells.
+__device__ __forceinline__ uint32_t cyl_fine_cell(const CylDev& g, float px, float py, float pz, uint32_t cube) {
+    const uint32_t n = g.n, k = g.fineK, nk = n * k;
+    const uint32_t cx = cube % n, cy = (cube / n) % n, cz = cube / (n * n);
+    const float hi = (float)(k - 1);
+    const float sx = fminf(fmaxf(floorf((px + 1.0f) * g.fineInv) - (float)(cx * k), 0.0f), hi);
+    const float sy = fminf(fmaxf(floorf((py + 1.0f) * g.fineInv) - (float)(cy * k), 0.0f), hi);
+    const float sz = fminf(fmaxf(floorf((pz + 1.0f) * g.fineInv) - (float)(cz * k), 0.0f), hi);
+    return ((cz * k + (uint32_t)sz) * nk + (cy * k + (uint32_t)sy)) * nk + cx * k + (uint32_t)sx;
+}
+
+// One list entry (fiber record f, list position j) of the first pass of a
+// spin outside every fiber, tested at the current p.
+__device__ __forceinline__ void cyl_outside_entry(float4 f, const uint32_t* list, uint32_t j, float ox, float oy,
+                                                  float oz, float& px, float& py, float& pz, float u, float perm,
+                                                  float inR, uint32_t& imo, uint32_t& nearest, uint32_t& nrej,
+                                                  uint32_t& nperm, bool& moved, bool& inside) {
+    float radSq = f.w;
+    float cur = cyl_dist_sq(px, py, pz, f);
+    inside |= (cur < inR * radSq) | (cur < radSq);
+    if ((cur <= radSq) & (cur > inR * radSq)) {
+        if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else { imo = 1; nearest = __ldg(list + j); nperm++; }
+    } else if (cur < inR * radSq) {
+        if (u < 1.0f - perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else if ((1.0f - perm < u) & (u < 1.0f - perm * perm)) {
+            px = ox; py = oy; pz = oz; nearest = __ldg(list + j); imo = 1; nrej++;
+            moved = true;
+        } else { imo = 0; nearest = __ldg(list + j); nperm++; }
+    }
+}
+
 // Membrane test of the proposed position p (from o) for a spin in region imo
 // (0 core, 1 myelin, 2 outside) with nearest fiber `nearest`: a rejected step
 // puts p back to o; permeation and the end-position region update imo.
@@ -72,45 +105,69 @@ __device__ __forceinline__ void cyl_membranes(const CylDev& g, float ox, float o
             uint32_t cnt = __ldg(g.cube_count + cube);
             const uint32_t* list = g.cubes + (size_t)cube * g.maxFPC;
             const float4* inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
-            for (uint32_t j = 0; j < cnt; j++) {
+            // The second pass below rejects the step once for each fiber of
+            // the end position's cell with d^2 < inR r^2 or d^2 < r^2.  While
+            // this pass moves nothing, the end position is the one tested
+            // here, so `inside` (that test on every entry) decides whether
+            // the second pass can change anything; if not, it is skipped.
+            bool moved = false, inside = false;
+            const bool fine = g.fine_start != nullptr && inR <= 1.0f;
+            uint32_t j = 0;
+            if (fine) {
+                // While the tested point is p, only the fine cell's entries
+                // can act; after the first rejection (p = o) the rest of the
+                // list is tested at o entry by entry.
+                const uint32_t fc = cyl_fine_cell(g, px, py, pz, cube);
+                const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+                j = cnt;
+                for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+                    const uint32_t jj = __ldg(g.fine_pos + e);
+                    cyl_outside_entry(__ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR, imo,
+                                      nearest, nrej, nperm, moved, inside);
+                    if (moved) { j = jj + 1; break; }
+                }
+            }
+            for (; j < cnt; j++) {
                 float4 f;
-                uint32_t fi = 0;
                 if (inl) {
                     f = __ldg(inl + j);
                 } else {
-                    fi = __ldg(list + j);
+                    const uint32_t fi = __ldg(list + j);
                     if (fi >= g.nF) { status |= kStatusBadCell; continue; }
                     f = __ldg(g.fibers + fi);
                 }
-                float radSq = f.w;
-                float cur = cyl_dist_sq(px, py, pz, f);
-                if ((cur <= radSq) & (cur > inR * radSq)) {
-                    if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
-                    else { imo = 1; nearest = inl ? __ldg(list + j) : fi; nperm++; }
-                } else if (cur < inR * radSq) {
-                    if (u < 1.0f - perm) { px = ox; py = oy; pz = oz; nrej++; }
-                    else if ((1.0f - perm < u) & (u < 1.0f - perm * perm)) {
-                        px = ox; py = oy; pz = oz; nearest = inl ? __ldg(list + j) : fi; imo = 1; nrej++;
-                    } else { imo = 0; nearest = inl ? __ldg(list + j) : fi; nperm++; }
-                }
+                cyl_outside_entry(f, list, j, ox, oy, oz, px, py, pz, u, perm, inR, imo, nearest, nrej, nperm,
+                                  moved, inside);
             }
-            if (imo == 2) {
+            if (imo == 2 && (moved || inside)) {
                 cube = cyl_cell(px, py, pz, g.L, g.n);
                 cnt = __ldg(g.cube_count + cube);
                 list = g.cubes + (size_t)cube * g.maxFPC;
                 inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
-                for (uint32_t j = 0; j < cnt; j++) {
-                    float4 f;
-                    if (inl) {
-                        f = __ldg(inl + j);
-                    } else {
-                        const uint32_t fi = __ldg(list + j);
-                        if (fi >= g.nF) { status |= kStatusBadCell; continue; }
-                        f = __ldg(g.fibers + fi);
+                if (fine && moved) {
+                    // p = o for the whole pass, so o's fine cell stands for the list
+                    const uint32_t fc = cyl_fine_cell(g, px, py, pz, cube);
+                    const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+                    for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+                        const float4 f = __ldg(g.fine_rec + e);
+                        float nd = cyl_dist_sq(px, py, pz, f);
+                        if (nd < inR * f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                        else if (nd < f.w) { px = ox; py = oy; pz = oz; nrej++; }
                     }
-                    float nd = cyl_dist_sq(px, py, pz, f);
-                    if (nd < inR * f.w) { px = ox; py = oy; pz = oz; nrej++; }
-                    else if (nd < f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                } else {
+                    for (uint32_t j2 = 0; j2 < cnt; j2++) {
+                        float4 f;
+                        if (inl) {
+                            f = __ldg(inl + j2);
+                        } else {
+                            const uint32_t fi = __ldg(list + j2);
+                            if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+                            f = __ldg(g.fibers + fi);
+                        }
+                        float nd = cyl_dist_sq(px, py, pz, f);
+                        if (nd < inR * f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                        else if (nd < f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                    }
                 }
             }
         }

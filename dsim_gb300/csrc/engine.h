@@ -183,6 +183,14 @@ struct CylDev {
     uint32_t n, maxFPC;
     float L;
     uint32_t nF;                // number of fibers (index bound)
+    // fine filter grid (or null): each grid cell split fineK^3 ways; a fine
+    // cell lists, in list order, the positions of its grid cell's entries
+    // whose fiber can contain a point of the fine cell
+    const uint32_t* fine_start; // (n fineK)^3 + 1 offsets
+    const float4* fine_rec;     // per fine entry, the fiber record
+    const uint32_t* fine_pos;   // per fine entry, its position in the grid cell's list
+    uint32_t fineK;
+    float fineInv;              // fineK / L
 };
 struct CylSpinsDev {
     float4* pos;       // x, y, z, phase (dSim2 GPU layout)
@@ -218,6 +226,8 @@ int mesh_views(const ::dsim_mesh* m, MeshDev* g, AccelDev* a);
 // builds the mesh's FP64 triangle table on first use (kept until the mesh is freed)
 int mesh_tri64(::dsim_mesh* m);
 int cyl_view(const ::dsim_cyl* c, CylDev* g);
+// batches holding a cylinder substrate's device view (+1 on add, -1 on free)
+void cyl_hold(const ::dsim_cyl* c, int delta);
 int mesh_rebuild_accel(::dsim_mesh* m, uint32_t nf);
 
 }  // namespace dsim

@@ -286,6 +286,15 @@ class Cylinders:
         check(native().dsim_cyl_info(self.h, geom, C.byref(L), cc, cubes, fp))
         return cc, cubes, fp[:4 * self.nF]
 
+    def set_fine(self, k):
+        """Rebuild the fine filter grid with k cells per grid-cell edge (0: none)."""
+        check(native().dsim_cyl_set_fine(self.h, int(k)))
+
+    def fine_info(self):
+        info = np.zeros(3, np.uint64)
+        check(native().dsim_cyl_fine_info(self.h, info))
+        return {"k": int(info[0]), "entries": int(info[1]), "nbytes": int(info[2])}
+
     def free(self):
         if self.h:
             native().dsim_cyl_free(self.h)

@@ -110,6 +110,16 @@ int dsim_cyl_create(const float* fiberPos4, uint32_t nFibers, float maxRadius, d
  * (either pointer may be NULL) */
 int dsim_cyl_info(const dsim_cyl* c, uint32_t geom[3], float* cubeLength, uint32_t* cubeCounter,
                   uint32_t* cubes, float* fiberPos4);
+/* Fine filter grid over the reference grid, built by default: each grid cell
+ * split k x k x k ways (k about twice the grid cell over the largest radius,
+ * at most 16); a fine cell lists, in list order, the grid cell's entries whose
+ * fiber can contain a point of it.  A spin outside every fiber tests only
+ * those while its tested point stays in the cell, with results equal to the
+ * full list scan.  dsim_cyl_set_fine rebuilds it with k cells per grid cell
+ * edge (0 or 1: none; at most (numCubes k)^3 = 2^24 cells; call it before
+ * the substrate is added to a batch).  info = {k, fine entries, bytes}. */
+int dsim_cyl_set_fine(dsim_cyl* c, uint32_t k);
+int dsim_cyl_fine_info(const dsim_cyl* c, uint64_t info[3]);
 void dsim_cyl_free(dsim_cyl* c);
 
 /* ---- spin state (device resident, one CUDA stream per object) ---------- */

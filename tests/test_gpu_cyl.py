@@ -128,3 +128,101 @@ def test_cyl_replay_bit_parity_dsim2_abi(engine, tmp_path):
     assert np.array_equal(sd[:, 2] - 1, rpar[:, 3].astype(np.uint32))
     for p in (dPos, dSeed, dFib, dCc, dCubes, dDraws, dCnt):
         L2.freeArray(p)
+
+
+def _mixed_fibers(seed, per_axis=24):
+    """Fibers along x, y and z (the axis coordinate 2.0), overlapping freely."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for axis in (0, 1, 2):
+        for _ in range(per_axis):
+            c = rng.uniform(-0.9, 0.9, 3)
+            r = rng.uniform(0.03, 0.12)
+            c[axis] = 2.0
+            rows.append([c[0], c[1], c[2], r * r])
+    fp = np.array(rows, np.float32).reshape(-1)
+    return fp, float(np.sqrt(fp.reshape(-1, 4)[:, 3].max()))
+
+
+@pytest.mark.parametrize("perm,inner", [(0.0, 1.0), (0.05, 0.7)])
+def test_cyl_fine_grid_equals_full_list_scan(engine, perm, inner):
+    """The fine filter grid against the full scan of the reference grid's
+    lists, bit for bit: mixed fiber axes, Philox draws, several fine sizes,
+    and a third of the spins labelled outside while inside a fiber (their
+    first test rejects, so the rest of the list runs at the old position)."""
+    from dsim_gb300.engine import Cylinders, Spins, cyl_params, cyl_run
+    fp, maxR = _mixed_fibers(5)
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, maxR)
+    N = 24000
+    rng = np.random.default_rng(6)
+    pos = rng.uniform(-0.99, 0.99, (N, 3)).astype(np.float32)
+    pos4 = np.zeros((N, 4), np.float32)
+    pos4[:, :3] = pos
+    near = np.zeros(N, np.uint32)
+    imo = np.zeros(N, np.uint32)
+    O.lib().or2_find_nearest(N, pos4.reshape(-1), fp, n, L, maxfpc, cc, cubes, float(inner), near, imo)
+    imo[::3] = 2
+    c = Cylinders.from_arrays(fp, maxR)
+    assert (c.numCubes, c.maxFPC) == (n, maxfpc)
+    assert c.fine_info()["k"] >= 2 and c.fine_info()["entries"] > 0
+    p = cyl_params(2.0, 2.0, 0.2, 10.0, 70.0, 8.0, 80.0, perm, inner, 0.01, 0.5)
+    outs = {}
+    for k in (0, 2, 7, 16, None):
+        if k is None:
+            c.free()
+            c = Cylinders.from_arrays(fp, maxR)   # the default size again
+        else:
+            c.set_fine(k)
+            assert c.fine_info()["k"] == k
+        s = Spins(N)
+        s.set_cyl(pos.reshape(-1), None, None, imo, near)
+        cyl_run(c, s, p, g=(0.01, 0.02, -0.01), iterations=400, seed=17, count=True)
+        assert s.status() == 0
+        outs[k] = (s.get_cyl(), s.counts())
+    (pos0, mag0, ph0, imo0, near0), cnt0 = outs[0]
+    assert cnt0[:, 0].sum() > 0
+    if perm > 0:
+        assert cnt0[:, 1].sum() > 0
+    for k, ((pk, mk, phk, ik, nk), ck) in outs.items():
+        assert np.array_equal(pk.view(np.uint32), pos0.view(np.uint32)), k
+        assert np.array_equal(phk.view(np.uint32), ph0.view(np.uint32)), k
+        assert np.array_equal(mk.view(np.uint32), mag0.view(np.uint32)), k
+        assert np.array_equal(ik, imo0) and np.array_equal(nk, near0) and np.array_equal(ck, cnt0), k
+
+
+def test_cyl_fine_grid_in_a_batch(engine):
+    """A cylinder job in a batch, with and without the fine grid: the same
+    spins, moments and counts."""
+    from dsim_gb300._lib import DsimError
+    from dsim_gb300.engine import Batch, Cylinders
+    fp, maxR = _mixed_fibers(8)
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, maxR)
+    N = 5000
+    rng = np.random.default_rng(9)
+    pos = rng.uniform(-0.99, 0.99, (N, 3)).astype(np.float32)
+    pos4 = np.zeros((N, 4), np.float32)
+    pos4[:, :3] = pos
+    near = np.zeros(N, np.uint32)
+    imo = np.zeros(N, np.uint32)
+    O.lib().or2_find_nearest(N, pos4.reshape(-1), fp, n, L, maxfpc, cc, cubes, 0.7, near, imo)
+    res = []
+    for fine in (True, False):
+        c = Cylinders.from_arrays(fp, maxR)
+        if not fine:
+            c.set_fine(0)
+        b = Batch(N + 32, 2)
+        sid = b.add_cyl(c)
+        with pytest.raises(DsimError, match="in a batch"):
+            c.set_fine(3)   # the batch holds the substrate's device view
+        j = b.submit(sid, pos.reshape(-1), imo.astype(np.uint8), near, 300, 0.01, [0.02, 0.02, 0.01, 0.0],
+                     [0.0] * 4, 0.5, 3, permeability=0.05, waveform="pgse", delta=1.0, Delta=2.0,
+                     inner_radius_proportion=0.7)
+        b.run()
+        res.append((b.get(j, N), b.counts(j)))
+        b.close()
+        c.set_fine(0)   # allowed again once the batch is gone
+        c.free()
+    (a, ca), (b_, cb) = res
+    assert ca[0] > 0 and np.array_equal(ca, cb)
+    for x, y in zip(a, b_):
+        assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8))
