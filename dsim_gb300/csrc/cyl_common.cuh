@@ -120,11 +120,28 @@ __device__ __forceinline__ void cyl_membranes(const CylDev& g, float ox, float o
                 const uint32_t fc = cyl_fine_cell(g, px, py, pz, cube);
                 const uint32_t e1 = __ldg(g.fine_start + fc + 1);
                 j = cnt;
+                uint32_t jm = 0;
                 for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
                     const uint32_t jj = __ldg(g.fine_pos + e);
                     cyl_outside_entry(__ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR, imo,
                                       nearest, nrej, nperm, moved, inside);
-                    if (moved) { j = jj + 1; break; }
+                    if (moved) { jm = jj; break; }
+                }
+                // the entries after position jm, at o: when o lies in the same
+                // grid cell, o's fine cell holds every one that can act there
+                if (moved) {
+                    if (cyl_cell(px, py, pz, g.L, g.n) == cube) {
+                        const uint32_t fo = cyl_fine_cell(g, px, py, pz, cube);
+                        const uint32_t eo1 = __ldg(g.fine_start + fo + 1);
+                        for (uint32_t e = __ldg(g.fine_start + fo); e < eo1; e++) {
+                            const uint32_t jj = __ldg(g.fine_pos + e);
+                            if (jj <= jm) continue;
+                            cyl_outside_entry(__ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR,
+                                              imo, nearest, nrej, nperm, moved, inside);
+                        }
+                    } else {
+                        j = jm + 1;
+                    }
                 }
             }
             for (; j < cnt; j++) {
