@@ -712,7 +712,12 @@ def run_cylinders(args):
            "signal_plain": plain_S[::8], "signal_batched": batch_S[::8], "signal_shared_walk": shared_S[::8],
            "rejections_per_spin_step": float(counts[0]) / (N * steps),
            "roofline": {"bytes_per_spin_step": 2 * 20 + 16 * Cbar, "C_bar": Cbar,
-                        "achieved_GBs_batched": (2 * 20 + 16 * Cbar) * work / batch_s / 1e9},
+                        "achieved_GBs_batched": (2 * 20 + 16 * Cbar) * work / batch_s / 1e9,
+                        "fine_grid": c.fine_info(),
+                        "note": "bytes of the reference's scan (C_bar list entries a step examines); the fine "
+                                "filter grid tests only the entries of the spin's fine cell (about 2 here), with "
+                                "equal results, so achieved can exceed the HBM copy peak: the kernel reads its "
+                                "fibers and grid from L1/L2 and is bound by instruction issue"},
            "note": "signals listed for every 8th gradient (G = 0 .. 80 mT/m along x)"}
     # the reference's CPU path (oracle port, MWC draws) on a sample
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
