@@ -94,6 +94,8 @@ def _declare_native(L):
         "dsim_cyl_create": (i32, [F32, u32, f32, C.POINTER(VP)]),
         "dsim_cyl_info": (i32, [VP, U32, C.POINTER(f32), OU32, OU32, OF32]),
         "dsim_cyl_set_fine": (i32, [VP, u32]),
+        "dsim_cyl_fine_lists": (i32, [F32, u32, u32, u32, f32, U32, U32, u32, OU32, OU32, C.c_uint64,
+                                      C.POINTER(C.c_uint64)]),
         "dsim_cyl_fine_info": (i32, [VP, _nd(np.uint64, flags="C_CONTIGUOUS")]),
         "dsim_cyl_free": (None, [VP]),
         "dsim_spins_create": (i32, [u32, C.POINTER(VP)]),

@@ -510,21 +510,22 @@ static uint32_t cyl_fine_default(const CylHost& h) {
     return k >= 2 ? k : 0;
 }
 
-static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
-    cyl_fine_release(c);
-    const CylHost& h = c->host;
-    const uint32_t n = h.numCubes;
-    const double L = (double)h.cubeLength;
-    if (k < 2 || n == 0 || !c->cubeF) return kOk;
-    if ((uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 24)) {
-        set_last_error(kErrTooLarge, "cylinder fine grid: (%u x %u)^3 cells, limit 2^24", n, k);
+// The fine lists on the host: start[(n k)^3 + 1] offsets, and per entry its
+// list position and fiber record.  Every listed fiber index must be < nF.
+static int cyl_fine_lists(const float* fiberPos, uint32_t nF, uint32_t n, uint32_t maxFPC, float cubeLength,
+                          const uint32_t* cubeCounter, const uint32_t* cubes, uint32_t k,
+                          std::vector<uint32_t>& start, std::vector<uint32_t>& pos, std::vector<float>& rec) {
+    if (k < 2 || n == 0 || (uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 24)) {
+        set_last_error(kErrTooLarge, "cylinder fine grid: (%u x %u)^3 cells, limit 2^24 and k >= 2", n, k);
         return kErrTooLarge;
     }
     const uint32_t nk = n * k;
     const size_t nfine = (size_t)nk * nk * nk;
+    const double L = (double)cubeLength;
     const double Lf = L / k, eps = 1e-5, inf = std::numeric_limits<double>::infinity();
-    std::vector<uint32_t> start(nfine + 1, 0), pos;
-    std::vector<float> rec;
+    start.assign(nfine + 1, 0);
+    pos.clear();
+    rec.clear();
     for (size_t fc = 0; fc < nfine; fc++) {
         const uint32_t gx = (uint32_t)(fc % nk), gy = (uint32_t)((fc / nk) % nk), gz = (uint32_t)(fc / ((size_t)nk * nk));
         const uint32_t gcoord[3] = {gx, gy, gz};
@@ -534,9 +535,17 @@ static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
             hi[a] = gcoord[a] == nk - 1 ? inf : -1.0 + (gcoord[a] + 1) * Lf + eps;
         }
         const size_t cell = ((size_t)(gz / k) * n + gy / k) * n + gx / k;
-        for (uint32_t j = 0; j < h.cubeCounter[cell]; j++) {
-            const uint32_t fi = h.cubes[cell * h.maxFPC + j];
-            const float* f = &h.fiberPos[4 * (size_t)fi];
+        if (cubeCounter[cell] > maxFPC) {
+            set_last_error(kErrFormat, "cylinder grid: cell %zu lists %u entries, limit %u", cell, cubeCounter[cell], maxFPC);
+            return kErrFormat;
+        }
+        for (uint32_t j = 0; j < cubeCounter[cell]; j++) {
+            const uint32_t fi = cubes[cell * maxFPC + j];
+            if (fi >= nF) {
+                set_last_error(kErrFormat, "cylinder grid: entry names fiber %u of %u", fi, nF);
+                return kErrFormat;
+            }
+            const float* f = &fiberPos[4 * (size_t)fi];
             // the axes of the distance, as the step's distance function picks them
             int a0 = 0, a1 = 2;
             if (f[0] == 2.0f) { a0 = 1; a1 = 2; }
@@ -558,7 +567,19 @@ static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
             return kErrTooLarge;
         }
     }
-    int rc;
+    return kOk;
+}
+
+static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
+    cyl_fine_release(c);
+    const CylHost& h = c->host;
+    if (k < 2 || h.numCubes == 0 || !c->cubeF) return kOk;
+    std::vector<uint32_t> start, pos;
+    std::vector<float> rec;
+    int rc = cyl_fine_lists(h.fiberPos.data(), h.nF, h.numCubes, h.maxFPC, h.cubeLength, h.cubeCounter.data(),
+                            h.cubes.data(), k, start, pos, rec);
+    if (rc) return rc;
+    const size_t nfine = start.size() - 1;
     if ((rc = dev_alloc(&c->fineStart, nfine + 1, &c->fineBytes)) || (rc = dev_alloc(&c->fineRec, pos.size(), &c->fineBytes)) ||
         (rc = dev_alloc(&c->finePos, pos.size(), &c->fineBytes))) {
         cyl_fine_release(c);
@@ -650,6 +671,26 @@ int dsim_cyl_set_fine(dsim_cyl* c, uint32_t k) {
         return kErrInvalid;
     }
     return cyl_fine_build(c, k);
+}
+
+int dsim_cyl_fine_lists(const float* fiberPos4, uint32_t nFibers, uint32_t numCubes, uint32_t maxFibersPerCube,
+                        float cubeLength, const uint32_t* cubeCounter, const uint32_t* cubes, uint32_t k,
+                        uint32_t* start, uint32_t* positions, uint64_t capacity, uint64_t* entries) {
+    if (!fiberPos4 || !cubeCounter || !cubes || !entries) { set_last_error(kErrInvalid, "dsim_cyl_fine_lists: null argument"); return kErrInvalid; }
+    std::vector<uint32_t> st, pos;
+    std::vector<float> rec;
+    int rc = cyl_fine_lists(fiberPos4, nFibers, numCubes, maxFibersPerCube, cubeLength, cubeCounter, cubes, k, st, pos, rec);
+    if (rc) return rc;
+    *entries = pos.size();
+    if (start) memcpy(start, st.data(), st.size() * 4);
+    if (positions) {
+        if (pos.size() > capacity) {
+            set_last_error(kErrTooLarge, "dsim_cyl_fine_lists: %zu entries, capacity %llu", pos.size(), (unsigned long long)capacity);
+            return kErrTooLarge;
+        }
+        if (!pos.empty()) memcpy(positions, pos.data(), pos.size() * 4);
+    }
+    return kOk;
 }
 
 int dsim_cyl_fine_info(const dsim_cyl* c, uint64_t info[3]) {

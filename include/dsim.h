@@ -120,6 +120,14 @@ int dsim_cyl_info(const dsim_cyl* c, uint32_t geom[3], float* cubeLength, uint32
  * the substrate is added to a batch).  info = {k, fine entries, bytes}. */
 int dsim_cyl_set_fine(dsim_cyl* c, uint32_t k);
 int dsim_cyl_fine_info(const dsim_cyl* c, uint64_t info[3]);
+/* The fine lists dsim_cyl_set_fine builds, computed on the host (no device
+ * call) from a reference grid: start[(numCubes k)^3 + 1] offsets and each
+ * entry's position in its grid cell's list; fine cell (gx, gy, gz) is
+ * (gz nk + gy) nk + gx, nk = numCubes k, inside grid cell (g / k).
+ * *entries = the entry count; positions (may be NULL) holds `capacity`. */
+int dsim_cyl_fine_lists(const float* fiberPos4, uint32_t nFibers, uint32_t numCubes, uint32_t maxFibersPerCube,
+                        float cubeLength, const uint32_t* cubeCounter, const uint32_t* cubes, uint32_t k,
+                        uint32_t* start, uint32_t* positions, uint64_t capacity, uint64_t* entries);
 void dsim_cyl_free(dsim_cyl* c);
 
 /* ---- spin state (device resident, one CUDA stream per object) ---------- */
