@@ -265,6 +265,7 @@ def _declare_abi2(L):
         "dsim2_last_status": (i32, []),
         "dsim2_set_replay": (None, [VP, VP]),
         "dsim2_status": (u32, []),
+        "dsim2_set_fine": (None, [C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

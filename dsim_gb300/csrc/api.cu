@@ -501,73 +501,7 @@ static void cyl_release(dsim_cyl* c) {
 // such a point is the clamped one).  The spin's fine cell is taken inside
 // its grid cell, so the fine list is a subsequence of the list it replaces.
 static uint32_t cyl_fine_default(const CylHost& h) {
-    // fine cells about half the largest radius across, at most 16 per grid
-    // cell edge and 2^22 fine cells in all
-    const uint32_t n = h.numCubes;
-    if (!(h.maxR > 0.0f) || n == 0) return 0;
-    uint32_t k = (uint32_t)std::min(16.0, std::ceil(2.0 * (double)h.cubeLength / (double)h.maxR));
-    while (k >= 2 && (uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 22)) k--;
-    return k >= 2 ? k : 0;
-}
-
-// The fine lists on the host: start[(n k)^3 + 1] offsets, and per entry its
-// list position and fiber record.  Every listed fiber index must be < nF.
-static int cyl_fine_lists(const float* fiberPos, uint32_t nF, uint32_t n, uint32_t maxFPC, float cubeLength,
-                          const uint32_t* cubeCounter, const uint32_t* cubes, uint32_t k,
-                          std::vector<uint32_t>& start, std::vector<uint32_t>& pos, std::vector<float>& rec) {
-    if (k < 2 || n == 0 || (uint64_t)(n * k) * (n * k) * (n * k) > (1ull << 24)) {
-        set_last_error(kErrTooLarge, "cylinder fine grid: (%u x %u)^3 cells, limit 2^24 and k >= 2", n, k);
-        return kErrTooLarge;
-    }
-    const uint32_t nk = n * k;
-    const size_t nfine = (size_t)nk * nk * nk;
-    const double L = (double)cubeLength;
-    const double Lf = L / k, eps = 1e-5, inf = std::numeric_limits<double>::infinity();
-    start.assign(nfine + 1, 0);
-    pos.clear();
-    rec.clear();
-    for (size_t fc = 0; fc < nfine; fc++) {
-        const uint32_t gx = (uint32_t)(fc % nk), gy = (uint32_t)((fc / nk) % nk), gz = (uint32_t)(fc / ((size_t)nk * nk));
-        const uint32_t gcoord[3] = {gx, gy, gz};
-        double lo[3], hi[3];
-        for (int a = 0; a < 3; a++) {
-            lo[a] = gcoord[a] == 0 ? -inf : -1.0 + gcoord[a] * Lf - eps;
-            hi[a] = gcoord[a] == nk - 1 ? inf : -1.0 + (gcoord[a] + 1) * Lf + eps;
-        }
-        const size_t cell = ((size_t)(gz / k) * n + gy / k) * n + gx / k;
-        if (cubeCounter[cell] > maxFPC) {
-            set_last_error(kErrFormat, "cylinder grid: cell %zu lists %u entries, limit %u", cell, cubeCounter[cell], maxFPC);
-            return kErrFormat;
-        }
-        for (uint32_t j = 0; j < cubeCounter[cell]; j++) {
-            const uint32_t fi = cubes[cell * maxFPC + j];
-            if (fi >= nF) {
-                set_last_error(kErrFormat, "cylinder grid: entry names fiber %u of %u", fi, nF);
-                return kErrFormat;
-            }
-            const float* f = &fiberPos[4 * (size_t)fi];
-            // the axes of the distance, as the step's distance function picks them
-            int a0 = 0, a1 = 2;
-            if (f[0] == 2.0f) { a0 = 1; a1 = 2; }
-            else if (f[2] == 2.0f) { a0 = 0; a1 = 1; }
-            double d2 = 0.0;
-            for (int a : {a0, a1}) {
-                const double x = (double)f[a];
-                const double d = std::max(std::max(lo[a] - x, 0.0), x - hi[a]);
-                d2 += d * d;
-            }
-            if (d2 <= (double)f[3] * (1.0 + 1e-4)) {
-                pos.push_back(j);
-                for (int q = 0; q < 4; q++) rec.push_back(f[q]);
-            }
-        }
-        start[fc + 1] = (uint32_t)pos.size();
-        if (pos.size() > 0xF0000000u) {
-            set_last_error(kErrTooLarge, "cylinder fine grid: too many entries");
-            return kErrTooLarge;
-        }
-    }
-    return kOk;
+    return cyl_fine_size(h.numCubes, h.cubeLength, h.maxR);
 }
 
 static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
@@ -576,7 +510,7 @@ static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
     if (k < 2 || h.numCubes == 0 || !c->cubeF) return kOk;
     std::vector<uint32_t> start, pos;
     std::vector<float> rec;
-    int rc = cyl_fine_lists(h.fiberPos.data(), h.nF, h.numCubes, h.maxFPC, h.cubeLength, h.cubeCounter.data(),
+    int rc = dsim::cyl_fine_lists(h.fiberPos.data(), h.nF, h.numCubes, h.maxFPC, h.cubeLength, h.cubeCounter.data(),
                             h.cubes.data(), k, start, pos, rec);
     if (rc) return rc;
     const size_t nfine = start.size() - 1;
@@ -679,7 +613,8 @@ int dsim_cyl_fine_lists(const float* fiberPos4, uint32_t nFibers, uint32_t numCu
     if (!fiberPos4 || !cubeCounter || !cubes || !entries) { set_last_error(kErrInvalid, "dsim_cyl_fine_lists: null argument"); return kErrInvalid; }
     std::vector<uint32_t> st, pos;
     std::vector<float> rec;
-    int rc = cyl_fine_lists(fiberPos4, nFibers, numCubes, maxFibersPerCube, cubeLength, cubeCounter, cubes, k, st, pos, rec);
+    int rc = dsim::cyl_fine_lists(fiberPos4, nFibers, numCubes, maxFibersPerCube, cubeLength, cubeCounter, cubes, k, st,
+                                  pos, rec);
     if (rc) return rc;
     *entries = pos.size();
     if (start) memcpy(start, st.data(), st.size() * 4);

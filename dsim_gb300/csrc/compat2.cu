@@ -2,12 +2,14 @@
 // (include/dsim2_abi.h), a drop-in for rfdougherty/dSim dSim2/src/spinSystem.cu.
 // integrateSystem launches the GB300 cylinder step on the legacy default
 // stream, ordered with the reference's synchronous copies.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #pragma GCC visibility push(default)
 #include "../../include/dsim2_abi.h"
@@ -34,8 +36,27 @@ const char* last_error_message() { return g_last_error.c_str(); }
 using namespace dsim;
 
 namespace {
+// The fine filter grid of the last grid arrays seen, with host copies of
+// their contents to detect a change.
+struct FineCache {
+    bool valid = false;
+    uint32_t n = 0, maxFPC = 0, nF = 0, k = 0;
+    float L = 0.0f;
+    std::vector<float> fib;
+    std::vector<uint32_t> cc, cubes;
+    uint32_t* start = nullptr;
+    float4* rec = nullptr;
+    uint32_t* pos = nullptr;
+    void release() {
+        cudaFree(start); cudaFree(rec); cudaFree(pos);
+        start = nullptr; rec = nullptr; pos = nullptr;
+        valid = false;
+    }
+};
 struct State {
     std::mutex mu;
+    FineCache fine;
+    int fineMode = -1;
     int last_status = 0;
     const float4* fibers = nullptr;
     uint32_t nF = 0;
@@ -49,6 +70,69 @@ State& S() {
     return s;
 }
 void fail(int code) { S().last_status = code; }
+
+// Points g at the fine filter grid of its arrays (rebuilt when their contents
+// differ from the last call's); false leaves g on the full list scan.
+bool fine_grid(State& s, CylDev& g) {
+    if (s.fineMode == 0 || s.fineMode == 1) return false;
+    FineCache& c = s.fine;
+    std::vector<float> fib((size_t)g.nF * 4);
+    if (cudaMemcpy(fib.data(), g.fibers, fib.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    uint32_t k = 0;
+    if (s.fineMode >= 2) {
+        k = (uint32_t)s.fineMode;
+    } else {
+        double maxR = 0.0;
+        for (uint32_t i = 0; i < g.nF; i++) {
+            const double w = fib[4 * (size_t)i + 3];
+            if (w > 0.0 && std::isfinite(w)) maxR = std::max(maxR, std::sqrt(w));
+        }
+        k = cyl_fine_size(g.n, g.L, maxR);
+    }
+    if (k < 2 || (uint64_t)(g.n * k) * (g.n * k) * (g.n * k) > (1ull << 24)) return false;
+    const size_t ncell = (size_t)g.n * g.n * g.n;
+    std::vector<uint32_t> cc(ncell), cubes(ncell * g.maxFPC);
+    if (cudaMemcpy(cc.data(), g.cube_count, cc.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+        (!cubes.empty() && cudaMemcpy(cubes.data(), g.cubes, cubes.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+        cudaGetLastError();
+        return false;
+    }
+    auto bytes_equal = [](const auto& a, const auto& b) {
+        return a.size() == b.size() && (a.empty() || memcmp(a.data(), b.data(), a.size() * sizeof(a[0])) == 0);
+    };
+    const bool same = c.valid && c.k == k && c.n == g.n && c.maxFPC == g.maxFPC && c.nF == g.nF &&
+                      memcmp(&c.L, &g.L, 4) == 0 && bytes_equal(c.fib, fib) && bytes_equal(c.cc, cc) &&
+                      bytes_equal(c.cubes, cubes);
+    if (!same) {
+        c.release();
+        std::vector<uint32_t> start, pos;
+        std::vector<float> rec;
+        // a grid the lists cannot describe (an index >= nF, a count above
+        // maxFibersPerCube) keeps the full scan and its status bits
+        if (cyl_fine_lists(fib.data(), g.nF, g.n, g.maxFPC, g.L, cc.data(), cubes.data(), k, start, pos, rec))
+            return false;
+        const size_t ne = std::max<size_t>(1, pos.size());
+        if (cudaMalloc(&c.start, start.size() * 4) != cudaSuccess || cudaMalloc(&c.rec, ne * 16) != cudaSuccess ||
+            cudaMalloc(&c.pos, ne * 4) != cudaSuccess ||
+            cudaMemcpy(c.start, start.data(), start.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+            (!pos.empty() && (cudaMemcpy(c.rec, rec.data(), rec.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+                              cudaMemcpy(c.pos, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess))) {
+            cudaGetLastError();
+            c.release();
+            return false;
+        }
+        c.k = k; c.n = g.n; c.maxFPC = g.maxFPC; c.nF = g.nF; c.L = g.L;
+        c.fib.swap(fib); c.cc.swap(cc); c.cubes.swap(cubes);
+        c.valid = true;
+    }
+    g.fine_start = c.start; g.fine_rec = c.rec; g.fine_pos = c.pos;
+    g.fineK = c.k;
+    g.fineInv = (float)c.k / g.L;
+    return true;
+}
 }  // namespace
 
 extern "C" {
@@ -143,6 +227,7 @@ void integrateSystem(float* pos, unsigned int* randSeed, float deltaTime, float*
         fail(kErrInvalid);
         return;
     }
+    fine_grid(s, g);
     CylStepArgs a;
     memset(&a, 0, sizeof(a));
     // integrateSystem, dSim2/src/spinSystem.cu:148-153: sd = sqrt(2 ADC dt)
@@ -187,6 +272,11 @@ void dsim2_set_replay(const float* draws, unsigned int* counts) {
     std::lock_guard<std::mutex> lk(S().mu);
     S().replay = reinterpret_cast<const float4*>(draws);
     S().counts = counts;
+}
+void dsim2_set_fine(int k) {
+    std::lock_guard<std::mutex> lk(S().mu);
+    S().fineMode = k;
+    S().fine.release();
 }
 unsigned int dsim2_status(void) {
     State& s = S();

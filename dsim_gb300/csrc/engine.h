@@ -226,6 +226,11 @@ int mesh_views(const ::dsim_mesh* m, MeshDev* g, AccelDev* a);
 // builds the mesh's FP64 triangle table on first use (kept until the mesh is freed)
 int mesh_tri64(::dsim_mesh* m);
 int cyl_view(const ::dsim_cyl* c, CylDev* g);
+// fine filter grid of a reference cylinder grid (cyl.cu), built on the host
+uint32_t cyl_fine_size(uint32_t n, float L, double maxR);
+int cyl_fine_lists(const float* fiberPos, uint32_t nF, uint32_t n, uint32_t maxFPC, float cubeLength,
+                   const uint32_t* cubeCounter, const uint32_t* cubes, uint32_t k, std::vector<uint32_t>& start,
+                   std::vector<uint32_t>& pos, std::vector<float>& rec);
 // batches holding a cylinder substrate's device view (+1 on add, -1 on free)
 void cyl_hold(const ::dsim_cyl* c, int delta);
 int mesh_rebuild_accel(::dsim_mesh* m, uint32_t nf);

@@ -61,6 +61,13 @@ int dsim2_last_status(void);
  * (device uint32[2N]); NULL restores Philox / disables counting */
 void dsim2_set_replay(const float* draws, unsigned int* counts);
 unsigned int dsim2_status(void);
+/* Fine filter grid over the caller's grid arrays: integrateSystem copies the
+ * fibers, cubeCounters and cubeList back each call, rebuilds the fine lists
+ * when their contents changed, and then tests a spin outside every fiber
+ * against its fine cell's entries only, with results equal to the full list
+ * scan.  k < 0: the default size (initially); 0 or 1: full list scan;
+ * k >= 2: k fine cells per grid-cell edge. */
+void dsim2_set_fine(int k);
 
 #ifdef __cplusplus
 }

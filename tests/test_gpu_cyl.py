@@ -80,10 +80,13 @@ def test_cyl_replay_bit_parity_native(engine, tmp_path, perm, inner):
     assert np.array_equal(gnear[inside], rpar[inside, 2].astype(np.uint32))
 
 
-def test_cyl_replay_bit_parity_dsim2_abi(engine, tmp_path):
-    """Replay through the reference-facing dSim2 C-ABI (libdsim2.so)."""
+@pytest.mark.parametrize("fine", [-1, 0, 3])
+def test_cyl_replay_bit_parity_dsim2_abi(engine, tmp_path, fine):
+    """Replay through the reference-facing dSim2 C-ABI (libdsim2.so), with
+    the fine filter grid at its default size (-1), off (0) and k = 3."""
     from dsim_gb300 import _lib
     L2 = _lib.abi2()
+    L2.dsim2_set_fine(fine)
     case = CylCase(tmp_path, permeability=0.05, inner=0.7, N=2000)
     fp, maxR, cc, cubes, n, maxfpc, L, near, imo = _setup(case)
     iters = 50
@@ -128,6 +131,92 @@ def test_cyl_replay_bit_parity_dsim2_abi(engine, tmp_path):
     assert np.array_equal(sd[:, 2] - 1, rpar[:, 3].astype(np.uint32))
     for p in (dPos, dSeed, dFib, dCc, dCubes, dDraws, dCnt):
         L2.freeArray(p)
+    L2.dsim2_set_fine(-1)
+
+
+def test_cyl_dsim2_abi_grid_rewritten_in_place(engine, tmp_path):
+    """The caller overwrites the fibers and grid in the same device arrays
+    between two integrateSystem calls: the second call walks the new fibers
+    (the fine grid follows the contents, not the pointers), bit for bit with
+    the oracle run on the same two grids."""
+    from dsim_gb300 import _lib
+    L2 = _lib.abi2()
+    L2.dsim2_set_fine(-1)
+    case = CylCase(tmp_path, permeability=0.05, inner=0.7, N=2000)
+    fp, maxR, cc, cubes, n, maxfpc, L, near, imo = _setup(case)
+    fp2 = fp.copy().reshape(-1, 4)
+    fp2[:, 0] = np.where(fp2[:, 0] == 2.0, fp2[:, 0], fp2[:, 0] + np.float32(0.05))
+    fp2[:, 1] = np.where(fp2[:, 1] == 2.0, fp2[:, 1], fp2[:, 1] - np.float32(0.03))
+    fp2 = fp2.reshape(-1)
+    cc2, cubes2, n2, maxfpc2, L2len = O.build_grid2(fp2, maxR)
+    assert (n2, maxfpc2) == (n, maxfpc) and len(cubes2) == len(cubes)
+    it1, it2 = 30, 30
+    d = draws(it1 + it2, case.N, seed=12)
+    # oracle: the first segment on the first grid, the second on the second
+    rpos, rpar, rcnt = _oracle(case, fp, cc, cubes, n, maxfpc, L, it1, d[:it1], near, imo)
+    p = O.Params2()
+    ss = np.float32(case.spaceScale)
+    p.intraAdcScaled = np.float32(case.D) / (ss * ss)
+    p.extraAdcScaled = np.float32(case.D) / (ss * ss)
+    p.myelinAdcScaled = np.float32(0.1 * case.D) / (ss * ss)
+    p.T2fiber, p.T2myelin, p.T2outside = 70.0, 8.0, 80.0
+    p.permeability = case.permeability
+    p.innerRadiusProportion = case.inner
+    p.spinRadius = 0.005
+    p.deltaTime = case.dt
+    p.numCubes, p.maxFibersPerCube, p.cubeLength = n, maxfpc, L2len
+    pos4 = np.ascontiguousarray(rpos.reshape(-1))
+    par = np.ascontiguousarray(rpar.reshape(-1))
+    seed4 = np.zeros(4 * case.N, np.uint32)
+    cnt = np.ascontiguousarray(rcnt.reshape(-1))
+    O.lib().or2_integrate(C.byref(p), case.N, pos4, seed4, par, fp2, cc2, cubes2, float(case.g[0]),
+                          float(case.g[1]), float(case.g[2]), float(case.pc), it2,
+                          np.ascontiguousarray(d[it1:].reshape(-1)), None, cnt)
+
+    def dev(arr):
+        q = C.c_void_p()
+        L2.allocateArray(C.byref(q), arr.nbytes)
+        L2.copyArrayToDevice(q, arr.ctypes.data, 0, arr.nbytes)
+        return q
+
+    g4 = np.zeros((case.N, 4), np.float32)
+    g4[:, :3] = case.pos.reshape(-1, 3)
+    sd4 = np.zeros((case.N, 4), np.uint32)
+    sd4[:, 2] = imo + 1
+    sd4[:, 3] = near
+    dPos, dSeed = dev(g4), dev(sd4)
+    dFib, dCc, dCubes = dev(fp), dev(cc), dev(cubes)
+    dDraws, dCnt = dev(d.reshape(-1)), dev(np.zeros(2 * case.N, np.uint32))
+    L2.bindFiberList(dFib, len(fp) // 4)
+    L2.bindCubeList(dCubes, len(cubes))
+    ss = np.float32(case.spaceScale)
+    adc = lambda a: float(np.float32(a) / (ss * ss))
+    g = _lib.Float3(*[float(x) for x in case.g])
+    for seg, (fib_h, cc_h, cubes_h, L_seg, its, off) in enumerate(
+            [(fp, cc, cubes, L, it1, 0), (fp2, cc2, cubes2, L2len, it2, it1)]):
+        if seg:
+            L2.copyArrayToDevice(dFib, fib_h.ctypes.data, 0, fib_h.nbytes)
+            L2.copyArrayToDevice(dCc, cc_h.ctypes.data, 0, cc_h.nbytes)
+            L2.copyArrayToDevice(dCubes, cubes_h.ctypes.data, 0, cubes_h.nbytes)
+        L2.dsim2_set_replay(C.c_void_p(dDraws.value + off * case.N * 16), dCnt)
+        L2.integrateSystem(dPos, dSeed, float(case.dt), dFib, float(case.permeability), adc(case.D),
+                           adc(case.D), adc(0.1 * case.D), case.N, g, float(case.pc), dCc, dCubes,
+                           float(L_seg), n, maxfpc, float(case.inner), its)
+        assert L2.dsim2_last_status() == 0, L2.dsim2_last_error()
+    L2.dsim2_set_replay(None, None)
+    out = np.zeros_like(g4)
+    sd = np.zeros_like(sd4)
+    gcnt = np.zeros(2 * case.N, np.uint32)
+    L2.copyArrayFromDevice(out.ctypes.data, dPos, 0, out.nbytes)
+    L2.copyArrayFromDevice(sd.ctypes.data, dSeed, 0, sd.nbytes)
+    L2.copyArrayFromDevice(gcnt.ctypes.data, dCnt, 0, gcnt.nbytes)
+    assert L2.dsim2_status() == 0
+    assert np.array_equal(gcnt, cnt) and gcnt.sum() > 0
+    assert np.array_equal(out[:, :3].view(np.uint32), pos4.reshape(-1, 4)[:, :3].view(np.uint32))
+    assert np.array_equal(out[:, 3].view(np.uint32), par.reshape(-1, 5)[:, 1].view(np.uint32))
+    assert np.array_equal(sd[:, 2] - 1, par.reshape(-1, 5)[:, 3].astype(np.uint32))
+    for q in (dPos, dSeed, dFib, dCc, dCubes, dDraws, dCnt):
+        L2.freeArray(q)
 
 
 def _mixed_fibers(seed, per_axis=24):
