@@ -178,3 +178,44 @@ def test_fine_lists_reject_bad_grids(engine):
     short = np.zeros(max(1, len(pos) - 1), np.uint32)
     assert lib.dsim_cyl_fine_lists(fp, len(fp) // 4, n, maxfpc, float(L), cc, cubes, 4, start, short, len(short),
                                    C.byref(ent)) != 0   # capacity short
+
+
+def test_fine_lists_keep_repeated_entries(engine):
+    """A fiber listed twice in one cell (the reference's halo lines can do
+    that) is tested twice by the reference; the fine lists keep both list
+    positions, in order, wherever the fiber can act."""
+    lib = engine.native()
+    fp, maxR = _mixed_fibers(5)
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, maxR)
+    k = 4
+    nk = n * k
+    cell = int(np.argmax(cc))
+    cx, cy, cz = cell % n, (cell // n) % n, cell // (n * n)
+    # an entry of that cell whose fiber reaches into it (the reference's halo
+    # also lists fibers that do not)
+    start0, pos0 = _fine_lists(lib, fp, (cc, cubes, n, maxfpc, L), k)
+    own = set()
+    for sz in range(k):
+        for sy in range(k):
+            for sx in range(k):
+                fc = ((cz * k + sz) * nk + (cy * k + sy)) * nk + cx * k + sx
+                own.update(int(j) for j in pos0[start0[fc]:start0[fc + 1]])
+    j0 = min(own)
+    cc = cc.copy()
+    cubes = cubes.copy().reshape(-1, maxfpc)
+    assert cc[cell] < maxfpc
+    cubes[cell, cc[cell]] = cubes[cell, j0]   # the same fiber again, at the end of the list
+    cc[cell] += 1
+    cubes = cubes.reshape(-1)
+    start, pos = _fine_lists(lib, fp, (cc, cubes, n, maxfpc, L), k)
+    seen_both = 0
+    for sz in range(k):
+        for sy in range(k):
+            for sx in range(k):
+                fc = ((cz * k + sz) * nk + (cy * k + sy)) * nk + cx * k + sx
+                lst = pos[start[fc]:start[fc + 1]]
+                has0, hasl = j0 in lst, (cc[cell] - 1) in lst
+                assert has0 == hasl                  # the same fiber: both or neither
+                seen_both += has0
+                assert np.all(np.diff(lst.astype(np.int64)) > 0)
+    assert seen_both > 0
