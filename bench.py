@@ -20,7 +20,8 @@ of the oracle port on a bounded sample.
 
 --impl reference times the reference's CPU algorithm (the oracle port of
 dSim3's cpuIntegrate, all host threads) on a bounded sample of the same
-workload.  Multi-GPU (--gpus N under torchrun): independent replicas, one
+workload; the oracle also builds that arm's mesh arrays and grid (initFibers
+and populateCubes from a mesh file of the workload), so it makes no GPU call.  Multi-GPU (--gpus N under torchrun): independent replicas, one
 per rank, no collective on the data path (weak scaling).
 """
 import argparse
@@ -182,9 +183,10 @@ def peaks():
 # --------------------------------------------------------------------------
 # CPU baseline: the oracle port of dSim3's cpuIntegrate on a bounded sample
 # --------------------------------------------------------------------------
-def cpu_sample(W, m, threads, budget_s=12.0):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
+def device_arrays(W, m):
+    """The reference's mesh arrays for the oracle, from the device mesh: its
+    vertices and grid (pinned equal to initFibers / populateCubes), helpers
+    recomputed in the reference's expression order."""
     start, tri = m.grid()
     counts = np.diff(start.astype(np.int64)).astype(np.uint32)
     maxtpc = int(counts.max())
@@ -192,12 +194,34 @@ def cpu_sample(W, m, threads, budget_s=12.0):
     idx = np.repeat(np.arange(len(counts)), counts)
     off = np.arange(len(tri)) - np.repeat(start[:-1].astype(np.int64), counts)
     dense[idx, off] = tri
-    dense = dense.reshape(-1)
     v, ti = m.arrays()
-    # helpers as the reference computes them (initFibers), from the device's vertices
     H = _helpers(v, W.tube["trgls"].reshape(-1))
+    return v, H, ti, counts, dense.reshape(-1), maxtpc, "mesh, grid and draws as on the GPU"
+
+
+def oracle_arrays(W):
+    """The reference's mesh arrays built on the host by the oracle alone: the
+    workload written as a dSim3 mesh file and read back by the restatement of
+    initFibers, the grid by the restatement of populateCubes."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from dsim_gb300 import substrates as S
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "workload.mesh")
+        S.write_mesh_file(path, W.tube)
+        mo = O.Mesh(path, W.spaceScale)
+    cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, W.numCubes)
+    return (mo.vertices, mo.helpers, mo.triInfo, cc, tic, maxtpc,
+            "mesh read and grid built by the oracle's initFibers / populateCubes")
+
+
+def cpu_sample(W, arrays, threads, budget_s=12.0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    v, H, ti, counts, dense, maxtpc, source = arrays
     p = O.params3(W.stdDevs, W.T2, 0.0, W.dt, W.numCubes, maxtpc)
-    n = 4096 if threads == 1 else 4096 * threads
+    n = min(W.N, 4096 if threads == 1 else 4096 * threads)
     sel = np.random.default_rng(5).choice(W.N, n, replace=False)
     pos = W.pos.reshape(-1, 3)[sel].reshape(-1).copy()
     seed = np.random.default_rng(6).integers(1, 2 ** 32 - 1, 2 * n, dtype=np.uint64).astype(np.uint32)
@@ -217,8 +241,7 @@ def cpu_sample(W, m, threads, budget_s=12.0):
                        float(W.g[0]), float(W.g[1]), float(W.g[2]), float(W.pc), iters, threads)
     el = time.perf_counter() - t0
     rate = n * iters / el
-    return rate, "%d spins x %d steps of the workload (mesh, grid and draws as on the GPU; %.1f s)" % (
-        n, iters, el)
+    return rate, "%d spins x %d steps of the workload (%s; %.1f s)" % (n, iters, source, el)
 
 
 def _helpers(v, trgls):
@@ -446,7 +469,7 @@ def run_ours(args, rank, world):
         res["cylinders"] = run_cylinders(args)
     if rank == 0 and not args.no_cpu:
         threads = 1
-        rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
+        rate, sample = cpu_sample(W, device_arrays(W, m), threads, budget_s=args.cpu_seconds)
         res["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": sample}
     return res
@@ -455,11 +478,10 @@ def run_ours(args, rank, world):
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    from dsim_gb300.engine import DeviceInfo  # noqa: F401  (GPU not used by this arm)
+    # host cores only: the oracle builds the mesh arrays and the grid, no GPU call
     W = Workload(axons=args.axons, spins=args.spins, seed=1)
-    m = make_mesh(W)
     threads = os.cpu_count() or 1
-    rate, sample = cpu_sample(W, m, threads, budget_s=args.cpu_seconds)
+    rate, sample = cpu_sample(W, oracle_arrays(W), threads, budget_s=args.cpu_seconds)
     return {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
