@@ -121,6 +121,17 @@ __host__ __device__ __forceinline__ uint32_t pack_info(uint32_t membrane, uint32
     return (membrane & 3u) | (fiber << 2);
 }
 
+// Region of a dSim2 spin (0 core, 1 myelin, 2 outside) from words 2 and 3 of
+// its seed record.  The engine stores imo + 1 in word 2.  The reference's
+// assignSeeds (dSim2/src/spinSystem.cpp:1129-1151) leaves word 2 at 0 and
+// puts the nearest fiber in word 3 for a spin inside a fiber, UINT_MAX for one
+// outside; such a record reads as core or outside.  A word 2 above 3 gives a
+// region above 2: the step treats it as outside, and the signal sums region 3
+// in its own slot and any higher region in the total only.
+__host__ __device__ __forceinline__ uint32_t dsim2_region(uint32_t w2, uint32_t w3) {
+    return (w2 == 0u) ? ((w3 != 0xFFFFFFFFu) ? 0u : 2u) : (w2 - 1u);
+}
+
 }  // namespace dsim
 
 #define DSIM_CUDA_TRY(expr)                                  \

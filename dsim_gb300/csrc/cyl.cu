@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(256) k_cyl_step(CylDev g, CylStepArgs a, CylSp
     float x = P.x, y = P.y, z = P.z, phase = P.w;
     float mag = S.mag ? S.mag[i] : 1.0f;
     uint32_t nearest = sd4.w;
-    uint32_t imo = (sd4.z == 0u) ? ((nearest != 0xFFFFFFFFu) ? 0u : 2u) : (sd4.z - 1u);
+    uint32_t imo = dsim2_region(sd4.z, nearest);
     if (imo < 2 && nearest >= g.nF) imo = 2;  // no valid fiber: treat as outside
     uint32_t nrej = 0, nperm = 0, status = 0;
     uint32_t k0 = a.key0, k1 = a.key1;

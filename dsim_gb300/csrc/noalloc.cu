@@ -21,11 +21,11 @@
 // device, so calls that could overlap (different streams, or host threads
 // without ordering) race on it; callers serialise them, e.g. on one stream.
 //
-// Setup: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (that device current) and caches it; later calls reuse
-// it.  Make the first call before any stream capture.
+// Setup: every call looks up the array's device address on the current device
+// with cudaGetSymbolAddress (it allocates nothing), so an address never
+// outlives a cudaDeviceReset that reloads the module.  The first call on a
+// device also loads the module there: make it before any stream capture.
 #include <cstdint>
-#include <mutex>
 
 #pragma GCC visibility push(default)
 #include "../../include/dsim.h"
@@ -39,33 +39,20 @@ static constexpr uint32_t kNaVals = 15;            // (X, Y, n) x (total + 4 com
 static constexpr uint32_t kNaSpinsPerBlock = 2048;  // 256 threads x 8 spins per partial record
 static constexpr uint32_t kNaMaxBlocks = 8192;
 static constexpr uint32_t kNaMaxSpins = kNaSpinsPerBlock * kNaMaxBlocks;
-static constexpr int kNaMaxDevices = 64;
-
 static __device__ __align__(256) double g_signal_scratch[kNaMaxBlocks * kNaVals];
 
-static std::mutex g_scratch_mu;
-static double* g_scratch_addr[kNaMaxDevices];
-
-// device address of the scratch array for the current device (set up once)
+// device address of the scratch array on the current device
 static int scratch_for_current_device(double** out) {
-    int dev = -1;
-    DSIM_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNaMaxDevices) {
-        set_last_error(kErrInvalid, "dsim_signal_noalloc: device %d outside 0..%d", dev, kNaMaxDevices - 1);
-        return kErrInvalid;
+    double* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_signal_scratch);
+    if (e != cudaSuccess || !ptr) {
+        int dev = -1;
+        cudaGetDevice(&dev);
+        set_last_error(kErrCuda, "dsim_signal_noalloc: cudaGetSymbolAddress of the scratch on device %d: %s", dev,
+                       cudaGetErrorString(e));
+        return kErrCuda;
     }
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
-        double* ptr = nullptr;
-        cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_signal_scratch);
-        if (e != cudaSuccess || !ptr) {
-            set_last_error(kErrCuda, "dsim_signal_noalloc: cudaGetSymbolAddress of the scratch on device %d: %s",
-                           dev, cudaGetErrorString(e));
-            return kErrCuda;
-        }
-        g_scratch_addr[dev] = ptr;
-    }
-    *out = g_scratch_addr[dev];
+    *out = ptr;
     return kOk;
 }
 

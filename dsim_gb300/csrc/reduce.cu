@@ -21,22 +21,28 @@ template <int LAYOUT>
 __device__ __forceinline__ bool load_sig(const SpinsDev& S, uint32_t i, double region, double& m,
                                          double& ph, uint32_t& comp) {
     float x, y, z;
+    // comp above 3 (outside the reference's four compartments) is counted in
+    // the total only: the caller sees it as n_total - sum of compartment n.
     if (LAYOUT == kLayoutSoA) {
         x = S.x[i]; y = S.y[i]; z = S.z[i];
         m = S.mag[i]; ph = S.phase[i];
-        comp = S.meta[i] & 3u;
+        comp = S.meta[i] & 0xFFu;
     } else if (LAYOUT == kLayoutAoS) {
         x = S.x[3 * i]; y = S.x[3 * i + 1]; z = S.x[3 * i + 2];
         const unsigned char* rec = reinterpret_cast<const unsigned char*>(S.meta) + 12 * (size_t)i;
         m = *reinterpret_cast<const float*>(rec);
         ph = *reinterpret_cast<const float*>(rec + 4);
-        comp = rec[8] & 3u;
+        comp = rec[8];
     } else {  // cylinder layout: x = float4 {x, y, z, phase}, mag optional
         const float4 p = reinterpret_cast<const float4*>(S.x)[i];
         x = p.x; y = p.y; z = p.z; ph = p.w;
         m = S.mag ? (double)S.mag[i] : 1.0;
-        uint32_t w = S.meta ? S.meta[4 * i + 2] : 0u;
-        comp = (w == 0u) ? 0u : ((w - 1u) & 3u);
+        if (S.meta) {
+            const uint2 w = reinterpret_cast<const uint2*>(S.meta)[2 * (size_t)i + 1];
+            comp = dsim2_region(w.x, w.y);
+        } else {
+            comp = 0u;
+        }
     }
     if (region > 0.0)
         return ((double)x > -region && (double)x < region && (double)y > -region &&

@@ -205,7 +205,10 @@ int dsim_cyl_run(dsim_cyl* c, dsim_spins* s, const dsim_cyl_params* p, const flo
 
 /* Ensemble signal in FP64: out[3c + 0..2] = {sum m cos(phi), sum m sin(phi), n}
  * for c = 0 (all spins) and c = 1 + compartment (mesh) / 1 + imo (cylinders).
- * region > 0 keeps spins with |x|,|y|,|z| < region (dSim2 uses 0.8). */
+ * region > 0 keeps spins with |x|,|y|,|z| < region (dSim2 uses 0.8).
+ * A spin whose compartment index is above 3 is counted in c = 0 only, so
+ * out[2] minus the four compartment counts is the number of such spins (the
+ * reference's arrays hold four compartments and would overrun). */
 int dsim_signal(dsim_spins* s, double region, double out[15]);
 
 /* dsim_signal over the reference's own device spin arrays, allocating
@@ -216,12 +219,15 @@ int dsim_signal(dsim_spins* s, double region, double out[15]);
  *   layout DSIM_SIGNAL_DSIM3: pos = float3[N], spinRecords = spinData[N]
  *          (12 B: mag, phase, compartment byte, pad, fiber u16)
  *   layout DSIM_SIGNAL_DSIM2: pos = float4[N] {x, y, z, phase},
- *          spinRecords = uint4 seeds[N] (imo + 1 in word 2) or NULL; mag = 1
+ *          spinRecords = uint4 seeds[N] or NULL; mag = 1.  Word 2 holds
+ *          imo + 1, or 0 as the reference's assignSeeds leaves it, when
+ *          word 3 (nearest fiber, UINT_MAX outside) gives core or outside
  * out: DEVICE pointer to 15 doubles, same meaning as dsim_signal; written
  * asynchronously on `stream` (a cudaStream_t; NULL = legacy default stream).
  * Scratch is a fixed array inside the library (983,040 bytes): N above
- * 16,777,216 returns DSIM_ETOOLARGE.  Nothing must start at zero.  The first
- * call on a device looks up the scratch address; make it before any stream
+ * 16,777,216 returns DSIM_ETOOLARGE.  Nothing must start at zero.  Every
+ * call looks up the scratch address (allocating nothing); the first call on a
+ * device loads the library's module there, so make it before any stream
  * capture.  Calls that may overlap in time race on the one scratch array:
  * serialise them (e.g. issue them on one stream). */
 #define DSIM_SIGNAL_DSIM3 1

@@ -116,6 +116,74 @@ def test_noalloc_signal_dsim2_arrays_match_dsim_signal(engine):
         d.free()
 
 
+def test_noalloc_signal_dsim2_fresh_reference_seeds(engine):
+    """Seed records as the reference's assignSeeds leaves them before the
+    first step (dSim2/src/spinSystem.cpp:1129-1151): word 2 = 0, word 3 = the
+    nearest fiber for a spin inside one, UINT_MAX outside.  They must read as
+    core (0) and outside (2), as the step kernel reads them."""
+    from dsim_gb300 import _lib
+    from dsim_gb300.engine import Spins
+    L = _lib.native()
+    N = 70_001
+    pos, _, ph, _, _ = _spins(N, seed=11)
+    rng = np.random.default_rng(12)
+    inside = rng.random(N) < 0.4
+    w3 = np.where(inside, rng.integers(0, 64, N), 0xFFFFFFFF).astype(np.uint32)
+    s = Spins(N)
+    s.set_cyl(pos, np.ones(N, np.float32), ph, np.where(inside, 0, 2).astype(np.uint32),
+              np.where(inside, w3, 0).astype(np.uint32))
+    pos4 = np.concatenate([pos, ph[:, None]], axis=1).astype(np.float32)
+    seeds = np.zeros((N, 4), np.uint32)
+    seeds[:, :2] = rng.integers(1, 2 ** 32 - 1, (N, 2), dtype=np.uint64).astype(np.uint32)
+    seeds[:, 3] = w3
+    d = _Dev()
+    try:
+        dpos, dseed = d.put(pos4), d.put(seeds)
+        dout = d.put(np.zeros(15, np.float64))
+        for region in (0.0, 0.8):
+            want = s.signal(region)
+            assert want[2, 2] == 0 and want[1, 2] > 0 and want[3, 2] > 0
+            for _ in range(2):
+                rc = L.dsim_signal_noalloc(dpos, dseed, N, DSIM_SIGNAL_DSIM2, region, dout, None)
+                assert rc == 0, L.dsim_last_error()
+                _close(d.get(dout, np.zeros(15, np.float64)), want)
+    finally:
+        d.free()
+
+
+def test_noalloc_signal_counts_compartments_above_3_in_the_total_only(engine):
+    """The reference sizes its sums by its four compartments
+    (dSim3/src/spinSystem.cpp:1452-1500); an index above 3 is counted in the
+    total and in no compartment, so the caller can see it as the difference."""
+    from dsim_gb300 import _lib
+    L = _lib.native()
+    N = 50_000
+    pos, mag, ph, _, fib = _spins(N, seed=13)
+    comp = np.random.default_rng(14).integers(0, 7, N).astype(np.uint8)
+    rec = np.zeros(N, np.dtype([("mag", "<f4"), ("phase", "<f4"), ("comp", "u1"), ("pad", "u1"),
+                                ("fiber", "<u2")]))
+    rec["mag"], rec["phase"], rec["comp"], rec["fiber"] = mag, ph, comp, fib
+    X = mag.astype(np.float64) * np.cos(ph.astype(np.float64))
+    Y = mag.astype(np.float64) * np.sin(ph.astype(np.float64))
+    want = np.zeros((5, 3))
+    want[0] = X.sum(), Y.sum(), N
+    for c in range(4):
+        sel = comp == c
+        want[1 + c] = X[sel].sum(), Y[sel].sum(), sel.sum()
+    d = _Dev()
+    try:
+        dpos, drec = d.put(pos), d.put(rec)
+        dout = d.put(np.zeros(15, np.float64))
+        for _ in range(2):
+            rc = L.dsim_signal_noalloc(dpos, drec, N, DSIM_SIGNAL_DSIM3, 0.0, dout, None)
+            assert rc == 0, L.dsim_last_error()
+            got = d.get(dout, np.zeros(15, np.float64)).reshape(5, 3)
+            _close(got, want)
+            assert got[0, 2] - got[1:, 2].sum() == (comp > 3).sum() > 0
+    finally:
+        d.free()
+
+
 def test_noalloc_signal_rejects_more_spins_than_its_scratch(engine):
     """Rejected on the host before any launch, so the (unused) pointers are
     never dereferenced."""
