@@ -166,6 +166,7 @@ def _declare_batch(L):
         "dsim_batch_run": (i32, [VP]),
         "dsim_batch_job_status": (i32, [VP, u32, C.POINTER(u32), C.POINTER(i32)]),
         "dsim_batch_signal": (i32, [VP, u32, F32, u32, F64]),
+        "dsim_batch_signal_region": (i32, [VP, u32, F32, u32, C.c_double, F64]),
         "dsim_batch_get": (i32, [VP, u32, OF32, OF32, OF32, OU8, OU32]),
         "dsim_batch_counts": (i32, [VP, u32, U64]),
         "dsim_batch_status": (u32, [VP]),

@@ -28,7 +28,7 @@ UNITS = ["mesh.cu", "accel.cu", "coop.cu", "flat.cu", "cyl.cu", "scan.cu", "redu
 LIBS = {
     "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "flat", "cyl", "scan", "reduce", "noalloc", "batch", "serve", "compartments", "simulate"],
     "libdsim3.so": ["compat3", "mesh", "accel", "flat", "scan"],
-    "libdsim2.so": ["compat2", "cyl"],
+    "libdsim2.so": ["compat2", "cyl", "scan"],
 }
 
 

@@ -620,7 +620,7 @@ __global__ void k_batch_gather64(BatchSpins S, uint32_t slot0, uint32_t len, dou
 static constexpr int kSigThreads = 256;
 __global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint32_t slot0, uint32_t len,
                                                               const double* __restrict__ kg, uint32_t nG,
-                                                              double* partials) {
+                                                              double region, double* partials) {
     __shared__ double sh[kSigThreads / 32][15];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t gi = 0; gi < nG; gi++) {
@@ -631,6 +631,10 @@ __global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint
         for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
             const uint32_t i = slot0 + k;
             if (S.u[U_ID][i] == 0xFFFFFFFFu) continue;
+            if (region > 0.0) {  // dSim2's readout box (dSim2/src/spinSystem.cpp:944-978)
+                const double x = S.f[F_X][i], y = S.f[F_Y][i], z = S.f[F_Z][i];
+                if (!(x > -region && x < region && y > -region && y < region && z > -region && z < region)) continue;
+            }
             const double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
             const double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
             const double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
@@ -1197,8 +1201,16 @@ int dsim_batch_job_status(dsim_batch* b, uint32_t jobId, uint32_t* stepsDone, in
 }
 
 int dsim_batch_signal(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG, double* out) {
+    return dsim_batch_signal_region(b, jobId, gradScaled, nG, 0.0, out);
+}
+
+int dsim_batch_signal_region(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG, double region,
+                             double* out) {
     BatchJob* j = b ? find_job(b, jobId) : nullptr;
-    if (!j || !gradScaled || !out || nG == 0) { set_last_error(kErrInvalid, "dsim_batch_signal: bad argument"); return kErrInvalid; }
+    if (!j || !gradScaled || !out || nG == 0 || !(region >= 0.0)) {
+        set_last_error(kErrInvalid, "dsim_batch_signal: bad argument");
+        return kErrInvalid;
+    }
     const uint32_t nb = std::min<uint32_t>(608u, (j->pad + kSigThreads * 4 - 1) / (kSigThreads * 4));
     std::vector<double> kg(3 * (size_t)nG);
     // phase = phaseConstant * (g . M); the job keeps phaseConstant in its descriptor
@@ -1214,7 +1226,7 @@ int dsim_batch_signal(dsim_batch* b, uint32_t jobId, const float* gradScaled, ui
     b->bytes -= kg.size() * 8 + (size_t)nb * nG * 15 * 8 + (size_t)nG * 15 * 8;
     cudaError_t e = cudaMemcpyAsync(dk, kg.data(), kg.size() * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) {
-        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, dp);
+        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, region, dp);
         k_batch_signal_final<<<(nG * 15 + 127) / 128, 128, 0, b->st>>>(dp, nb, nG, dout);
         e = cudaGetLastError();
     }

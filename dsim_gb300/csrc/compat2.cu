@@ -36,14 +36,15 @@ const char* last_error_message() { return g_last_error.c_str(); }
 using namespace dsim;
 
 namespace {
-// The fine filter grid of the last grid arrays seen, with host copies of
-// their contents to detect a change.
+// The fine filter grid of the last grid arrays seen, with the device content
+// hashes of the arrays it was built from to detect a change.
 struct FineCache {
     bool valid = false;
     uint32_t n = 0, maxFPC = 0, nF = 0, k = 0;
     float L = 0.0f;
-    std::vector<float> fib;
-    std::vector<uint32_t> cc, cubes;
+    const void* ptrs[3] = {nullptr, nullptr, nullptr};  // fibers, cube counts, cube lists
+    uint64_t hash[3] = {0, 0, 0};                        // their contents when built
+    unsigned long long* hashDev = nullptr;               // 3 device words (kept across releases)
     uint32_t* start = nullptr;
     float4* rec = nullptr;
     uint32_t* pos = nullptr;
@@ -71,43 +72,49 @@ State& S() {
 }
 void fail(int code) { S().last_status = code; }
 
-// Points g at the fine filter grid of its arrays (rebuilt when their contents
-// differ from the last call's); false leaves g on the full list scan.
+// Points g at the fine filter grid of its arrays; false leaves g on the full
+// list scan.  Each call hashes the three arrays on the device (one read each,
+// nothing copied back); only when a pointer, a size or a hash differs from
+// the cached grid's are the arrays copied to the host and the lists rebuilt.
 bool fine_grid(State& s, CylDev& g) {
     if (s.fineMode == 0 || s.fineMode == 1) return false;
     FineCache& c = s.fine;
-    std::vector<float> fib((size_t)g.nF * 4);
-    if (cudaMemcpy(fib.data(), g.fibers, fib.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    uint32_t k = 0;
-    if (s.fineMode >= 2) {
-        k = (uint32_t)s.fineMode;
-    } else {
-        double maxR = 0.0;
-        for (uint32_t i = 0; i < g.nF; i++) {
-            const double w = fib[4 * (size_t)i + 3];
-            if (w > 0.0 && std::isfinite(w)) maxR = std::max(maxR, std::sqrt(w));
-        }
-        k = cyl_fine_size(g.n, g.L, maxR);
-    }
-    if (k < 2 || (uint64_t)(g.n * k) * (g.n * k) * (g.n * k) > (1ull << 24)) return false;
     const size_t ncell = (size_t)g.n * g.n * g.n;
-    std::vector<uint32_t> cc(ncell), cubes(ncell * g.maxFPC);
-    if (cudaMemcpy(cc.data(), g.cube_count, cc.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
-        (!cubes.empty() && cudaMemcpy(cubes.data(), g.cubes, cubes.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+    if (!c.hashDev && cudaMalloc(&c.hashDev, 3 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    auto bytes_equal = [](const auto& a, const auto& b) {
-        return a.size() == b.size() && (a.empty() || memcmp(a.data(), b.data(), a.size() * sizeof(a[0])) == 0);
-    };
-    const bool same = c.valid && c.k == k && c.n == g.n && c.maxFPC == g.maxFPC && c.nF == g.nF &&
-                      memcmp(&c.L, &g.L, 4) == 0 && bytes_equal(c.fib, fib) && bytes_equal(c.cc, cc) &&
-                      bytes_equal(c.cubes, cubes);
+    const void* ptrs[3] = {g.fibers, g.cube_count, g.cubes};
+    const size_t nw[3] = {(size_t)g.nF * 4, ncell, ncell * g.maxFPC};
+    uint64_t h[3] = {0, 0, 0};
+    if (hash_device_arrays(ptrs, nw, 3, c.hashDev, h, 0) != kOk) {
+        cudaGetLastError();
+        return false;
+    }
+    const bool same = c.valid && c.n == g.n && c.maxFPC == g.maxFPC && c.nF == g.nF && memcmp(&c.L, &g.L, 4) == 0 &&
+                      memcmp(c.ptrs, ptrs, sizeof(ptrs)) == 0 && memcmp(c.hash, h, sizeof(h)) == 0;
     if (!same) {
         c.release();
+        std::vector<float> fib((size_t)g.nF * 4);
+        std::vector<uint32_t> cc(ncell), cubes(ncell * g.maxFPC);
+        if ((!fib.empty() && cudaMemcpy(fib.data(), g.fibers, fib.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess) ||
+            cudaMemcpy(cc.data(), g.cube_count, cc.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            (!cubes.empty() && cudaMemcpy(cubes.data(), g.cubes, cubes.size() * 4, cudaMemcpyDeviceToHost) != cudaSuccess)) {
+            cudaGetLastError();
+            return false;
+        }
+        uint32_t k = 0;
+        if (s.fineMode >= 2) {
+            k = (uint32_t)s.fineMode;
+        } else {
+            double maxR = 0.0;
+            for (uint32_t i = 0; i < g.nF; i++) {
+                const double w = fib[4 * (size_t)i + 3];
+                if (w > 0.0 && std::isfinite(w)) maxR = std::max(maxR, std::sqrt(w));
+            }
+            k = cyl_fine_size(g.n, g.L, maxR);
+        }
+        if (k < 2 || (uint64_t)(g.n * k) * (g.n * k) * (g.n * k) > (1ull << 24)) return false;
         std::vector<uint32_t> start, pos;
         std::vector<float> rec;
         // a grid the lists cannot describe (an index >= nF, a count above
@@ -125,7 +132,8 @@ bool fine_grid(State& s, CylDev& g) {
             return false;
         }
         c.k = k; c.n = g.n; c.maxFPC = g.maxFPC; c.nF = g.nF; c.L = g.L;
-        c.fib.swap(fib); c.cc.swap(cc); c.cubes.swap(cubes);
+        memcpy(c.ptrs, ptrs, sizeof(ptrs));
+        memcpy(c.hash, h, sizeof(h));
         c.valid = true;
     }
     g.fine_start = c.start; g.fine_rec = c.rec; g.fine_pos = c.pos;

@@ -156,6 +156,10 @@ int launch_compartments(const MeshDev& g, const AccelDev& acc, const SpinsSorted
                         uint32_t* moved, cudaStream_t st);
 
 // ---- scan.cu --------------------------------------------------------------
+// content hashes of n device arrays of 32-bit words (nwords[k] words at
+// ptrs[k]) into hostOut[n]; dOut is n device words of scratch.  Synchronous.
+int hash_device_arrays(const void* const* ptrs, const size_t* nwords, int n, unsigned long long* dOut,
+                       uint64_t* hostOut, cudaStream_t st);
 // exclusive prefix sum: out[0..n] (out[n] = total); scratch >= scan_scratch_words(n)
 size_t scan_scratch_words(uint32_t n);
 int launch_scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* scratch,

@@ -1,6 +1,8 @@
 // scan.cu -- device-wide exclusive prefix sum of uint32 counts, used by the
 // grid builders (count -> offsets -> fill).  Three launches: per-block scan
 // with block totals, one-block scan of the totals, offset add.
+#include <algorithm>
+
 #include "common.cuh"
 #include "engine.h"
 
@@ -91,6 +93,43 @@ int launch_scan_exclusive(const uint32_t* in, uint32_t* out, uint32_t n, uint32_
     k_scan_totals<<<1, kScanThreads, 0, st>>>(scratch, ntiles, out, n);
     k_scan_add<<<(n + 255) / 256, 256, 0, st>>>(out, n, scratch);
     DSIM_CUDA_TRY(cudaGetLastError());
+    return kOk;
+}
+
+// ---- content hash of device arrays ------------------------------------------
+// Sum over i of mix64(word_i ^ (i * golden) + salt), wrapping: one read of
+// the array, order-sensitive through the index, deterministic.  The C-ABI
+// drop-ins compare these per call to notice a caller that rewrote bound
+// arrays in place, without copying them back.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void __launch_bounds__(256) k_hash_words(const uint32_t* __restrict__ p, size_t n,
+                                                    unsigned long long salt, unsigned long long* out) {
+    unsigned long long acc = 0ull;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        acc += mix64(((unsigned long long)__ldg(p + i) ^ ((unsigned long long)i * 0x9E3779B97F4A7C15ull)) + salt);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xFFFFFFFFu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
+
+int hash_device_arrays(const void* const* ptrs, const size_t* nwords, int n, unsigned long long* dOut,
+                       uint64_t* hostOut, cudaStream_t st) {
+    if (n <= 0) return kOk;
+    DSIM_CUDA_TRY(cudaMemsetAsync(dOut, 0, (size_t)n * 8, st));
+    for (int k = 0; k < n; k++) {
+        if (!ptrs[k] || nwords[k] == 0) continue;
+        const size_t blocks = std::min<size_t>(608, (nwords[k] + 255) / 256);
+        k_hash_words<<<(unsigned)blocks, 256, 0, st>>>(static_cast<const uint32_t*>(ptrs[k]), nwords[k],
+                                                        0x632BE59BD9B4E019ull * (unsigned long long)(k + 1), dOut + k);
+    }
+    DSIM_CUDA_TRY(cudaGetLastError());
+    DSIM_CUDA_TRY(cudaMemcpyAsync(hostOut, dOut, (size_t)n * 8, cudaMemcpyDeviceToHost, st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(st));
     return kOk;
 }
 

@@ -692,7 +692,7 @@ int dsim_simulate(const char* cfgPath, uint64_t seed, uint32_t flags, double* si
             for (size_t q = 0; q < members.size(); q++)
                 for (int k = 0; k < 3; k++) gs[3 * q + k] = rows[6 * members[q] + 3 + k] * 1e-9f * ss;
             std::vector<double> out(15 * members.size());
-            rc = dsim_batch_signal(b, job, gs.data(), (uint32_t)members.size(), out.data());
+            rc = dsim_batch_signal_region(b, job, gs.data(), (uint32_t)members.size(), region, out.data());
             elapsed += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             for (size_t q = 0; q < members.size() && !rc; q++)
                 for (int k = 0; k < 5; k++) signals[5 * (size_t)members[q] + k] = sig_of(&out[15 * q], k);

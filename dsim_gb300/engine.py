@@ -400,10 +400,12 @@ class Batch:
         check(native().dsim_batch_job_status(self.h, int(job), C.byref(s), C.byref(d)))
         return s.value, bool(d.value)
 
-    def signal(self, job, grad_scaled):
+    def signal(self, job, grad_scaled, region=0.0):
+        """FP64 sums (nG, 5, 3) of X, Y, n; region > 0 keeps spins inside
+        +-region (dSim2 reads +-0.8)."""
         g = np.ascontiguousarray(grad_scaled, F).reshape(-1, 3)
         out = np.zeros(15 * len(g), np.float64)
-        check(native().dsim_batch_signal(self.h, int(job), g.reshape(-1), len(g), out))
+        check(native().dsim_batch_signal_region(self.h, int(job), g.reshape(-1), len(g), float(region), out))
         return out.reshape(len(g), 5, 3)
 
     def get(self, job, n):

@@ -159,18 +159,22 @@ def beaded_tubes(n_axons=400, verts_per_ring=32, ring_spacing=0.5, length=50.0, 
 
 def write_mesh_file(path, mesh):
     """dSim3 mesh fiber file: V block, T block, then per fiber and membrane a
-    block 'A<k>' / 'M<k>' / 'G<k>' listing its triangle indices."""
-    V, T, mem, fib = mesh["vertices"], mesh["trgls"], mesh["membrane"], mesh["fiber"]
+    block 'A<k>' / 'M<k>' / 'G<k>' listing its triangle indices (ascending).
+    Vertices are written with 9 significant digits, so a float32 vertex reads
+    back as the same float."""
+    V, T = np.asarray(mesh["vertices"]), np.asarray(mesh["trgls"])
+    mem, fib = np.asarray(mesh["membrane"]), np.asarray(mesh["fiber"])
     letters = {0: "A", 1: "M", 2: "G"}
+    order = np.lexsort((np.arange(len(fib)), mem, fib))
+    key = fib[order].astype(np.int64) * 4 + mem[order]
+    cuts = np.nonzero(np.diff(key))[0] + 1
     with open(path, "w") as f:
         f.write("V\n")
-        np.savetxt(f, V, fmt="%.7g")
+        np.savetxt(f, V, fmt="%.9g")
         f.write("T\n")
         np.savetxt(f, T, fmt="%d")
-        for fi in np.unique(fib):
-            for m in (0, 1, 2):
-                idx = np.nonzero((fib == fi) & (mem == m))[0]
-                if len(idx) == 0:
-                    continue
-                f.write("%s%d\n" % (letters[m], fi))
-                np.savetxt(f, idx, fmt="%d")
+        for idx in np.split(order, cuts):
+            if len(idx) == 0:
+                continue
+            f.write("%s%d\n" % (letters[int(mem[idx[0]])], int(fib[idx[0]])))
+            f.write("\n".join(map(str, idx.tolist())) + "\n")

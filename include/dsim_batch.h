@@ -103,6 +103,12 @@ int dsim_batch_job_status(dsim_batch* b, uint32_t jobId, uint32_t* stepsDone, in
  * dsim_signal (c = 0 all, 1 + compartment).  Synchronous. */
 int dsim_batch_signal(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG,
                       double* out);
+/* dsim_batch_signal over the spins with |x|, |y|, |z| < region only (region 0:
+ * every spin).  dSim2's getMrSignal reads the box +-0.8
+ * (dSim2/src/spinSystem.cpp:944-978); the simulate call passes 0.8 for
+ * cylinder configurations. */
+int dsim_batch_signal_region(dsim_batch* b, uint32_t jobId, const float* gradScaled, uint32_t nG,
+                             double region, double* out);
 /* a job's spins in spin order: pos3, mag, moments (M and its compensation,
  * 6 per spin), compartment, fiber (any pointer may be NULL).  Synchronous. */
 int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float* moments6,

@@ -105,6 +105,22 @@ uint32_t or3_integrate_f64_moments(const or3_params* p, uint32_t N, double* pos,
                                    const double* waves, uint32_t iterations, const float* draws,
                                    double* moments, uint32_t* counts, int nthreads);
 
+/* The reference's walk for nG gradient runs at once.  The walk (positions,
+ * compartments, magnitudes) does not depend on the gradient, so one walk
+ * with the reference's own MWC draws (seed[2N], or replay draws) serves every
+ * run: after each step, for run k, phases[i*nG + k] += (gx*x + gy*y + gz*z)*pc
+ * with g = wave[t] * grads[k] in float -- the reference's phase update
+ * (spinKernelCpu.cpp:490) for the gradient the sequencer passes at step t
+ * (wave 1, 0, -1 for PGSE: diffusion.cpp:553-625).  OpenMP over spins (each
+ * spin's MWC stream is its own, so the result does not depend on nthreads). */
+uint32_t or3_integrate_multi(const or3_params* p, uint32_t N, float* pos, uint32_t* seed,
+                             float* mag, uint8_t* comp, uint16_t* fiber,
+                             const float* vertices, const float* helpers,
+                             const uint32_t* triInfo, const uint32_t* cubeCounter,
+                             const uint32_t* trianglesInCubes, uint32_t nG, const float* grads,
+                             const float* wave, float phaseConstant, uint32_t iterations,
+                             const float* draws, float* phases, uint32_t* counts, int nthreads);
+
 /* getMrSignal(double[]) spinSystem.cpp:1452-1500: out[0]=total, out[1+c]=c */
 void or3_signal(uint32_t N, const float* mag, const float* phase, const uint8_t* comp,
                 double out[5]);
@@ -143,6 +159,16 @@ void or2_integrate(const or2_params* p, uint32_t N, float* pos4, uint32_t* seed4
                    const uint32_t* cubes, float gx, float gy, float gz,
                    float phaseConstant, uint32_t iterations, const float* draws,
                    float* drawsOut, uint32_t* counts);
+
+/* or2_integrate for nG gradient runs at once (see or3_integrate_multi):
+ * one walk with the reference's MWC draws (seed4 words 0-1) or replay draws;
+ * phases[i*nG + k] += (gx*x + gy*y + gz*z)*pc with g = wave[t] * grads[k]
+ * (dSim2/src/spinKernelCpu.cpp:636).  OpenMP over spins. */
+void or2_integrate_multi(const or2_params* p, uint32_t N, float* pos4, uint32_t* seed4,
+                         float* params5, const float* fiberPos, const uint32_t* cubeCounter,
+                         const uint32_t* cubes, uint32_t nG, const float* grads, const float* wave,
+                         float phaseConstant, uint32_t iterations, const float* draws,
+                         float* phases, uint32_t* counts, int nthreads);
 
 /* getMrSignal() dSim2/src/spinSystem.cpp:944-978 (spins inside +-0.8 only) */
 double or2_signal(uint32_t N, const float* pos4, const float* params5);

@@ -109,6 +109,13 @@ def _declare(L):
                                             C.c_uint32, P_F64, P_U32, P_U32, P_U32, P_U32, C.c_uint32,
                                             P_F64, C.c_uint32, P_F32, P_F64, _opt(P_U32), C.c_int]
     L.or3_integrate_f64_moments.restype = C.c_uint32
+    L.or3_integrate_multi.argtypes = [C.POINTER(Params3), C.c_uint32, P_F32, P_U32, P_F32, P_U8, P_U16,
+                                      P_F32, P_F32, P_U32, P_U32, P_U32, C.c_uint32, P_F32, P_F32,
+                                      C.c_float, C.c_uint32, _opt(P_F32), P_F32, _opt(P_U32), C.c_int]
+    L.or3_integrate_multi.restype = C.c_uint32
+    L.or2_integrate_multi.argtypes = [C.POINTER(Params2), C.c_uint32, P_F32, P_U32, P_F32, P_F32, P_U32,
+                                      P_U32, C.c_uint32, P_F32, P_F32, C.c_float, C.c_uint32, _opt(P_F32),
+                                      P_F32, _opt(P_U32), C.c_int]
     L.or3_signal.argtypes = [C.c_uint32, P_F32, P_F32, P_U8, P_F64]
     L.or2_load_fibers.argtypes = [C.c_char_p, C.c_float, _opt(P_F32), C.POINTER(C.c_float)]
     L.or2_load_fibers.restype = C.c_int
@@ -197,6 +204,36 @@ def integrate3(p, pos, seed, mag, phase, comp, fiber, vertices, helpers, triInfo
                                  float(phaseConstant), iterations, d,
                                  None if dout is None else dout.reshape(-1), counts)
     return capped, dout
+
+
+def integrate3_multi(p, pos, seed, mag, comp, fiber, vertices, helpers, triInfo, cc, tic, grads, wave,
+                     phaseConstant, draws=None, counts=None, nthreads=None):
+    """One dSim3 walk (MWC draws from `seed`, or replay `draws`) giving the
+    reference's phase for every gradient run: returns phases [N][nG].  pos,
+    seed, mag, comp, fiber are updated in place; wave[t] scales grads at step t."""
+    N = len(mag)
+    g = np.ascontiguousarray(grads, np.float32).reshape(-1, 3)
+    w = np.ascontiguousarray(wave, np.float32)
+    ph = np.zeros(N * len(g), np.float32)
+    d = None if draws is None else np.ascontiguousarray(draws, np.float32).reshape(-1)
+    capped = lib().or3_integrate_multi(C.byref(p), N, pos, seed, mag, comp, fiber, vertices, helpers, triInfo, cc,
+                                       tic, len(g), g.reshape(-1), w, float(phaseConstant), len(w), d, ph, counts,
+                                       int(nthreads or os.cpu_count() or 1))
+    return capped, ph.reshape(N, len(g))
+
+
+def integrate2_multi(p, pos4, seed4, params5, fiberPos, cc, cubes, grads, wave, phaseConstant, draws=None,
+                     counts=None, nthreads=None):
+    """One dSim2 walk giving the reference's phase for every gradient run:
+    returns phases [N][nG]; pos4, seed4, params5 are updated in place."""
+    N = len(pos4) // 4
+    g = np.ascontiguousarray(grads, np.float32).reshape(-1, 3)
+    w = np.ascontiguousarray(wave, np.float32)
+    ph = np.zeros(N * len(g), np.float32)
+    d = None if draws is None else np.ascontiguousarray(draws, np.float32).reshape(-1)
+    lib().or2_integrate_multi(C.byref(p), N, pos4, seed4, params5, fiberPos, cc, cubes, len(g), g.reshape(-1), w,
+                              float(phaseConstant), len(w), d, ph, counts, int(nthreads or os.cpu_count() or 1))
+    return ph.reshape(N, len(g))
 
 
 def signal3(mag, phase, comp):

@@ -347,3 +347,38 @@ double or2_signal(uint32_t N, const float* pos4, const float* params5) {
     }
     return sqrt(X * X + Y * Y) / (double)n;
 }
+
+void or2_integrate_multi(const or2_params* P, uint32_t N, float* pos4, uint32_t* seed4, float* params5,
+                         const float* fiberPos, const uint32_t* cc, const uint32_t* cubes, uint32_t nG,
+                         const float* grads, const float* wave, float phaseConstant, uint32_t iterations,
+                         const float* draws, float* phases, uint32_t* counts, int nthreads) {
+    float dt = P->deltaTime;
+    /* cpuIntegrateSystem, dSim2/src/spinKernelCpu.cpp:2-20 */
+    float intraSd = sqrtf(2.0f * P->intraAdcScaled * dt);
+    float extraSd = sqrtf(2.0f * P->extraAdcScaled * dt);
+    float myelinSd = sqrtf(2.0f * P->myelinAdcScaled * dt);
+    float inRadPropSq = P->innerRadiusProportion * P->innerRadiusProportion;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (uint32_t i = 0; i < N; i++) {
+        float* ph = phases + (size_t)i * nG;
+        for (uint32_t it = 0; it < iterations; it++) {
+            float d[4];
+            if (draws) {
+                const float* src = draws + ((size_t)it * N + i) * 4;
+                d[0] = src[0]; d[1] = src[1]; d[2] = src[2]; d[3] = src[3];
+            } else {
+                uint32_t s[2] = {seed4[4 * i], seed4[4 * i + 1]};
+                or_myrandn(s, d);
+                seed4[4 * i] = s[0]; seed4[4 * i + 1] = s[1];
+            }
+            step2(P, i, pos4, seed4, params5, fiberPos, cc, cubes, 0.0f, 0.0f, 0.0f, phaseConstant, intraSd,
+                  extraSd, myelinSd, inRadPropSq, d, counts ? counts + 2 * (size_t)i : NULL);
+            const float w = wave[it];
+            const float* q = pos4 + 4 * (size_t)i;
+            for (uint32_t k = 0; k < nG; k++) {
+                float gx = w * grads[3 * k], gy = w * grads[3 * k + 1], gz = w * grads[3 * k + 2];
+                ph[k] += (gx * q[0] + gy * q[1] + gz * q[2]) * phaseConstant;
+            }
+        }
+    }
+}

@@ -362,6 +362,40 @@ uint32_t or3_integrate_mt(const or3_params* p, uint32_t N, float* pos, uint32_t*
     return capped;
 }
 
+uint32_t or3_integrate_multi(const or3_params* p, uint32_t N, float* pos, uint32_t* seed,
+                             float* mag, uint8_t* comp, uint16_t* fiber,
+                             const float* vertices, const float* helpers,
+                             const uint32_t* triInfo, const uint32_t* cubeCounter,
+                             const uint32_t* trianglesInCubes, uint32_t nG, const float* grads,
+                             const float* wave, float phaseConstant, uint32_t iterations,
+                             const float* draws, float* phases, uint32_t* counts, int nthreads) {
+    uint32_t capped = 0;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads) reduction(+ : capped)
+    for (uint32_t i = 0; i < N; i++) {
+        float* q = pos + 3 * (size_t)i;
+        float* ph = phases + (size_t)i * nG;
+        for (uint32_t it = 0; it < iterations; it++) {
+            float d[4];
+            if (draws) {
+                const float* src = draws + ((size_t)it * N + i) * 4;
+                d[0] = src[0]; d[1] = src[1]; d[2] = src[2]; d[3] = src[3];
+            } else {
+                or_myrandn(seed + 2 * (size_t)i, d);
+            }
+            float unused = 0.0f;
+            capped += step_f32(p, q, mag + i, &unused, comp + i, fiber + i, vertices, helpers, triInfo,
+                               cubeCounter, trianglesInCubes, 0.0f, 0.0f, 0.0f, phaseConstant, d,
+                               counts ? counts + 2 * (size_t)i : NULL);
+            const float w = wave[it];
+            for (uint32_t k = 0; k < nG; k++) {
+                float gx = w * grads[3 * k], gy = w * grads[3 * k + 1], gz = w * grads[3 * k + 2];
+                ph[k] += (gx * q[0] + gy * q[1] + gz * q[2]) * phaseConstant;
+            }
+        }
+    }
+    return capped;
+}
+
 uint32_t or3_integrate_f64(const or3_params* p, uint32_t N, double* pos, double* mag,
                            double* phase, uint8_t* comp, uint16_t* fiber,
                            uint32_t nT, const double* vertices, const uint32_t* trgls,

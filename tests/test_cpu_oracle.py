@@ -218,3 +218,92 @@ def test_fp64_oracle_moments_equal_its_phase_and_track_fp32(tmp_path):
     # against the FP32 oracle's (= the reference's) end positions
     d = np.abs(pos_b.reshape(-1, 3) - g["pos1"].reshape(-1, 3).astype(np.float64)).max(1)
     assert (d < 1e-5).mean() >= 0.95
+
+
+def _pgse_segments(iters, nd, nD):
+    """(wave value, steps) runs of a PGSE waveform as the reference's
+    sequencer passes it: +G for nd steps, 0 until nD, -G for nd, 0 after."""
+    w = np.zeros(iters, np.float32)
+    w[:nd] = 1
+    w[nD:nD + nd] = -1
+    segs, k = [], 0
+    while k < iters:
+        j = k
+        while j < iters and w[j] == w[k]:
+            j += 1
+        segs.append((float(w[k]), j - k))
+        k = j
+    return w, segs
+
+
+def test_multi_gradient_walk_equals_one_run_per_gradient_mesh(tmp_path):
+    """or3_integrate_multi (one walk, the phase of every gradient run) against
+    or3_integrate run once per gradient over the PGSE segments with the
+    reference's MWC draws: positions, magnitudes, compartments and every
+    phase bit for bit."""
+    from dsim_gb300.engine import grad_scaled, phase_constant
+    g = _load("mesh_am")
+    prm = json.loads(str(g["params"]))
+    path = tmp_path / "mesh.txt"
+    path.write_bytes(g["mesh_text"].tobytes())
+    m = O.Mesh(str(path), prm["spaceScale"])
+    cc, tic, maxtpc = O.populate_cubes(m.vertices, m.trgls, 50)
+    N, iters = prm["N"], 60
+    p = O.params3(g["stdDevs"], g["T2"], 0.05, prm["dt"], 50, maxtpc)
+    grads = grad_scaled([[40.0, -20.0, 60.0], [0.0, 0.0, 80.0], [-70.0, 10.0, 0.0]], prm["spaceScale"])
+    pc = phase_constant(prm["gamma"], prm["dt"])
+    w, segs = _pgse_segments(iters, 15, 35)
+    mag0, _, comp0, fib0 = O.spin_fields(g["spins0"])
+    seed0 = np.random.default_rng(3).integers(1, 2 ** 32 - 1, 2 * N, dtype=np.uint64).astype(np.uint32)
+    pos_m, seed_m, mag_m, comp_m, fib_m = g["pos0"].copy(), seed0.copy(), mag0.copy(), comp0.copy(), fib0.copy()
+    cnt_m = np.zeros(2 * N, np.uint32)
+    _, ph_m = O.integrate3_multi(p, pos_m, seed_m, mag_m, comp_m, fib_m, m.vertices, m.helpers, m.triInfo, cc, tic,
+                                 grads, w, pc, counts=cnt_m, nthreads=3)
+    assert cnt_m.sum() > 0
+    for k in range(len(grads)):
+        pos, seed, mag, comp, fib = g["pos0"].copy(), seed0.copy(), mag0.copy(), comp0.copy(), fib0.copy()
+        ph = np.zeros(N, np.float32)
+        for wv, n in segs:
+            gk = (np.float32(wv) * grads[k]).astype(np.float32)
+            O.integrate3(p, pos, seed, mag, ph, comp, fib, m.vertices, m.helpers, m.triInfo, cc, tic, gk, pc, n)
+        assert np.array_equal(_bits(ph), _bits(ph_m[:, k])), k
+        assert np.array_equal(_bits(pos), _bits(pos_m)) and np.array_equal(seed, seed_m)
+        assert np.array_equal(_bits(mag), _bits(mag_m)) and np.array_equal(comp, comp_m)
+        assert np.array_equal(fib, fib_m)
+
+
+def test_multi_gradient_walk_equals_one_run_per_gradient_cylinders(tmp_path):
+    """or2_integrate_multi against or2_integrate once per gradient (MWC draws)."""
+    from dsim_gb300.engine import grad_scaled, phase_constant
+    g = _load("cyl")
+    prm = json.loads(str(g["params"]))
+    path = tmp_path / "cyl.fibers"
+    path.write_bytes(g["fibers_text"].tobytes())
+    fp, maxR = O.load_fibers2(str(path), prm["spaceScale"])
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, maxR)
+    N, iters = prm["N"], 50
+    p = O.Params2()
+    ss = np.float32(prm["spaceScale"])
+    p.intraAdcScaled = np.float32(prm["intraAdc"]) / (ss * ss)
+    p.extraAdcScaled = np.float32(prm["extraAdc"]) / (ss * ss)
+    p.myelinAdcScaled = np.float32(prm["myelinAdc"]) / (ss * ss)
+    p.T2fiber, p.T2myelin, p.T2outside = prm["intraT2"], prm["myelinT2"], prm["extraT2"]
+    p.permeability, p.innerRadiusProportion, p.spinRadius, p.deltaTime = 0.05, prm["inner"], 0.005, prm["dt"]
+    p.numCubes, p.maxFibersPerCube, p.cubeLength = n, maxfpc, L
+    grads = grad_scaled([[80.0, 0.0, 0.0], [0.0, 56.0, 56.0]], prm["spaceScale"])
+    pc = phase_constant(prm["gamma"], prm["dt"])
+    w, segs = _pgse_segments(iters, 12, 30)
+    seed0 = g["seed0"].copy()
+    seed0.reshape(-1, 4)[:, :2] = np.random.default_rng(4).integers(1, 2 ** 32 - 1, (N, 2), dtype=np.uint64)
+    pos_m, seed_m, par_m = g["pos0"].copy(), seed0.copy(), g["params0"].copy()
+    ph_m = O.integrate2_multi(p, pos_m, seed_m, par_m, fp, cc, cubes, grads, w, pc, nthreads=3)
+    for k in range(len(grads)):
+        pos, seed, par = g["pos0"].copy(), seed0.copy(), g["params0"].copy()
+        for wv, nst in segs:
+            gk = (np.float32(wv) * grads[k]).astype(np.float32)
+            O.lib().or2_integrate(C.byref(p), N, pos, seed, par, fp, cc, cubes, float(gk[0]), float(gk[1]),
+                                  float(gk[2]), float(pc), nst, None, None, None)
+        assert not g["params0"].reshape(-1, 5)[:, 1].any()  # runs start at phase 0
+        assert np.array_equal(_bits(par.reshape(-1, 5)[:, 1]), _bits(ph_m[:, k])), k
+        assert np.array_equal(_bits(pos), _bits(pos_m)) and np.array_equal(seed, seed_m)
+        assert np.array_equal(_bits(par.reshape(-1, 5)[:, [0, 2, 3]]), _bits(par_m.reshape(-1, 5)[:, [0, 2, 3]]))

@@ -219,3 +219,100 @@ def test_mesh_replay_parity_at_the_subsegment_cap(engine, tmp_path, cap, refl):
     assert np.array_equal(gpos.view(np.uint32), pos.view(np.uint32))
     assert np.array_equal(gph.view(np.uint32), ph.view(np.uint32))
     assert np.array_equal(gcomp, comp) and np.array_equal(gfib, fib)
+
+
+def test_mesh_dsim3_abi_arrays_rewritten_in_place(engine, tmp_path):
+    """Between two integrateSystem calls the caller overwrites vertices,
+    helpers, triInfo and the grid in the same device arrays (the same sizes
+    and constants): the second call must walk the new mesh, bit for bit with
+    the oracle run on the two meshes in turn.  The drop-in notices the change
+    from the arrays' contents, not their addresses."""
+    from dsim_gb300 import _lib
+    from dsim_gb300 import substrates as S
+    L = _lib.abi3()
+    case = MeshCase(tmp_path, membranes="AM", permeability=0.05, N=1500)
+    tube2 = dict(case.tube)
+    tube2["vertices"] = (case.tube["vertices"] + np.array([0.6, -0.35, 0.2], np.float32)).astype(np.float32)
+    path2 = str(tmp_path / "mesh_shifted.txt")
+    S.write_mesh_file(path2, tube2)
+    meshes = []
+    for pth in (case.path, path2):
+        mo = O.Mesh(pth, case.spaceScale)
+        cc, tic, maxtpc = O.populate_cubes(mo.vertices, mo.trgls, 50)
+        meshes.append((mo, cc, tic.reshape(-1, maxtpc), maxtpc))
+    W = max(m[3] for m in meshes)
+    dense = []
+    for mo, cc, tic, maxtpc in meshes:
+        t = np.zeros((50 ** 3, W), np.uint32)
+        t[:, :maxtpc] = tic
+        dense.append(np.ascontiguousarray(t.reshape(-1)))
+    assert not np.array_equal(meshes[0][0].vertices, meshes[1][0].vertices)
+    it1, it2 = 30, 30
+    d = draws(it1 + it2, case.N, seed=23)
+    p = O.params3(case.stdDevs, case.T2, case.permeability, case.dt, 50, W)
+    pos = case.pos.copy(); seed = np.zeros(2 * case.N, np.uint32)
+    mag = case.mag.copy(); ph = case.phase.copy(); comp = case.comp.copy(); fib = case.fiber.copy()
+    cnt = np.zeros(2 * case.N, np.uint32)
+    for (mo, cc, _, _), t, dd in ((meshes[0], dense[0], d[:it1]), (meshes[1], dense[1], d[it1:])):
+        capped, _ = O.integrate3(p, pos, seed, mag, ph, comp, fib, mo.vertices, mo.helpers, mo.triInfo, cc, t,
+                                 case.g, case.pc, len(dd), draws=dd, counts=cnt)
+        assert capped == 0
+    bufs = []
+
+    def dev(arr):
+        q = C.c_void_p()
+        L.allocateArray(C.byref(q), arr.nbytes)
+        L.copyArrayToDevice(q, arr.ctypes.data, 0, arr.nbytes)
+        bufs.append(q)
+        return q
+
+    try:
+        mo0, cc0 = meshes[0][0], meshes[0][1]
+        dV, dH, dTI = dev(mo0.vertices), dev(mo0.helpers), dev(mo0.triInfo)
+        dTic, dCc = dev(dense[0]), dev(cc0)
+        L.bindVertices(dV, len(mo0.vertices))
+        L.bindTriangleHelpers(dH, len(mo0.helpers))
+        L.bindTriInfo(dTI, len(mo0.triInfo))
+        for name, val, ty in (("k_numCubes", 50, np.uint32), ("k_totalNumCubes", 50 ** 3, np.uint32),
+                              ("k_maxTrianglesPerCube", W, np.uint32),
+                              ("k_cubeLength", np.float32(2.0) / np.float32(50), np.float32),
+                              ("k_reflectionType", 1, np.uint32), ("k_permeability", case.permeability, np.float32),
+                              ("k_deltaTime", case.dt, np.float32)):
+            a = np.array([val], ty)
+            L.copyConstantToDevice(name.encode(), a.ctypes.data, 0, 4)
+        for name, tab in (("k_T2Values", case.T2), ("k_stdDevs", case.stdDevs)):
+            a = np.ascontiguousarray(tab, np.float32)
+            L.copyConstantToDevice(name.encode(), a.ctypes.data, 0, 16)
+        spins = np.zeros(case.N, np.dtype([("mag", "<f4"), ("phase", "<f4"), ("comp", "u1"), ("pad", "u1"),
+                                            ("fiber", "<u2")]))
+        spins["mag"], spins["phase"], spins["comp"], spins["fiber"] = case.mag, case.phase, case.comp, case.fiber
+        dPos, dSeed, dSpins = dev(case.pos.copy()), dev(np.zeros(2 * case.N, np.uint32)), dev(spins)
+        dD1, dD2 = dev(np.ascontiguousarray(d[:it1]).reshape(-1)), dev(np.ascontiguousarray(d[it1:]).reshape(-1))
+        dCnt = dev(np.zeros(2 * case.N, np.uint32))
+        g = _lib.Float3(*[float(x) for x in case.g])
+        for seg, (dd, its) in enumerate(((dD1, it1), (dD2, it2))):
+            if seg:
+                mo1, cc1 = meshes[1][0], meshes[1][1]
+                for dst, src in ((dV, mo1.vertices), (dH, mo1.helpers), (dTI, mo1.triInfo), (dTic, dense[1]),
+                                 (dCc, cc1)):
+                    L.copyArrayToDevice(dst, src.ctypes.data, 0, src.nbytes)
+            L.dsim3_set_replay(dd, dCnt)
+            L.integrateSystem(dPos, dSeed, dSpins, float(case.dt), float(case.permeability), case.N, g,
+                              float(case.pc), its, dTic, dCc)
+            L.dsim3_set_replay(None, None)
+            assert L.dsim3_last_status() == 0, L.dsim3_last_error()
+        gpos = np.zeros_like(case.pos)
+        out = np.zeros_like(spins)
+        gcnt = np.zeros(2 * case.N, np.uint32)
+        L.copyArrayFromDevice(gpos.ctypes.data, dPos, 0, gpos.nbytes)
+        L.copyArrayFromDevice(out.ctypes.data, dSpins, 0, out.nbytes)
+        L.copyArrayFromDevice(gcnt.ctypes.data, dCnt, 0, gcnt.nbytes)
+        assert L.dsim3_status() == 0
+        assert np.array_equal(gcnt, cnt)
+        assert np.array_equal(gpos.view(np.uint32), pos.view(np.uint32))
+        assert np.array_equal(out["phase"].view(np.uint32), ph.view(np.uint32))
+        assert np.array_equal(out["mag"].view(np.uint32), mag.view(np.uint32))
+        assert np.array_equal(out["comp"], comp) and np.array_equal(out["fiber"], fib)
+    finally:
+        for q in bufs:
+            L.freeArray(q)

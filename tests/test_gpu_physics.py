@@ -7,7 +7,8 @@
 * The device FP64 signal reduction equals the oracle's getMrSignal.
 * Free diffusion: the PGSE signal equals exp(-b D),
   b = (2 pi gamma G delta)^2 (Delta - delta/3) (dSim3/src/diffusion.cpp:317),
-  within 4 Monte-Carlo standard errors.
+  in the exact form of the discrete walk (below), within 3 Monte-Carlo
+  standard errors and no other slack.
 """
 import numpy as np
 import pytest
@@ -63,6 +64,25 @@ def test_signal_reduction_matches_oracle(engine):
     assert sums[0, 2] == N and sums[1:, 2].sum() == N
 
 
+def discrete_free_signal(grad_per_step, sigma, pc):
+    """Expected signal of the discrete free walk x_t = x_0 + sigma sum_{s<=t} n_s
+    with phase pc sum_t g_t . x_t.  For a balanced waveform (sum_t g_t = 0) the
+    phase is pc sigma sum_s n_s . W_s, W_s = sum_{t>=s} g_t, a Gaussian of
+    variance V = (pc sigma)^2 sum_s |W_s|^2, so E cos(phi) = exp(-V/2).  This
+    is exp(-b D) with b in the form of the walk's own time steps."""
+    g = np.asarray(grad_per_step, np.float64).reshape(-1, 3)
+    assert np.allclose(g.sum(0), 0.0, atol=1e-12)
+    W = np.cumsum(g[::-1], axis=0)[::-1]
+    V = (float(pc) * float(sigma)) ** 2 * float((W ** 2).sum())
+    return np.exp(-V / 2)
+
+
+def free_se(S, N):
+    """Standard error of mean cos(phi) for phi ~ N(0, V), E cos = S:
+    Var cos = (1 + S^4)/2 - S^2 = (1 - S^2)^2 / 2."""
+    return (1.0 - S * S) / np.sqrt(2.0 * N)
+
+
 @pytest.mark.parametrize("G,direction", [(0.0, (1, 0, 0)), (40.0, (1, 0, 0)),
                                          (80.0, (0, 0, 1)), (80.0, (1, 1, 0))])
 def test_free_diffusion_pgse_matches_exp_minus_bD(engine, G, direction):
@@ -70,7 +90,7 @@ def test_free_diffusion_pgse_matches_exp_minus_bD(engine, G, direction):
                                    phase_constant, signal_from_sums, std_devs)
     D, dt, delta, Delta = 2.0, 0.01, 10.0, 30.0
     spaceScale = 1000.0
-    N = 1 << 18
+    N = 1 << 20
     # a substrate with no triangles: free diffusion
     m = Mesh.from_arrays(np.zeros((3, 3), np.float32), np.zeros((0, 3), np.uint32), None, None,
                          spaceScale)
@@ -78,19 +98,22 @@ def test_free_diffusion_pgse_matches_exp_minus_bD(engine, G, direction):
     s = Spins(N)
     s.set(rng.uniform(-0.3, 0.3, 3 * N).astype(np.float32), np.ones(N, np.float32),
           np.zeros(N, np.float32), np.zeros(N, np.uint8), np.full(N, 0xFFFF, np.uint16))
-    p = mesh_params(std_devs(D, D, D, spaceScale, dt), [1e30] * 4, 0.0, dt, phase_constant(42576.0, dt))
+    sd = std_devs(D, D, D, spaceScale, dt)
+    pc = phase_constant(42576.0, dt)
+    p = mesh_params(sd, [1e30] * 4, 0.0, dt, pc)
     u = np.asarray(direction, np.float64)
     u = u / np.linalg.norm(u)
     g = grad_scaled(G * u, spaceScale)
     nd, nD = int(round(delta / dt)), int(round(Delta / dt))
     step = 0
-    for gg, n in ((g, nd), (np.zeros(3, np.float32), nD - nd), (-g, nd)):
+    segs = ((g, nd), (np.zeros(3, np.float32), nD - nd), (-g, nd))
+    for gg, n in segs:
         mesh_run(m, s, p, g=gg, iterations=n, seed=99, step0=step)
         step += n
     S = signal_from_sums(s.signal())[0]
     assert s.status() == 0
-    gamma = 42576.0
-    b = (2 * np.pi * gamma * G * 1e-9 * delta) ** 2 * (Delta - delta / 3.0)
-    expect = np.exp(-b * D)
-    se = np.sqrt(max(1 - expect ** 2, 1e-6) / (2 * N))
-    assert abs(S - expect) < 4 * se + 2e-3, (S, expect, b)
+    gps = np.concatenate([np.repeat(np.asarray(gg, np.float64)[None, :], n, 0) for gg, n in segs])
+    expect = discrete_free_signal(gps, sd[0], pc)
+    b = (2 * np.pi * 42576.0 * G * 1e-9 * delta) ** 2 * (Delta - delta / 3.0)
+    assert abs(expect - np.exp(-b * D)) < 5e-3              # the continuous closed form
+    assert abs(S - expect) <= 3 * free_se(expect, N), (S, expect, b)
