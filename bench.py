@@ -87,6 +87,7 @@ class Workload:
         w = np.zeros(self.total_steps, F)
         w[:nd] = 1
         w[nD:nD + nd] = -1
+        self.wave = w
         self.grad = (w[:, None] * self.g[None, :]).astype(F)
         log("workload: %d triangles, %d vertices, overlap=%s, %.1fs" % (
             len(self.tube["trgls"]), len(self.tube["vertices"]), self.tube["overlap"], time.time() - t0))
@@ -268,8 +269,17 @@ def _helpers(v, trgls):
 # e2e through the reference-facing dSim3 C-ABI
 # --------------------------------------------------------------------------
 def e2e_abi3(W, m, steps, warmup, pinned):
+    """The headline walk through the reference-facing dSim3 C-ABI
+    (libdsim3.so), as a host that keeps the spin state in its own memory
+    drives it: every call copies pos, randSeed and spinData from pinned host
+    buffers to the device, runs integrateSystem for one 1000-step update with
+    that update's PGSE gradient, and copies all three back (so each spin's
+    Philox key, advanced by the call, goes into the next call).  The timed
+    calls start from the same reset as the device-timed leg and walk the same
+    steps; L2 is flushed before each call, outside its timed interval."""
     import ctypes as C
     from dsim_gb300 import _lib
+    from dsim_gb300.engine import Spins
     L = _lib.abi3()
     start, tri = m.grid()
     counts = np.diff(start.astype(np.int64)).astype(np.uint32)
@@ -309,38 +319,58 @@ def e2e_abi3(W, m, steps, warmup, pinned):
     spins["comp"], spins["fiber"] = W.comp, W.fiber
     seeds = np.random.default_rng(9).integers(1, 2 ** 32 - 1, 2 * N, dtype=np.uint64).astype(np.uint32)
     hpos, hseed, hspin = pinned(W.pos.nbytes), pinned(seeds.nbytes), pinned(spins.nbytes)
-    hpos[:] = W.pos.view(np.uint8)
-    hseed[:] = seeds.view(np.uint8)
-    hspin[:] = spins.view(np.uint8)
     dPos, dSeed, dSpin = dev(W.pos), dev(seeds), dev(spins)
-    g = _lib.Float3(*[float(x) for x in W.g])
+    flusher = Spins(1)
     it = W.steps_per_launch
 
-    def one():
-        # the reference host loop per update: setArray/setSpinArray, integrateSystem, getArray/getSpinArray
+    def reset():
+        hpos[:] = W.pos.view(np.uint8)
+        hseed[:] = seeds.view(np.uint8)
+        hspin[:] = spins.view(np.uint8)
+
+    def one(k):
+        # the update's gradient: the PGSE waveform is constant over each 1000-step update
+        lo = (k * it) % W.total_steps
+        assert np.all(W.wave[lo:lo + it] == W.wave[lo])
+        g = _lib.Float3(*[float(F(W.wave[lo] * x)) for x in W.g])
         L.copyArrayToDevice(dPos, hpos.ctypes.data, 0, hpos.nbytes)
         L.copyArrayToDevice(dSeed, hseed.ctypes.data, 0, hseed.nbytes)
         L.copyArrayToDevice(dSpin, hspin.ctypes.data, 0, hspin.nbytes)
         L.integrateSystem(dPos, dSeed, dSpin, float(W.dt), 0.0, N, g, float(W.pc), it, dTic, dCc)
         L.copyArrayFromDevice(hpos.ctypes.data, dPos, 0, hpos.nbytes)
+        L.copyArrayFromDevice(hseed.ctypes.data, dSeed, 0, hseed.nbytes)
         L.copyArrayFromDevice(hspin.ctypes.data, dSpin, 0, hspin.nbytes)
 
-    for _ in range(warmup):
-        one()
+    reset()
+    for k in range(warmup):
+        one(k)
     L.threadSync()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        one()
-    L.threadSync()
-    el = time.perf_counter() - t0
+    reset()
+    per = []
+    for k in range(steps):
+        flusher.flush_l2(512 << 20)
+        flusher.sync()
+        L.threadSync()
+        t0 = time.perf_counter()
+        one(k)
+        L.threadSync()
+        per.append(time.perf_counter() - t0)
+    el = sum(per)
     st = L.dsim3_last_status()
     if st != 0:
         raise RuntimeError("dSim3 ABI: %s" % L.dsim3_last_error())
+    out = np.frombuffer(hspin.tobytes(), spins.dtype)
+    X = (out["mag"].astype(np.float64) * np.cos(out["phase"].astype(np.float64))).sum()
+    Y = (out["mag"].astype(np.float64) * np.sin(out["phase"].astype(np.float64))).sum()
     for p in allocs:
         L.freeArray(p)
+    flusher.free()
     return {"value": steps * it * N / el, "unit": UNIT, "h2d_bytes_per_step": int(hpos.nbytes + hseed.nbytes + hspin.nbytes),
-            "d2h_bytes_per_step": int(hpos.nbytes + hspin.nbytes), "ms_per_step": 1e3 * el / steps,
-            "path": "libdsim3.so integrateSystem, pinned host buffers"}
+            "d2h_bytes_per_step": int(hpos.nbytes + hseed.nbytes + hspin.nbytes), "ms_per_step": 1e3 * el / steps,
+            "calls": steps, "steps_walked": [0, steps * it], "l2": "flushed before each call (untimed)",
+            "signal_after_run": float(np.hypot(X, Y) / N),
+            "path": "libdsim3.so integrateSystem; pos, randSeed, spinData copied in and out of pinned host buffers "
+                    "every call"}
 
 
 def pinned_factory():
@@ -456,9 +486,11 @@ def run_ours(args, rank, world):
     }
     if rank == 0 and not args.no_e2e:
         pinned, is_pinned = pinned_factory()
-        e = e2e_abi3(W, m, max(2, min(args.steps, 5)), 1, pinned)
+        e = e2e_abi3(W, m, args.steps, args.warmup, pinned)
         e["pinned"] = is_pinned
         res["e2e"] = e
+    if rank == 0 and not args.no_err:
+        res["err_vs_fp64"] = run_headline_error(args, W, m)
     if rank == 0 and not args.no_forms:
         res["forms"] = run_forms(args, W, m)
     if rank == 0 and not args.no_precision:
@@ -490,6 +522,112 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# --------------------------------------------------------------------------
+# signal error against an FP64 run on the same draws
+# --------------------------------------------------------------------------
+ERR_BAR = 1e-3
+
+
+def _z_from_moments(mag, mom6, gs, pc):
+    """Per-spin m e^{i phi} for every gradient from a batch job's moments
+    (phi = pc g . M, M = moment - its Kahan compensation)."""
+    M = mom6[:, :3].astype(np.float64) - mom6[:, 3:].astype(np.float64)
+    return mag.astype(np.float64)[:, None] * np.exp(1j * float(pc) * (M @ np.asarray(gs, np.float64).reshape(-1, 3).T))
+
+
+def _S(z, sel=None):
+    if sel is not None:
+        z = z[sel]
+    return np.abs(z.sum(0)) / max(len(z), 1)
+
+
+def _err_summary(dS, what):
+    dS = np.asarray(dS, np.float64).reshape(-1)
+    return {"max_abs_dS": float(dS.max()), "median_abs_dS": float(np.median(dS)), "gradients": int(len(dS)),
+            "within_1e-3": bool(dS.max() <= ERR_BAR), "against": what}
+
+
+def philox_draw_chunks(seed, n, steps, chunk=500):
+    """The step kernels' own draws for spins [0, n) of a job keyed by `seed`,
+    [steps][n][4], yielded `chunk` steps at a time."""
+    from dsim_gb300.engine import rng_draws
+    for t0 in range(0, steps, chunk):
+        t1 = min(steps, t0 + chunk)
+        yield t0, np.stack([rng_draws(seed, 0, t, n) for t in range(t0, t1)])
+
+
+def cyl_fp64_z(cyl, pos3, imo, near, step_sd_adc, T2, perm, inner, dt, pc, grads, wave, seed):
+    """FP64 oracle walk (restated dSim2 step in double, oracle/) of a
+    cylinder job's spins on the GPU's Philox draws for that job: per-spin
+    m e^{i phi} [n][nG] and final positions."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    cc, cubes, fp = cyl.grid()
+    P = O.Params2()
+    P.intraAdcScaled, P.myelinAdcScaled, P.extraAdcScaled = [F(a) for a in step_sd_adc]
+    P.T2fiber, P.T2myelin, P.T2outside = [float(x) if x > 0 else 1e30 for x in T2[:3]]
+    P.permeability, P.innerRadiusProportion, P.spinRadius, P.deltaTime = float(perm), float(inner), 0.005, float(dt)
+    P.numCubes, P.maxFibersPerCube, P.cubeLength = cyl.numCubes, cyl.maxFPC, cyl.cubeLength
+    n = len(imo)
+    pos = np.ascontiguousarray(pos3, np.float64).reshape(-1).copy()
+    mag = np.ones(n, np.float64)
+    im = np.ascontiguousarray(imo, np.uint32).copy()
+    nr = np.ascontiguousarray(near, np.uint32).copy()
+    ph = np.zeros((n, len(np.asarray(grads).reshape(-1, 3))), np.float64)
+    for t0, d in philox_draw_chunks(seed, n, len(wave)):
+        ph += O.integrate2_f64_multi(P, pos, mag, im, nr, fp, cc, cubes, grads, wave[t0:t0 + len(d)],
+                                     float(pc), d)
+    return mag[:, None] * np.exp(1j * ph), pos.reshape(-1, 3)
+
+
+def run_headline_error(args, W, m):
+    """Signal error of the headline workload's FP32 forms against the FP64
+    form on the same Philox draws (the FP64 form walks the reference's step in
+    double and equals the FP64 oracle bit for bit): every spin of the
+    workload over the whole PGSE (delta 15, Delta 40 ms: 11,000 steps)."""
+    from dsim_gb300.engine import Batch, Spins, grad_scaled, mesh_run, signal_from_sums
+    from dsim_gb300.jobs import fibonacci_dirs, pgse_gmag
+    steps = int(round((W.delta + W.Delta) / W.dt))
+    nd, nD = int(round(W.delta / W.dt)), int(round(W.Delta / W.dt))
+    w = np.zeros(steps, F)
+    w[:nd] = 1
+    w[nD:nD + nd] = -1
+    seed = 5
+    t0 = time.time()
+    s = Spins(W.N)
+    s.set(W.pos, np.ones(W.N, F), np.zeros(W.N, F), W.comp, W.fiber)
+    mesh_run(m, s, mesh_params_of(W), grad_per_step=(w[:, None] * W.g[None, :]).astype(F), iterations=steps,
+             seed=seed)
+    S_plain = signal_from_sums(s.signal())[0]
+    assert s.status() == 0
+    s.free()
+    G = np.concatenate([pgse_gmag(b, W.delta, W.Delta) * fibonacci_dirs(64) for b in (1.0, 2.0, 3.0)])
+    gs = np.concatenate([W.g[None, :], grad_scaled(G, W.spaceScale).astype(F).reshape(-1, 3)])
+    b = Batch(3 * (W.N + 64), 3)
+    sid = b.add_mesh(m)
+    common = dict(pos=W.pos, comp=W.comp, fiber=W.fiber.astype(np.uint32), steps=steps, dt=W.dt, step_sd=W.stdDevs,
+                  T2=W.T2, phase_constant=W.pc, seed=seed, waveform="pgse", delta=W.delta, Delta=W.Delta)
+    j64 = b.submit(sid, precise=True, **common)
+    j32 = b.submit(sid, **common)
+    jloc = b.submit(sid, local=True, **common)
+    b.run()
+    st = b.status()
+    S = {}
+    for name, j in (("fp64", j64), ("batch_fp32", j32), ("local", jloc)):
+        sums = b.signal(j, gs)
+        S[name] = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
+    b.close()
+    return {"workload": "every spin of the headline workload (%d) x %d steps (the whole PGSE), seed %d, the "
+                        "headline gradient plus 64 Fibonacci directions x b 1, 2, 3 ms/um2" % (W.N, steps, seed),
+            "against": "the FP64 form on the same draws (the reference step in double; equal to the FP64 oracle "
+                       "bit for bit)",
+            "plain": dict(_err_summary([abs(S_plain - S["fp64"][0])], "FP64 form"),
+                          note="the timed form: one walk with the headline gradient (b 3 ms/um2)"),
+            "batch_fp32": _err_summary(np.abs(S["batch_fp32"] - S["fp64"]), "FP64 form"),
+            "local": _err_summary(np.abs(S["local"] - S["fp64"]), "FP64 form"),
+            "signal_headline_fp64": float(S["fp64"][0]), "status": st, "seconds": time.time() - t0}
 
 
 # --------------------------------------------------------------------------
@@ -595,9 +733,10 @@ def run_served_mix(subs, mix, cfg, rate, seed=3):
     srv.drain()
     st = srv.stats()
     srv.stop()
-    lat, first, last = [], None, None
+    lat, first, last, sigs = [], None, None, []
     for t in tickets:
         done, sig, tm = srv.poll(t)
+        sigs.append(sig)
         lat.append(tm[2] - tm[0])
         first = tm[0] if first is None else min(first, tm[0])
         last = tm[2] if last is None else max(last, tm[2])
@@ -605,7 +744,74 @@ def run_served_mix(subs, mix, cfg, rate, seed=3):
     work = sum(j["n"] * j["steps"] for j in mix)
     return {"rate_jobs_per_s": rate, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "spin_steps_per_s": work / (last - first), "max_jobs_in_flight": int(st["max_inflight"]),
-            "errors": int(st["errors"])}
+            "errors": int(st["errors"])}, sigs
+
+
+def mix_fp64_reference(mix, ns_cyl=2048):
+    """FP64 references of a job mix on the same Philox draws.
+    Mesh jobs: the FP64 form on the GPU (the reference step in double, equal
+    to the FP64 oracle bit for bit), whole jobs: {job: S64 per gradient}.
+    Cylinder jobs: the first min(n, ns_cyl) spins as an FP32 batch job and as
+    the FP64 oracle walk (oracle/, on the CPU) on the same draws:
+    {job: |S32 - S64| per gradient} on that sample."""
+    from dsim_gb300.engine import Batch, pgse_table
+    mesh = [i for i, j in enumerate(mix) if j["sub"].kind == "mesh"]
+    cyl = [i for i, j in enumerate(mix) if j["sub"].kind != "mesh"]
+    ref, cyl_err = {}, {}
+    if mesh:
+        b = Batch(sum((mix[i]["n"] + 31) // 32 * 32 for i in mesh), len(mesh))
+        sids = {}
+        for i in mesh:
+            if id(mix[i]["sub"]) not in sids:
+                sids[id(mix[i]["sub"])] = b.add_mesh(mix[i]["sub"].handle)
+        ids = {i: b.submit(sids[id(mix[i]["sub"])], mix[i]["pos"], mix[i]["comp"], mix[i]["fiber"], precise=True,
+                           **_submit_kw(mix[i])) for i in mesh}
+        b.run()
+        for i in mesh:
+            sums = b.signal(ids[i], mix[i]["grads"])
+            ref[i] = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
+        b.close()
+    if cyl:
+        nsam = {i: min(mix[i]["n"], ns_cyl) for i in cyl}
+        b = Batch(sum((nsam[i] + 31) // 32 * 32 for i in cyl), len(cyl))
+        sids = {}
+        for i in cyl:
+            if id(mix[i]["sub"]) not in sids:
+                sids[id(mix[i]["sub"])] = b.add_cyl(mix[i]["sub"].handle)
+        ids = {}
+        for i in cyl:
+            j, n = mix[i], nsam[i]
+            ids[i] = b.submit(sids[id(j["sub"])], j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], **_submit_kw(j))
+        b.run()
+        for i in cyl:
+            j, n = mix[i], nsam[i]
+            _, bmag, bmom, _, _ = b.get(ids[i], n)
+            z32 = _z_from_moments(bmag, bmom, j["grads"], j["phase_constant"])
+            ss = F(j["sub"].spaceScale)
+            adc = tuple(F(a) / (ss * ss) for a in (2.0, 0.2, 2.0))      # intra, myelin, extra (jobs.make_job)
+            wave = pgse_table(j["steps"], float(j["dt"]), j["delta"], j["Delta"])
+            z64, _ = cyl_fp64_z(j["sub"].handle, j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], adc, j["T2"],
+                                j["permeability"], j["inner"], j["dt"], j["phase_constant"], j["grads"], wave,
+                                j["seed"])
+            cyl_err[i] = np.abs(_S(z32) - _S(z64))
+        b.close()
+    return ref, cyl_err
+
+
+def mix_err(mix, sigs, ref, cyl_err):
+    """Per-form error summary: mesh jobs from the form's own signals `sigs`
+    (per job, sums [nG][5][3]) against the FP64 form; cylinder jobs on their
+    spin sample (mix_fp64_reference)."""
+    me = [np.abs(np.hypot(sigs[i][:, 0, 0], sigs[i][:, 0, 1]) / sigs[i][:, 0, 2] - ref[i]) for i in ref]
+    ce = list(cyl_err.values())
+    allv = np.concatenate(me + ce) if (me or ce) else np.zeros(1)
+    out = {"all": _err_summary(allv, "FP64 on the same Philox draws")}
+    if me:
+        out["mesh_jobs"] = _err_summary(np.concatenate(me), "FP64 form on the GPU, whole jobs")
+    if ce:
+        out["cylinder_jobs"] = _err_summary(np.concatenate(ce), "FP64 oracle walk (CPU), first 2048 spins of each "
+                                                                 "job against the same spins in FP32")
+    return out
 
 
 def run_forms(args, W, m):
@@ -626,6 +832,10 @@ def run_forms(args, W, m):
     plain_s = sum(per)
     el, sigs, info, st = run_batched_mix(subs, mix, cfg)
     plain_rate = work / plain_s
+    t_err = time.time()
+    ref, cyl_err = mix_fp64_reference(mix)
+    batched_err = mix_err(mix, sigs, ref, cyl_err)
+    batched_err["seconds"] = time.time() - t_err
     out = {
         "mix": {"jobs": n_jobs, "spins": list(spins_range), "steps": list(steps_range), "dt_us": [5, 10],
                 "substrates": "beaded tubes 400 and 100 axons (2.56M / 0.64M triangles), packed cylinders 64 and 256",
@@ -638,7 +848,7 @@ def run_forms(args, W, m):
                     "note": "all jobs in one batch; signals_speedup counts one plain walk per gradient, as the "
                             "reference re-walks every gradient",
                     "autotuned": best, "kernel_launches": info["launches"], "graph_launches": info["graph_launches"],
-                    "status": st},
+                    "status": st, "err_vs_fp64": batched_err},
     }
     # serving: the same substrates and ranges with permeable membranes (per-hit
     # permeation log-uniform 1e-4 - 1e-2); arrival rates relative to the plain
@@ -651,9 +861,12 @@ def run_forms(args, W, m):
         out["served_mix"] = {"jobs": n_jobs, "seed": 12, "permeability": "log-uniform 1e-4 - 1e-2 per hit",
                              "plain_spin_steps_per_s": sum(j["n"] * j["steps"] for j in pmix) / pplain_s,
                              "plain_jobs_per_s": cap_jobs}
-        out["served"] = [run_served_mix(subs, pmix, cfg, r * cap_jobs) for r in args.serve_rates]
-        for o, r in zip(out["served"], args.serve_rates):
+        pref, pcyl = mix_fp64_reference(pmix)
+        for r in args.serve_rates:
+            o, ssig = run_served_mix(subs, pmix, cfg, r * cap_jobs)
             o["rate_x_plain_capacity"] = r
+            o["err_vs_fp64"] = mix_err(pmix, ssig, pref, pcyl)
+            out["served"].append(o)
     return out
 
 
@@ -689,7 +902,7 @@ def run_cylinders(args):
     for k, g in enumerate(gs):
         s.set_cyl(pos, None, None, imo.astype(np.uint32), near)
         cyl_run(c, s, p, grad_per_step=(w[:, None] * g[None, :]).astype(F), iterations=steps, seed=k + 1)
-        sums = s.signal()
+        sums = s.signal(0.8)                      # dSim2 reads spins inside +-0.8
         plain_S.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
     plain_s = time.perf_counter() - t0
     # batch form: the same 48 fresh walks as 48 jobs of one launch
@@ -701,7 +914,7 @@ def run_cylinders(args):
     b.run()
     batch_S = []
     for k, j in enumerate(ids):
-        sums = b.signal(j, gs[k][None, :])[0]
+        sums = b.signal(j, gs[k][None, :], region=0.8)[0]
         batch_S.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
     batch_s = time.perf_counter() - t0
     counts = b.counts(ids[0])
@@ -713,10 +926,26 @@ def run_cylinders(args):
     j = b.submit(sid, pos.reshape(-1), imo, near, steps, dt, sd, T2, pc, 1, waveform="pgse", delta=delta,
                  Delta=Delta, inner_radius_proportion=1.0)
     b.run()
-    sums = b.signal(j, gs)
+    sums = b.signal(j, gs, region=0.8)
     shared_S = (np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]).tolist()
     shared_s = time.perf_counter() - t0
+    sw_pos, sw_mag, sw_mom, _, _ = b.get(j, N)
     b.close()
+    # signal error against the FP64 oracle walk on the same Philox draws
+    t_err = time.perf_counter()
+    in_box = lambda q: np.all(np.abs(np.asarray(q).reshape(-1, 3)) < 0.8, axis=1)
+    adc = (F(2.0) / (ss * ss),) * 3
+    z64, p64 = cyl_fp64_z(c, pos, imo, near, adc, [0, 0, 0], 0.0, 1.0, dt, pc, gs, w, 1)
+    z32 = _z_from_moments(sw_mag, sw_mom, gs, pc)
+    err_shared = np.abs(_S(z32, in_box(sw_pos)) - _S(z64, in_box(p64)))
+    err_plain = []
+    for k in range(len(gs) - 6, len(gs)):          # 80 mT/m along each of the 6 directions
+        zk, pk = cyl_fp64_z(c, pos, imo, near, adc, [0, 0, 0], 0.0, 1.0, dt, pc, gs[k][None, :], w, k + 1)
+        err_plain.append(abs(plain_S[k] - float(_S(zk, in_box(pk))[0])))
+    err = {"shared_walk": _err_summary(err_shared, "FP64 oracle walk on the same Philox draws, all 48 gradients"),
+           "plain": _err_summary(err_plain, "FP64 oracle walk on each walk's Philox draws, 80 mT/m along the "
+                                            "6 directions"),
+           "seconds": time.perf_counter() - t_err}
     # C-bar: cell-list entries a step examines (own fiber inside; the new
     # position's cell list outside), from the initial state
     cc, cubes, fp = c.grid()
@@ -733,6 +962,7 @@ def run_cylinders(args):
            "plain_seconds": plain_s, "batched_seconds": batch_s,
            "signal_plain": plain_S[::8], "signal_batched": batch_S[::8], "signal_shared_walk": shared_S[::8],
            "rejections_per_spin_step": float(counts[0]) / (N * steps),
+           "err_vs_fp64": err, "readout": "spins inside +-0.8 (dSim2 getMrSignal)",
            "roofline": {"bytes_per_spin_step": 2 * 20 + 16 * Cbar, "C_bar": Cbar,
                         "achieved_GBs_batched": (2 * 20 + 16 * Cbar) * work / batch_s / 1e9,
                         "fine_grid": c.fine_info(),
@@ -974,6 +1204,7 @@ def main():
     ap.add_argument("--records", type=int, default=0, help="fine-grid record bytes (0 default)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-err", action="store_true", help="skip the headline signal error against the FP64 form")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched / served job-mix runs")
     ap.add_argument("--mix-jobs", type=int, default=48)

@@ -170,6 +170,16 @@ void or2_integrate_multi(const or2_params* p, uint32_t N, float* pos4, uint32_t*
                          float phaseConstant, uint32_t iterations, const float* draws,
                          float* phases, uint32_t* counts, int nthreads);
 
+/* FP64 precision oracle for cylinders: the same walk with every
+ * position-dependent quantity in double, on replay draws (float[iters][N][4]),
+ * one walk for nG gradient runs (phases[i*nG + k] in double).  pos3, mag,
+ * imo, nearest are updated in place.  OpenMP over spins. */
+void or2_integrate_f64_multi(const or2_params* p, uint32_t N, double* pos3, double* mag, uint32_t* imo,
+                             uint32_t* nearest, const float* fiberPos, const uint32_t* cubeCounter,
+                             const uint32_t* cubes, uint32_t nG, const double* grads, const double* wave,
+                             double phaseConstant, uint32_t iterations, const float* draws, double* phases,
+                             int nthreads);
+
 /* getMrSignal() dSim2/src/spinSystem.cpp:944-978 (spins inside +-0.8 only) */
 double or2_signal(uint32_t N, const float* pos4, const float* params5);
 

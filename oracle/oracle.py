@@ -116,6 +116,9 @@ def _declare(L):
     L.or2_integrate_multi.argtypes = [C.POINTER(Params2), C.c_uint32, P_F32, P_U32, P_F32, P_F32, P_U32,
                                       P_U32, C.c_uint32, P_F32, P_F32, C.c_float, C.c_uint32, _opt(P_F32),
                                       P_F32, _opt(P_U32), C.c_int]
+    L.or2_integrate_f64_multi.argtypes = [C.POINTER(Params2), C.c_uint32, P_F64, P_F64, P_U32, P_U32, P_F32,
+                                          P_U32, P_U32, C.c_uint32, P_F64, P_F64, C.c_double, C.c_uint32, P_F32,
+                                          P_F64, C.c_int]
     L.or3_signal.argtypes = [C.c_uint32, P_F32, P_F32, P_U8, P_F64]
     L.or2_load_fibers.argtypes = [C.c_char_p, C.c_float, _opt(P_F32), C.POINTER(C.c_float)]
     L.or2_load_fibers.restype = C.c_int
@@ -233,6 +236,22 @@ def integrate2_multi(p, pos4, seed4, params5, fiberPos, cc, cubes, grads, wave, 
     d = None if draws is None else np.ascontiguousarray(draws, np.float32).reshape(-1)
     lib().or2_integrate_multi(C.byref(p), N, pos4, seed4, params5, fiberPos, cc, cubes, len(g), g.reshape(-1), w,
                               float(phaseConstant), len(w), d, ph, counts, int(nthreads or os.cpu_count() or 1))
+    return ph.reshape(N, len(g))
+
+
+def integrate2_f64_multi(p, pos3, mag, imo, nearest, fiberPos, cc, cubes, grads, wave, phaseConstant, draws,
+                        nthreads=None):
+    """FP64 cylinder walk on replay draws [iters][N][4]; returns phases [N][nG]
+    (double).  pos3 (float64 [N*3]), mag (float64), imo, nearest (uint32) are
+    updated in place."""
+    N = len(mag)
+    g = np.ascontiguousarray(grads, np.float64).reshape(-1, 3)
+    w = np.ascontiguousarray(wave, np.float64)
+    ph = np.zeros(N * len(g), np.float64)
+    d = np.ascontiguousarray(draws, np.float32).reshape(-1)
+    assert len(d) == 4 * N * len(w)
+    lib().or2_integrate_f64_multi(C.byref(p), N, pos3, mag, imo, nearest, fiberPos, cc, cubes, len(g), g.reshape(-1),
+                                  w, float(phaseConstant), len(w), d, ph, int(nthreads or os.cpu_count() or 1))
     return ph.reshape(N, len(g))
 
 

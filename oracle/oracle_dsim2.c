@@ -382,3 +382,135 @@ void or2_integrate_multi(const or2_params* P, uint32_t N, float* pos4, uint32_t*
         }
     }
 }
+
+/* ---- FP64 restatement (precision oracle for cylinders) ---------------------
+ * step2 with every position-dependent quantity in double: the proposed step,
+ * the distances to the fibers (fiberPos promoted), the clamp, T2 decay and
+ * the phases.  Same rules and branch order as cpuIntegrate
+ * (dSim2/src/spinKernelCpu.cpp:312-641); the draws are the same float stream
+ * as the FP32 walk's. */
+static inline double dist_sq_f64(double px, double py, double pz, const float* f) {
+    const double fx = f[0], fy = f[1], fz = f[2];
+    if (f[0] == 2.0f) return (pz - fz) * (pz - fz) + (py - fy) * (py - fy);
+    else if (f[2] == 2.0f) return (px - fx) * (px - fx) + (py - fy) * (py - fy);
+    return (px - fx) * (px - fx) + (pz - fz) * (pz - fz);
+}
+
+static inline uint32_t cube_hash2_f64(double px, double py, double pz, double L, uint32_t n) {
+    double hi = (double)(n - 1);
+    double cx = fmax(fmin(floor((px + 1.0) / L), hi), 0.0);
+    double cy = fmax(fmin(floor((py + 1.0) / L), hi), 0.0);
+    double cz = fmax(fmin(floor((pz + 1.0) / L), hi), 0.0);
+    return (uint32_t)cz * n * n + (uint32_t)cy * n + (uint32_t)cx;
+}
+
+static void step2_f64(const or2_params* P, double* q, double* mag, uint32_t* imoP, uint32_t* nearP,
+                      const float* FP, const uint32_t* cc, const uint32_t* cubes, double intraSd,
+                      double extraSd, double myelinSd, double inRadPropSq, const float d[4]) {
+    double ox = q[0], oy = q[1], oz = q[2];
+    double px = ox, py = oy, pz = oz;
+    uint32_t nearest = *nearP, imo = *imoP;
+    double u = d[3];
+    double sd = (imo == 0) ? intraSd : ((imo == 1) ? myelinSd : extraSd);
+    px += (double)d[0] * sd;
+    py += (double)d[1] * sd;
+    pz += (double)d[2] * sd;
+    double perm = P->permeability;
+    if (perm < 1.0) {
+        double radSq, cur;
+        if (imo < 2) {
+            const float* f = FP + 4 * (size_t)nearest;
+            radSq = f[3];
+            cur = dist_sq_f64(px, py, pz, f);
+            if (imo == 0) {
+                if ((cur > inRadPropSq * radSq) & (cur <= radSq)) {
+                    if (u >= perm) { px = ox; py = oy; pz = oz; }
+                    else { imo = 1; }
+                } else if (cur > radSq) {
+                    if (u < 1 - perm) { px = ox; py = oy; pz = oz; }
+                    else if ((1 - perm < u) & (u < 1 - perm * perm)) { px = ox; py = oy; pz = oz; imo = 1; }
+                    else { imo = 2; }
+                }
+            } else {
+                if (cur > radSq) {
+                    if (u >= perm) { px = ox; py = oy; pz = oz; }
+                    else { imo = 2; }
+                } else if (cur < inRadPropSq * radSq) {
+                    if (u >= perm) { px = ox; py = oy; pz = oz; }
+                    else { imo = 0; }
+                }
+            }
+            double endD = dist_sq_f64(px, py, pz, f);
+            if (endD > radSq) imo = 2;
+            else if (endD < inRadPropSq * radSq) imo = 0;
+            else imo = 1;
+        } else {
+            uint32_t cube = cube_hash2_f64(px, py, pz, P->cubeLength, P->numCubes);
+            for (uint32_t j = 0; j < cc[cube]; j++) {
+                uint32_t i = cubes[(size_t)cube * P->maxFibersPerCube + j];
+                const float* f = FP + 4 * (size_t)i;
+                radSq = f[3];
+                cur = dist_sq_f64(px, py, pz, f);
+                if ((cur <= radSq) & (cur > inRadPropSq * radSq)) {
+                    if (u >= perm) { px = ox; py = oy; pz = oz; }
+                    else { imo = 1; nearest = i; }
+                } else if (cur < inRadPropSq * radSq) {
+                    if (u < 1 - perm) { px = ox; py = oy; pz = oz; }
+                    else if ((1 - perm < u) & (u < 1 - perm * perm)) { px = ox; py = oy; pz = oz; nearest = i; imo = 1; }
+                    else { imo = 0; nearest = i; }
+                }
+            }
+            cube = cube_hash2_f64(px, py, pz, P->cubeLength, P->numCubes);
+            if (imo == 2) {
+                for (uint32_t j = 0; j < cc[cube]; j++) {
+                    uint32_t i = cubes[(size_t)cube * P->maxFibersPerCube + j];
+                    const float* f = FP + 4 * (size_t)i;
+                    radSq = f[3];
+                    double nd = dist_sq_f64(px, py, pz, f);
+                    if (nd < inRadPropSq * radSq) { px = ox; py = oy; pz = oz; }
+                    else if (nd < radSq) { px = ox; py = oy; pz = oz; }
+                }
+            }
+        }
+    }
+    double sr = P->spinRadius;
+    if (px > 1.0 - sr) { px = 1.0 - sr; } else if (px < -1.0 + sr) { px = -1.0 + sr; }
+    if (py > 1.0 - sr) { py = 1.0 - sr; } else if (py < -1.0 + sr) { py = -1.0 + sr; }
+    if (pz > 1.0 - sr) { pz = 1.0 - sr; } else if (pz < -1.0 + sr) { pz = -1.0 + sr; }
+    q[0] = px; q[1] = py; q[2] = pz;
+    double dt = P->deltaTime;
+    switch (imo) {
+        case 0: *mag += -*mag / (double)P->T2fiber * dt; break;
+        case 1: *mag += -*mag / (double)P->T2myelin * dt; break;
+        case 2: *mag += -*mag / (double)P->T2outside * dt; break;
+    }
+    *imoP = imo;
+    *nearP = nearest;
+}
+
+void or2_integrate_f64_multi(const or2_params* P, uint32_t N, double* pos3, double* mag, uint32_t* imo,
+                             uint32_t* nearest, const float* fiberPos, const uint32_t* cc, const uint32_t* cubes,
+                             uint32_t nG, const double* grads, const double* wave, double phaseConstant,
+                             uint32_t iterations, const float* draws, double* phases, int nthreads) {
+    /* the parameters are the reference's float values (sigma as
+     * cpuIntegrateSystem computes it, dSim2/src/spinKernelCpu.cpp:2-20);
+     * the walk is in double */
+    float fdt = P->deltaTime;
+    double intraSd = sqrtf(2.0f * P->intraAdcScaled * fdt);
+    double extraSd = sqrtf(2.0f * P->extraAdcScaled * fdt);
+    double myelinSd = sqrtf(2.0f * P->myelinAdcScaled * fdt);
+    double inRadPropSq = (double)P->innerRadiusProportion * (double)P->innerRadiusProportion;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
+    for (uint32_t i = 0; i < N; i++) {
+        double* q = pos3 + 3 * (size_t)i;
+        double* ph = phases + (size_t)i * nG;
+        for (uint32_t it = 0; it < iterations; it++) {
+            step2_f64(P, q, mag + i, imo + i, nearest + i, fiberPos, cc, cubes, intraSd, extraSd, myelinSd,
+                      inRadPropSq, draws + ((size_t)it * N + i) * 4);
+            const double w = wave[it];
+            if (w == 0.0) continue;
+            for (uint32_t k = 0; k < nG; k++)
+                ph[k] += w * (grads[3 * k] * q[0] + grads[3 * k + 1] * q[1] + grads[3 * k + 2] * q[2]) * phaseConstant;
+        }
+    }
+}

@@ -307,3 +307,40 @@ def test_multi_gradient_walk_equals_one_run_per_gradient_cylinders(tmp_path):
         assert np.array_equal(_bits(par.reshape(-1, 5)[:, 1]), _bits(ph_m[:, k])), k
         assert np.array_equal(_bits(pos), _bits(pos_m)) and np.array_equal(seed, seed_m)
         assert np.array_equal(_bits(par.reshape(-1, 5)[:, [0, 2, 3]]), _bits(par_m.reshape(-1, 5)[:, [0, 2, 3]]))
+
+
+def test_fp64_cylinder_oracle_tracks_the_fp32_oracle():
+    """The FP64 cylinder walk on the reference's own draws (golden cyl
+    fixture, permeable, myelin shell) stays with the FP32 oracle (pinned to
+    the reference above): regions and positions agree for nearly every spin
+    and the signal to float precision."""
+    from dsim_gb300.engine import grad_scaled, phase_constant
+    g = _load("cyl")
+    prm = json.loads(str(g["params"]))
+    fp = g["fiberPos"]
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, float(g["maxR"][0]))
+    N, iters = prm["N"], prm["iters"]
+    p = O.Params2()
+    ss = np.float32(prm["spaceScale"])
+    p.intraAdcScaled = np.float32(prm["intraAdc"]) / (ss * ss)
+    p.extraAdcScaled = np.float32(prm["extraAdc"]) / (ss * ss)
+    p.myelinAdcScaled = np.float32(prm["myelinAdc"]) / (ss * ss)
+    p.T2fiber, p.T2myelin, p.T2outside = prm["intraT2"], prm["myelinT2"], prm["extraT2"]
+    p.permeability, p.innerRadiusProportion, p.spinRadius, p.deltaTime = prm["perm"], prm["inner"], 0.005, prm["dt"]
+    p.numCubes, p.maxFibersPerCube, p.cubeLength = n, maxfpc, L
+    gs = grad_scaled([prm["gx"], prm["gy"], prm["gz"]], prm["spaceScale"])
+    pc = phase_constant(prm["gamma"], prm["dt"])
+    par0 = g["params0"].reshape(-1, 5)
+    pos3 = g["pos0"].reshape(-1, 4)[:, :3].astype(np.float64).reshape(-1).copy()
+    mag = par0[:, 0].astype(np.float64).copy()
+    imo = par0[:, 3].astype(np.uint32).copy()
+    near = par0[:, 2].astype(np.uint32).copy()
+    ph = O.integrate2_f64_multi(p, pos3, mag, imo, near, fp, cc, cubes, gs[None, :].astype(np.float64),
+                                np.ones(iters), float(pc), g["draws"], nthreads=2)
+    par1 = g["params1"].reshape(-1, 5)
+    d = np.abs(pos3.reshape(-1, 3) - g["pos1"].reshape(-1, 4)[:, :3].astype(np.float64)).max(1)
+    assert (d < 1e-5).mean() >= 0.95
+    assert (imo == par1[:, 3].astype(np.uint32)).mean() >= 0.95
+    ok = d < 1e-5
+    assert np.allclose(ph[ok, 0], par1[ok, 1], rtol=1e-4, atol=1e-4)
+    assert np.allclose(mag[ok], par1[ok, 0], rtol=1e-5)
