@@ -647,10 +647,16 @@ def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False, sub
     return subs, mix
 
 
-def _submit_kw(j):
-    return dict(steps=j["steps"], dt=j["dt"], step_sd=j["step_sd"], T2=j["T2"], phase_constant=j["phase_constant"],
-                seed=j["seed"], permeability=j["permeability"], waveform="pgse", delta=j["delta"],
-                Delta=j["Delta"], inner_radius_proportion=j["inner"])
+def _submit_kw(j, form="fp32"):
+    """Job keywords; form "fp32": the plain FP32 step with Kahan moments;
+    "bar": the forms that hold the 1e-3 signal-error bar (mesh jobs
+    cell-local, DSIM_JOB_LOCAL; cylinder jobs FP64 positions, DSIM_JOB_PRECISE)."""
+    kw = dict(steps=j["steps"], dt=j["dt"], step_sd=j["step_sd"], T2=j["T2"], phase_constant=j["phase_constant"],
+              seed=j["seed"], permeability=j["permeability"], waveform="pgse", delta=j["delta"],
+              Delta=j["Delta"], inner_radius_proportion=j["inner"])
+    if form == "bar":
+        kw.update(local=j["sub"].kind == "mesh", precise=j["sub"].kind != "mesh")
+    return kw
 
 
 def run_plain_mix(mix):
@@ -680,14 +686,14 @@ def run_plain_mix(mix):
     return per
 
 
-def run_batched_mix(subs, mix, cfg):
+def run_batched_mix(subs, mix, cfg, form="fp32"):
     from dsim_gb300.engine import Batch
     cap = sum((j["n"] + 31) // 32 * 32 for j in mix)
     b = Batch(cap, len(mix))
     sids = {id(sb): (b.add_mesh(sb.handle) if sb.kind == "mesh" else b.add_cyl(sb.handle)) for sb in subs}
     b.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
     t0 = time.perf_counter()
-    ids = [b.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], **_submit_kw(j)) for j in mix]
+    ids = [b.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], **_submit_kw(j, form)) for j in mix]
     b.run()
     sigs = [b.signal(i, j["grads"]) for i, j in zip(ids, mix)]
     el = time.perf_counter() - t0
@@ -711,7 +717,7 @@ def tune_mix(subs, mix):
     return best, ms
 
 
-def run_served_mix(subs, mix, cfg, rate, seed=3):
+def run_served_mix(subs, mix, cfg, rate, seed=3, form="bar"):
     """Poisson arrivals at `rate` jobs/s into the request loop."""
     from dsim_gb300.engine import Server
     cap = max(sum((j["n"] + 31) // 32 * 32 for j in mix) // 2, max((j["n"] + 31) // 32 * 32 for j in mix))
@@ -729,7 +735,8 @@ def run_served_mix(subs, mix, cfg, rate, seed=3):
         d = t_next - time.perf_counter()
         if d > 0:
             time.sleep(d)
-        tickets.append(srv.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], j["grads"], **_submit_kw(j)))
+        tickets.append(srv.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], j["grads"],
+                                  **_submit_kw(j, form)))
     srv.drain()
     st = srv.stats()
     srv.stop()
@@ -772,45 +779,53 @@ def mix_fp64_reference(mix, ns_cyl=2048):
             ref[i] = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
         b.close()
     if cyl:
-        nsam = {i: min(mix[i]["n"], ns_cyl) for i in cyl}
-        b = Batch(sum((nsam[i] + 31) // 32 * 32 for i in cyl), len(cyl))
+        # cylinder jobs: the precision form on the GPU (the dSim2 step in
+        # double, equal to the FP64 oracle bit for bit), whole jobs
+        b = Batch(sum((mix[i]["n"] + 31) // 32 * 32 for i in cyl), len(cyl))
         sids = {}
         for i in cyl:
             if id(mix[i]["sub"]) not in sids:
                 sids[id(mix[i]["sub"])] = b.add_cyl(mix[i]["sub"].handle)
-        ids = {}
-        for i in cyl:
-            j, n = mix[i], nsam[i]
-            ids[i] = b.submit(sids[id(j["sub"])], j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], **_submit_kw(j))
+        ids = {i: b.submit(sids[id(mix[i]["sub"])], mix[i]["pos"], mix[i]["comp"], mix[i]["fiber"], precise=True,
+                           **_submit_kw(mix[i])) for i in cyl}
         b.run()
         for i in cyl:
-            j, n = mix[i], nsam[i]
-            _, bmag, bmom, _, _ = b.get(ids[i], n)
-            z32 = _z_from_moments(bmag, bmom, j["grads"], j["phase_constant"])
-            ss = F(j["sub"].spaceScale)
-            adc = tuple(F(a) / (ss * ss) for a in (2.0, 0.2, 2.0))      # intra, myelin, extra (jobs.make_job)
-            wave = pgse_table(j["steps"], float(j["dt"]), j["delta"], j["Delta"])
-            z64, _ = cyl_fp64_z(j["sub"].handle, j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], adc, j["T2"],
-                                j["permeability"], j["inner"], j["dt"], j["phase_constant"], j["grads"], wave,
-                                j["seed"])
-            cyl_err[i] = np.abs(_S(z32) - _S(z64))
+            sums = b.signal(ids[i], mix[i]["grads"])
+            ref[i] = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
         b.close()
+        # and the FP64 oracle itself (CPU) on the first spins of the first cylinder job
+        i = cyl[0]
+        j, n = mix[i], min(mix[i]["n"], ns_cyl)
+        b = Batch((n + 31) // 32 * 32, 2)
+        sid = b.add_cyl(j["sub"].handle)
+        j64 = b.submit(sid, j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], precise=True, **_submit_kw(j))
+        b.run()
+        _, bmag, bmom, _, _ = b.get(j64, n)
+        b.close()
+        ss = F(j["sub"].spaceScale)
+        adc = tuple(F(a) / (ss * ss) for a in (2.0, 0.2, 2.0))      # intra, myelin, extra (jobs.make_job)
+        wave = pgse_table(j["steps"], float(j["dt"]), j["delta"], j["Delta"])
+        z64, _ = cyl_fp64_z(j["sub"].handle, j["pos"][:3 * n], j["comp"][:n], j["fiber"][:n], adc, j["T2"],
+                            j["permeability"], j["inner"], j["dt"], j["phase_constant"], j["grads"], wave, j["seed"])
+        cyl_err["oracle_check_max_abs_dS"] = float(np.max(np.abs(_S(_z_from_moments(bmag, bmom, j["grads"],
+                                                                                     j["phase_constant"])) - _S(z64))))
     return ref, cyl_err
 
 
 def mix_err(mix, sigs, ref, cyl_err):
-    """Per-form error summary: mesh jobs from the form's own signals `sigs`
-    (per job, sums [nG][5][3]) against the FP64 form; cylinder jobs on their
-    spin sample (mix_fp64_reference)."""
-    me = [np.abs(np.hypot(sigs[i][:, 0, 0], sigs[i][:, 0, 1]) / sigs[i][:, 0, 2] - ref[i]) for i in ref]
-    ce = list(cyl_err.values())
-    allv = np.concatenate(me + ce) if (me or ce) else np.zeros(1)
-    out = {"all": _err_summary(allv, "FP64 on the same Philox draws")}
+    """A form's error summary: every job's signals `sigs` (sums [nG][5][3]) against
+    the FP64 references of mix_fp64_reference (whole jobs, same draws)."""
+    d = {i: np.abs(np.hypot(sigs[i][:, 0, 0], sigs[i][:, 0, 1]) / sigs[i][:, 0, 2] - ref[i]) for i in ref}
+    me = [d[i] for i in d if mix[i]["sub"].kind == "mesh"]
+    ce = [d[i] for i in d if mix[i]["sub"].kind != "mesh"]
+    out = {"all": _err_summary(np.concatenate(me + ce), "FP64 on the same Philox draws, whole jobs")}
     if me:
-        out["mesh_jobs"] = _err_summary(np.concatenate(me), "FP64 form on the GPU, whole jobs")
+        out["mesh_jobs"] = _err_summary(np.concatenate(me), "the FP64 form (equal to the FP64 oracle bit for bit)")
     if ce:
-        out["cylinder_jobs"] = _err_summary(np.concatenate(ce), "FP64 oracle walk (CPU), first 2048 spins of each "
-                                                                 "job against the same spins in FP32")
+        out["cylinder_jobs"] = _err_summary(np.concatenate(ce), "the FP64 form (equal to the FP64 oracle bit for "
+                                                                 "bit)")
+    if "oracle_check_max_abs_dS" in cyl_err:
+        out["cylinder_fp64_form_vs_oracle_max_abs_dS"] = cyl_err["oracle_check_max_abs_dS"]
     return out
 
 
@@ -848,8 +863,16 @@ def run_forms(args, W, m):
                     "note": "all jobs in one batch; signals_speedup counts one plain walk per gradient, as the "
                             "reference re-walks every gradient",
                     "autotuned": best, "kernel_launches": info["launches"], "graph_launches": info["graph_launches"],
-                    "status": st, "err_vs_fp64": batched_err},
+                    "status": st, "err_vs_fp64": batched_err, "form": "fp32: the plain FP32 step, Kahan moments"},
     }
+    # the same mix in the forms that hold the 1e-3 error bar
+    el_b, sigs_b, info_b, st_b = run_batched_mix(subs, mix, cfg, form="bar")
+    out["batched_bar"] = {"spin_steps_per_s": work / el_b, "seconds": el_b,
+                          "speedup_vs_plain": (work / el_b) / plain_rate,
+                          "signals_speedup_vs_plain": (grad_work / el_b) / plain_rate,
+                          "status": st_b, "err_vs_fp64": mix_err(mix, sigs_b, ref, cyl_err),
+                          "form": "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions "
+                                  "(DSIM_JOB_PRECISE)"}
     # serving: the same substrates and ranges with permeable membranes (per-hit
     # permeation log-uniform 1e-4 - 1e-2); arrival rates relative to the plain
     # form's capacity on that mix
@@ -866,6 +889,7 @@ def run_forms(args, W, m):
             o, ssig = run_served_mix(subs, pmix, cfg, r * cap_jobs)
             o["rate_x_plain_capacity"] = r
             o["err_vs_fp64"] = mix_err(pmix, ssig, pref, pcyl)
+            o["form"] = "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
             out["served"].append(o)
     return out
 
@@ -942,7 +966,22 @@ def run_cylinders(args):
     for k in range(len(gs) - 6, len(gs)):          # 80 mT/m along each of the 6 directions
         zk, pk = cyl_fp64_z(c, pos, imo, near, adc, [0, 0, 0], 0.0, 1.0, dt, pc, gs[k][None, :], w, k + 1)
         err_plain.append(abs(plain_S[k] - float(_S(zk, in_box(pk))[0])))
+    # the shared walk in the cylinder precision form (FP64 positions)
+    b = Batch((N + 31) // 32 * 32, 1)
+    sid = b.add_cyl(c)
+    t0 = time.perf_counter()
+    j = b.submit(sid, pos.reshape(-1), imo, near, steps, dt, sd, T2, pc, 1, waveform="pgse", delta=delta,
+                 Delta=Delta, inner_radius_proportion=1.0, precise=True)
+    b.run()
+    sums = b.signal(j, gs, region=0.8)
+    prec_s = time.perf_counter() - t0
+    S_prec = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
+    b.close()
     err = {"shared_walk": _err_summary(err_shared, "FP64 oracle walk on the same Philox draws, all 48 gradients"),
+           "shared_walk_precise": dict(_err_summary(np.abs(S_prec - _S(z64, in_box(p64))), "FP64 oracle walk on "
+                                                    "the same Philox draws, all 48 gradients"),
+                                       form="DSIM_JOB_PRECISE: the dSim2 step with FP64 positions",
+                                       spin_steps_per_s=N * steps / prec_s),
            "plain": _err_summary(err_plain, "FP64 oracle walk on each walk's Philox draws, 80 mT/m along the "
                                             "6 directions"),
            "seconds": time.perf_counter() - t_err}

@@ -423,7 +423,7 @@ k_batch_step64(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs,
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
-    if (!(J.flags & DSIM_JOB_PRECISE)) return;  // warp-uniform
+    if (!(J.flags & DSIM_JOB_PRECISE) || subS[wi].kind != kSubMesh) return;  // warp-uniform
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;
@@ -618,9 +618,11 @@ __global__ void k_batch_gather64(BatchSpins S, uint32_t slot0, uint32_t len, dou
 
 // FP64 signal of one job for nG gradients: partial records per (block, g)
 static constexpr int kSigThreads = 256;
+// fp64: the job keeps FP64 positions and magnitudes (precision and
+// cell-local forms), which the readout then uses
 __global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint32_t slot0, uint32_t len,
                                                               const double* __restrict__ kg, uint32_t nG,
-                                                              double region, double* partials) {
+                                                              double region, bool fp64, double* partials) {
     __shared__ double sh[kSigThreads / 32][15];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (uint32_t gi = 0; gi < nG; gi++) {
@@ -632,14 +634,16 @@ __global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint
             const uint32_t i = slot0 + k;
             if (S.u[U_ID][i] == 0xFFFFFFFFu) continue;
             if (region > 0.0) {  // dSim2's readout box (dSim2/src/spinSystem.cpp:944-978)
-                const double x = S.f[F_X][i], y = S.f[F_Y][i], z = S.f[F_Z][i];
+                const double x = fp64 ? S.d[D_X][i] : (double)S.f[F_X][i];
+                const double y = fp64 ? S.d[D_Y][i] : (double)S.f[F_Y][i];
+                const double z = fp64 ? S.d[D_Z][i] : (double)S.f[F_Z][i];
                 if (!(x > -region && x < region && y > -region && y < region && z > -region && z < region)) continue;
             }
             const double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
             const double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
             const double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
             const double ph = gx * Mx + gy * My + gz * Mz;
-            const double m = S.f[F_MAG][i];
+            const double m = fp64 ? S.d[D_MAG][i] : (double)S.f[F_MAG][i];
             double s, c;
             sincos(ph, &s, &c);
             const double X = m * c, Y = m * s;
@@ -723,7 +727,8 @@ struct dsim_batch {
     uint32_t *hist = nullptr, *hstart = nullptr, *scratch = nullptr;
     uint64_t keyCap = 0, K = 0;
     uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
-    bool anyPrecise = false, anyLocal = false;
+    bool anyPrecise = false, anyLocal = false;  // precision-form / cell-local mesh jobs
+    bool anyPreciseCyl = false;                 // precision-form cylinder jobs
     cudaGraphExec_t exec = nullptr;
     bool graphValid = false;
     int graphCur = -1;
@@ -814,7 +819,87 @@ uint32_t step_layouts(const dsim_batch* b) {
 uint64_t chunk_launches(const dsim_batch* b) {
     const uint32_t mask = step_layouts(b);
     return 5ull + (uint64_t)__builtin_popcount(mask & 0xEu) + (b->anyPrecise ? 1ull : 0ull) +
-           (b->anyLocal ? 1ull : 0ull) + 1ull;
+           (b->anyLocal ? 1ull : 0ull) + (b->anyPreciseCyl ? 1ull : 0ull) + 1ull;
+}
+
+// Precision-form cylinder jobs (DSIM_JOB_PRECISE): the dSim2 step of
+// cpuIntegrate (dSim2/src/spinKernelCpu.cpp:312-641) with positions,
+// distances, clamp, T2 decay and moments in double (cyl_membranes64); the
+// parameters are the job's float values.  Position and magnitude persist in
+// the double fields; the moment is kept as the float pair m - c.
+__global__ void __launch_bounds__(kFlatThreads, 4)
+k_batch_step_cyl64(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
+                   const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
+                   unsigned long long* jobCounts) {
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
+    const uint32_t jb = S.u[U_JOB][i & ~31u];
+    const JobDev& J = jobs[jb];
+    if (!(__ldg(&J.flags) & DSIM_JOB_PRECISE)) return;  // warp-uniform
+    const SubDev& sub = subs[__ldg(&J.sub)];
+    if (__ldg(&sub.kind) != kSubCyl) return;
+    const uint32_t now = *stepNow;
+    const uint32_t start = __ldg(&J.start), steps = __ldg(&J.steps);
+    if (now < start || now - start >= steps) return;
+    const uint32_t ls0 = now - start;
+    const uint32_t nsteps = min(chunk, steps - ls0);
+    const uint32_t id = S.u[U_ID][i];
+    const bool valid = id != 0xFFFFFFFFu;
+    uint32_t nrefl = 0, nperm = 0, st = 0;
+    if (valid) {
+        const CylDev g = sub.c;
+        double x = S.d[D_X][i], y = S.d[D_Y][i], z = S.d[D_Z][i], mag = S.d[D_MAG][i];
+        double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
+        double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
+        double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
+        const uint32_t meta = S.u[U_META][i];
+        uint32_t imo = meta & 0xFFu, nearest = meta >> 8;
+        if (imo < 2 && nearest >= g.nF) imo = 2;
+        const double perm = (double)__ldg(&J.perm), inR = (double)__ldg(&J.inR);
+        const double hiC = 1.0 - (double)__ldg(&J.spinR), loC = -1.0 + (double)__ldg(&J.spinR);
+        const double dt = (double)__ldg(&J.dt);
+        const uint32_t k0 = __ldg(&J.key0), k1 = __ldg(&J.key1);
+        const float* __restrict__ wave = J.wave;
+        for (uint32_t it = 0; it < nsteps; it++) {
+            const Draw d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+            const double ox = x, oy = y, oz = z;
+            const double sd = (double)__ldg(&J.sd[imo == 0 ? 0 : (imo == 1 ? 1 : 2)]);
+            double px = x + (double)d.nx * sd, py = y + (double)d.ny * sd, pz = z + (double)d.nz * sd;
+            cyl_membranes64(g, ox, oy, oz, px, py, pz, (double)d.u, perm, inR, imo, nearest, nrefl, nperm, st);
+            if (px > hiC) px = hiC; else if (px < loC) px = loC;
+            if (py > hiC) py = hiC; else if (py < loC) py = loC;
+            if (pz > hiC) pz = hiC; else if (pz < loC) pz = loC;
+            x = px; y = py; z = pz;
+            if (imo <= 2) {
+                const float T2 = __ldg(&J.T2[imo]);
+                if (T2 > 0.0f) mag += -mag / (double)T2 * dt;
+            }
+            const double w = (double)__ldg(wave + ls0 + it);
+            Mx += w * x; My += w * y; Mz += w * z;
+        }
+        S.d[D_X][i] = x; S.d[D_Y][i] = y; S.d[D_Z][i] = z; S.d[D_MAG][i] = mag;
+        S.f[F_X][i] = (float)x; S.f[F_Y][i] = (float)y; S.f[F_Z][i] = (float)z;
+        S.f[F_MAG][i] = (float)mag;
+        const float mx = (float)Mx, my = (float)My, mz = (float)Mz;
+        S.f[F_MX][i] = mx; S.f[F_MY][i] = my; S.f[F_MZ][i] = mz;
+        S.f[F_CX][i] = (float)((double)mx - Mx);
+        S.f[F_CY][i] = (float)((double)my - My);
+        S.f[F_CZ][i] = (float)((double)mz - Mz);
+        S.u[U_META][i] = (imo & 0xFFu) | ((nearest & 0xFFFFFFu) << 8);
+    }
+    unsigned long long r = nrefl, p = nperm;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        p += __shfl_down_sync(FULL, p, o);
+    }
+    if (lane == 0) {
+        if (r) atomicAdd(jobCounts + 4 * jb, r);
+        if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+    }
+    if (st) atomicOr(status, st);
 }
 
 template <int LAYOUT>
@@ -853,6 +938,9 @@ int enqueue_chunk(dsim_batch* b) {
     if (b->anyPrecise)
         k_batch_step64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status,
                                                          b->d_counts);
+    if (b->anyPreciseCyl)
+        k_batch_step_cyl64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                             b->d_status, b->d_counts);
     k_batch_advance<<<1, 1, 0, b->st>>>(b->d_stepNow, b->chunk);
     DSIM_CUDA_TRY(cudaGetLastError());
     b->launches += chunk_launches(b);  // keys, scan (3), scatter, step (per layout), advance
@@ -1004,11 +1092,14 @@ int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate) {
 // first precision-form job on a substrate: the mesh's FP64 triangle table, and
 // for the batch the FP64 state fields of both spin buffers
 static int ensure_precise(dsim_batch* b, uint32_t substrate) {
-    dsim_mesh* m = const_cast<dsim_mesh*>(b->meshes[substrate]);
-    int rc = mesh_tri64(m);
-    if (rc) return rc;
+    int rc = kOk;
     SubDev& sd = b->subs[substrate];
-    if (!sd.g.tri64) {
+    if (sd.kind == kSubMesh) {
+        dsim_mesh* m = const_cast<dsim_mesh*>(b->meshes[substrate]);
+        if ((rc = mesh_tri64(m))) return rc;
+    }
+    if (sd.kind == kSubMesh && !sd.g.tri64) {
+        dsim_mesh* m = const_cast<dsim_mesh*>(b->meshes[substrate]);
         if ((rc = mesh_views(m, &sd.g, &sd.acc))) return rc;
         DSIM_CUDA_TRY(cudaMemcpyAsync(b->d_subs + substrate, &sd, sizeof(SubDev), cudaMemcpyHostToDevice, b->st));
         invalidate_graph(b);
@@ -1064,8 +1155,8 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
         return kErrInvalid;
     }
     J.spinR = d->spinRadius;
-    if (J.flags && cyl) {
-        set_last_error(kErrInvalid, "dsim_batch_submit: the precision and cell-local forms apply to mesh jobs");
+    if ((J.flags & DSIM_JOB_LOCAL) && cyl) {
+        set_last_error(kErrInvalid, "dsim_batch_submit: the cell-local form applies to mesh jobs");
         return kErrInvalid;
     }
     if (J.flags) {
@@ -1127,7 +1218,7 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
     DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 4 * jobIndex, 0, 32, b->st));
     DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
-    if (J.flags & DSIM_JOB_PRECISE) b->anyPrecise = true;
+    if (J.flags & DSIM_JOB_PRECISE) (cyl ? b->anyPreciseCyl : b->anyPrecise) = true;
     if (J.flags & DSIM_JOB_LOCAL) b->anyLocal = true;
     invalidate_graph(b);
     *jobId = j.id;
@@ -1226,7 +1317,8 @@ int dsim_batch_signal_region(dsim_batch* b, uint32_t jobId, const float* gradSca
     b->bytes -= kg.size() * 8 + (size_t)nb * nG * 15 * 8 + (size_t)nG * 15 * 8;
     cudaError_t e = cudaMemcpyAsync(dk, kg.data(), kg.size() * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) {
-        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, region, dp);
+        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, region,
+                                                          j->d.flags != 0 && b->buf[b->cur].d[0] != nullptr, dp);
         k_batch_signal_final<<<(nG * 15 + 127) / 128, 128, 0, b->st>>>(dp, nb, nG, dout);
         e = cudaGetLastError();
     }
@@ -1387,9 +1479,10 @@ int dsim_batch_compact(dsim_batch* b) {
     b->cur = 1 - b->cur;
     b->jobs = kept;
     b->N = slot;
-    b->anyPrecise = b->anyLocal = false;
+    b->anyPrecise = b->anyLocal = b->anyPreciseCyl = false;
     for (const auto& j : b->jobs) {
-        b->anyPrecise |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
+        const bool jc = b->subs[j.d.sub].kind == kSubCyl;
+        (jc ? b->anyPreciseCyl : b->anyPrecise) |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
         b->anyLocal |= (j.d.flags & DSIM_JOB_LOCAL) != 0;
     }
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;

@@ -191,4 +191,168 @@ __device__ __forceinline__ void cyl_membranes(const CylDev& g, float ox, float o
     }
 }
 
+// ---- the same rules with positions and distances in double ----------------
+// (the cylinder precision form, DSIM_JOB_PRECISE).  Parameters are the
+// reference's float values (fiber records, r^2, inner radius proportion
+// squared, permeability, draws) promoted to double; every position-dependent
+// quantity is formed in double in the same order as the FP32 rules above.
+__device__ __forceinline__ uint32_t cyl_cell64(double px, double py, double pz, float L, uint32_t n) {
+    const double inv = 1.0 / (double)L;
+    const double hi = (double)(n - 1);
+    const double cx = fmax(fmin(floor((px + 1.0) * inv), hi), 0.0);
+    const double cy = fmax(fmin(floor((py + 1.0) * inv), hi), 0.0);
+    const double cz = fmax(fmin(floor((pz + 1.0) * inv), hi), 0.0);
+    return (uint32_t)cz * n * n + (uint32_t)cy * n + (uint32_t)cx;
+}
+
+__device__ __forceinline__ double cyl_dist_sq64(double px, double py, double pz, float4 f) {
+    const double fx = f.x, fy = f.y, fz = f.z;
+    if (f.x == 2.0f) return (pz - fz) * (pz - fz) + (py - fy) * (py - fy);
+    else if (f.z == 2.0f) return (px - fx) * (px - fx) + (py - fy) * (py - fy);
+    return (px - fx) * (px - fx) + (pz - fz) * (pz - fz);
+}
+
+// the fine cell of p in grid cell `cube`; the fine lists are registered in
+// double against cells widened by 1e-5, so every entry able to act at p is in
+// the list of the cell this picks
+__device__ __forceinline__ uint32_t cyl_fine_cell64(const CylDev& g, double px, double py, double pz, uint32_t cube) {
+    const uint32_t n = g.n, k = g.fineK, nk = n * k;
+    const uint32_t cx = cube % n, cy = (cube / n) % n, cz = cube / (n * n);
+    const double hi = (double)(k - 1), inv = (double)g.fineInv;
+    const double sx = fmin(fmax(floor((px + 1.0) * inv) - (double)(cx * k), 0.0), hi);
+    const double sy = fmin(fmax(floor((py + 1.0) * inv) - (double)(cy * k), 0.0), hi);
+    const double sz = fmin(fmax(floor((pz + 1.0) * inv) - (double)(cz * k), 0.0), hi);
+    return ((cz * k + (uint32_t)sz) * nk + (cy * k + (uint32_t)sy)) * nk + cx * k + (uint32_t)sx;
+}
+
+__device__ __forceinline__ void cyl_outside_entry64(float4 f, const uint32_t* list, uint32_t j, double ox, double oy,
+                                                    double oz, double& px, double& py, double& pz, double u,
+                                                    double perm, double inR, uint32_t& imo, uint32_t& nearest,
+                                                    uint32_t& nrej, uint32_t& nperm, bool& moved, bool& inside) {
+    const double radSq = f.w;
+    const double cur = cyl_dist_sq64(px, py, pz, f);
+    inside |= (cur < inR * radSq) | (cur < radSq);
+    if ((cur <= radSq) & (cur > inR * radSq)) {
+        if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else { imo = 1; nearest = __ldg(list + j); nperm++; }
+    } else if (cur < inR * radSq) {
+        if (u < 1.0 - perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else if ((1.0 - perm < u) & (u < 1.0 - perm * perm)) {
+            px = ox; py = oy; pz = oz; nearest = __ldg(list + j); imo = 1; nrej++;
+            moved = true;
+        } else { imo = 0; nearest = __ldg(list + j); nperm++; }
+    }
+}
+
+__device__ __forceinline__ void cyl_membranes64(const CylDev& g, double ox, double oy, double oz, double& px,
+                                                double& py, double& pz, double u, double perm, double inR,
+                                                uint32_t& imo, uint32_t& nearest, uint32_t& nrej, uint32_t& nperm,
+                                                uint32_t& status) {
+    if (!(perm < 1.0)) return;
+    if (imo < 2) {
+        const float4 f = __ldg(g.fibers + nearest);
+        const double radSq = f.w;
+        const double cur = cyl_dist_sq64(px, py, pz, f);
+        if (imo == 0) {
+            if ((cur > inR * radSq) & (cur <= radSq)) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 1; nperm++; }
+            } else if (cur > radSq) {
+                if (u < 1.0 - perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else if ((1.0 - perm < u) & (u < 1.0 - perm * perm)) {
+                    px = ox; py = oy; pz = oz; imo = 1; nrej++;
+                } else { imo = 2; nperm++; }
+            }
+        } else {
+            if (cur > radSq) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 2; nperm++; }
+            } else if (cur < inR * radSq) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 0; nperm++; }
+            }
+        }
+        const double endD = cyl_dist_sq64(px, py, pz, f);
+        if (endD > radSq) imo = 2;
+        else if (endD < inR * radSq) imo = 0;
+        else imo = 1;
+        return;
+    }
+    uint32_t cube = cyl_cell64(px, py, pz, g.L, g.n);
+    uint32_t cnt = __ldg(g.cube_count + cube);
+    const uint32_t* list = g.cubes + (size_t)cube * g.maxFPC;
+    const float4* inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
+    bool moved = false, inside = false;
+    const bool fine = g.fine_start != nullptr && inR <= 1.0;
+    uint32_t j = 0;
+    if (fine) {
+        const uint32_t fc = cyl_fine_cell64(g, px, py, pz, cube);
+        const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+        j = cnt;
+        uint32_t jm = 0;
+        for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+            const uint32_t jj = __ldg(g.fine_pos + e);
+            cyl_outside_entry64(__ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR, imo, nearest,
+                                nrej, nperm, moved, inside);
+            if (moved) { jm = jj; break; }
+        }
+        if (moved) {
+            if (cyl_cell64(px, py, pz, g.L, g.n) == cube) {
+                const uint32_t fo = cyl_fine_cell64(g, px, py, pz, cube);
+                const uint32_t eo1 = __ldg(g.fine_start + fo + 1);
+                for (uint32_t e = __ldg(g.fine_start + fo); e < eo1; e++) {
+                    const uint32_t jj = __ldg(g.fine_pos + e);
+                    if (jj <= jm) continue;
+                    cyl_outside_entry64(__ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR, imo,
+                                        nearest, nrej, nperm, moved, inside);
+                }
+            } else {
+                j = jm + 1;
+            }
+        }
+    }
+    for (; j < cnt; j++) {
+        float4 f;
+        if (inl) {
+            f = __ldg(inl + j);
+        } else {
+            const uint32_t fi = __ldg(list + j);
+            if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+            f = __ldg(g.fibers + fi);
+        }
+        cyl_outside_entry64(f, list, j, ox, oy, oz, px, py, pz, u, perm, inR, imo, nearest, nrej, nperm, moved,
+                            inside);
+    }
+    if (imo == 2 && (moved || inside)) {
+        cube = cyl_cell64(px, py, pz, g.L, g.n);
+        cnt = __ldg(g.cube_count + cube);
+        list = g.cubes + (size_t)cube * g.maxFPC;
+        inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
+        if (fine && moved) {
+            const uint32_t fc = cyl_fine_cell64(g, px, py, pz, cube);
+            const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+            for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+                const float4 f = __ldg(g.fine_rec + e);
+                const double nd = cyl_dist_sq64(px, py, pz, f);
+                if (nd < inR * (double)f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                else if (nd < (double)f.w) { px = ox; py = oy; pz = oz; nrej++; }
+            }
+        } else {
+            for (uint32_t j2 = 0; j2 < cnt; j2++) {
+                float4 f;
+                if (inl) {
+                    f = __ldg(inl + j2);
+                } else {
+                    const uint32_t fi = __ldg(list + j2);
+                    if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+                    f = __ldg(g.fibers + fi);
+                }
+                const double nd = cyl_dist_sq64(px, py, pz, f);
+                if (nd < inR * (double)f.w) { px = ox; py = oy; pz = oz; nrej++; }
+                else if (nd < (double)f.w) { px = ox; py = oy; pz = oz; nrej++; }
+            }
+        }
+    }
+}
+
 }  // namespace dsim

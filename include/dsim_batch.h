@@ -53,7 +53,7 @@ typedef struct {
     float frequency;               /* Hz (OGSE) */
     const float* table;            /* DSIM_WAVE_TABLE: `steps` values (host) */
     uint64_t seed;                 /* Philox key; counter = (spin, step, 0) */
-    uint32_t flags;                /* DSIM_JOB_PRECISE or DSIM_JOB_LOCAL (mesh jobs) */
+    uint32_t flags;                /* DSIM_JOB_PRECISE (mesh or cylinder jobs) or DSIM_JOB_LOCAL (mesh jobs) */
     uint32_t reserved;
 } dsim_job_desc;
 
@@ -62,8 +62,12 @@ typedef struct {
  * formulas of dSim3/src/spinSystem.cpp:612-648 in double), reflections, the
  * clamp, T2 decay and the gradient moments -- on the same draws as the plain
  * form; FP32 only prunes fine-grid records whose plane lies clearly off the
- * sub-segment.  Positions and magnitudes persist in FP64
- * (dsim_batch_get_precise); dsim_batch_get returns them rounded to float. */
+ * sub-segment.  For a cylinder job it is the dSim2 step
+ * (dSim2/src/spinKernelCpu.cpp:312-641) with positions, distances to the
+ * fibers, the clamp, T2 decay and moments in FP64 (the fiber records and the
+ * other parameters are the job's float values).  Positions and magnitudes
+ * persist in FP64 (dsim_batch_get_precise); dsim_batch_get returns them
+ * rounded to float. */
 #define DSIM_JOB_PRECISE 1u
 /* Cell-local form: the plain FP32 step with every position held as an FP32
  * offset from a lattice origin (a multiple of 1/16 in normalised units), so

@@ -396,11 +396,14 @@ static inline double dist_sq_f64(double px, double py, double pz, const float* f
     return (px - fx) * (px - fx) + (pz - fz) * (pz - fz);
 }
 
-static inline uint32_t cube_hash2_f64(double px, double py, double pz, double L, uint32_t n) {
+/* calcCubePos/calcCubeHash in double, multiplying by the reciprocal as the
+ * reference's float3 division does (cube_hash2 above) */
+static inline uint32_t cube_hash2_f64(double px, double py, double pz, float L, uint32_t n) {
+    double inv = 1.0 / (double)L;
     double hi = (double)(n - 1);
-    double cx = fmax(fmin(floor((px + 1.0) / L), hi), 0.0);
-    double cy = fmax(fmin(floor((py + 1.0) / L), hi), 0.0);
-    double cz = fmax(fmin(floor((pz + 1.0) / L), hi), 0.0);
+    double cx = fmax(fmin(floor((px + 1.0) * inv), hi), 0.0);
+    double cy = fmax(fmin(floor((py + 1.0) * inv), hi), 0.0);
+    double cz = fmax(fmin(floor((pz + 1.0) * inv), hi), 0.0);
     return (uint32_t)cz * n * n + (uint32_t)cy * n + (uint32_t)cx;
 }
 
@@ -499,7 +502,7 @@ void or2_integrate_f64_multi(const or2_params* P, uint32_t N, double* pos3, doub
     double intraSd = sqrtf(2.0f * P->intraAdcScaled * fdt);
     double extraSd = sqrtf(2.0f * P->extraAdcScaled * fdt);
     double myelinSd = sqrtf(2.0f * P->myelinAdcScaled * fdt);
-    double inRadPropSq = (double)P->innerRadiusProportion * (double)P->innerRadiusProportion;
+    double inRadPropSq = P->innerRadiusProportion * P->innerRadiusProportion;
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads)
     for (uint32_t i = 0; i < N; i++) {
         double* q = pos3 + 3 * (size_t)i;

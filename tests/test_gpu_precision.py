@@ -126,11 +126,11 @@ def test_precision_form_signal_matches_fp64_oracle(engine, tmp_path):
             S = np.abs(np.sum(gmag[:, None] * np.exp(1j * float(case.pc) * (M @ gs.T)), 0)) / case.N
             S64 = np.abs(np.sum(mag64[:, None] * np.exp(1j * float(case.pc) * (M64[:, k, :] @ gs.T)), 0)) / case.N
             worst = max(worst, float(np.abs(S - S64).max()))
-            # the device's FP64 reduction (float magnitudes) of the same moments
+            # the device's FP64 reduction of the same moments reads the FP64 magnitudes
             sig = b.signal(j, gs.astype(F))
             Sd = np.hypot(sig[:, 0, 0], sig[:, 0, 1]) / sig[:, 0, 2]
-            Sb = np.abs(np.sum(bmag[:, None] * np.exp(1j * float(case.pc) * (M @ gs.T)), 0)) / case.N
-            assert np.allclose(Sd, Sb, rtol=1e-9, atol=1e-12)
+            assert np.allclose(Sd, S, rtol=1e-9, atol=1e-12)
+            assert np.allclose(Sd, S64, rtol=0, atol=1e-9)
     assert worst <= 1e-9, worst
     # the plain job sharing the batch with precision-form jobs equals the job alone
     for a, w in zip(b.get(plain, case.N), alone):
@@ -239,3 +239,76 @@ def test_cell_local_form_tracks_fp64_oracle_closer_than_plain(engine, tmp_path):
         S = np.abs(np.sum(lmag[:, None] * np.exp(1j * float(case.pc) * (M @ gs.T)), 0)) / case.N
         S64 = np.abs(np.sum(mag64[:, None] * np.exp(1j * float(case.pc) * (M64[:, 0, :] @ gs.T)), 0)) / case.N
         assert np.abs(S - S64).max() <= 1e-3
+
+
+@pytest.mark.parametrize("perm,inner,fine", [(0.0, 1.0, -1), (0.05, 0.7, -1), (0.05, 0.7, 0), (0.02, 1.0, 4)])
+def test_cylinder_precision_form_equals_fp64_oracle(engine, tmp_path, perm, inner, fine):
+    """Cylinder jobs in the precision form walk the dSim2 step in FP64: on the
+    kernel's own Philox draws, positions and magnitudes equal the FP64 oracle
+    (oracle/oracle_dsim2.c, or2_integrate_f64_multi) bit for bit, regions and
+    nearest fibers exactly, with the fine filter grid at its default size,
+    off, and k = 4; signals within 1e-9."""
+    from dsim_gb300.engine import Batch, Cylinders, grad_scaled, pgse_table, phase_constant, rng_draws
+    from scenarios import CylCase
+    case = CylCase(tmp_path, permeability=perm, inner=inner, N=1500)
+    fp, maxR = O.load_fibers2(case.path, case.spaceScale)
+    cc, cubes, n, maxfpc, L = O.build_grid2(fp, maxR)
+    near = np.zeros(case.N, np.uint32)
+    imo = np.zeros(case.N, np.uint32)
+    pos4 = np.zeros((case.N, 4), F)
+    pos4[:, :3] = case.pos.reshape(-1, 3)
+    O.lib().or2_find_nearest(case.N, pos4.reshape(-1), fp, n, L, maxfpc, cc, cubes, float(inner), near, imo)
+    c = Cylinders.load(case.path, case.spaceScale)
+    if fine >= 0:
+        c.set_fine(fine)
+    steps, dt, seed = 300, case.dt, 4242
+    ss = F(case.spaceScale)
+    adc = (F(2.0) / (ss * ss), F(0.2) / (ss * ss), F(2.0) / (ss * ss))       # intra, myelin, extra
+    sd = [float(np.sqrt(F(2) * a * F(dt))) for a in adc] + [0.0]
+    T2 = [70.0, 8.0, 80.0, 0.0]
+    pc = phase_constant(42576.0, dt)
+    table = pgse_table(steps, float(dt), 0.3 * steps * float(dt), 0.6 * steps * float(dt))
+    gs = grad_scaled(np.array([[80.0, 0, 0], [0, 60.0, 30.0], [0, 0, 80.0]]), case.spaceScale).astype(F)
+    b = Batch(2 * 1536, 2)
+    sid = b.add_cyl(c)
+    kw = dict(steps=steps, dt=dt, step_sd=sd, T2=T2, phase_constant=pc, seed=seed, permeability=perm,
+              waveform="table", table=table, inner_radius_proportion=inner)
+    j64 = b.submit(sid, case.pos, imo.astype(np.uint8), near, precise=True, **kw)
+    j32 = b.submit(sid, case.pos, imo.astype(np.uint8), near, **kw)
+    b.run()
+    assert b.status() == 0
+    gpos, gmag = b.get_precise(j64, case.N)
+    _, _, gmom, gimo, gnear = b.get(j64, case.N)
+    sums = b.signal(j64, gs)
+    cnt = b.counts(j64)
+    # the FP64 oracle on the same draws
+    d = np.stack([rng_draws(seed, 0, t, case.N) for t in range(steps)])
+    P = O.Params2()
+    P.intraAdcScaled, P.myelinAdcScaled, P.extraAdcScaled = adc
+    P.T2fiber, P.T2myelin, P.T2outside = 70.0, 8.0, 80.0
+    P.permeability, P.innerRadiusProportion, P.spinRadius, P.deltaTime = perm, inner, 0.005, float(dt)
+    P.numCubes, P.maxFibersPerCube, P.cubeLength = n, maxfpc, L
+    rpos = case.pos.astype(np.float64).copy()
+    rmag = np.ones(case.N)
+    rimo, rnear = imo.copy(), near.copy()
+    rph = O.integrate2_f64_multi(P, rpos, rmag, rimo, rnear, fp, cc, cubes, gs.astype(np.float64),
+                                 table.astype(np.float64), float(pc), d, nthreads=4)
+    assert np.array_equal(gpos.reshape(-1).view(np.uint64), rpos.view(np.uint64))
+    assert np.array_equal(gmag.view(np.uint64), rmag.view(np.uint64))
+    assert np.array_equal(gimo, rimo.astype(np.uint8))
+    inside = rimo < 2
+    assert np.array_equal(gnear[inside], rnear[inside])
+    if perm > 0 or inner < 1.0:
+        assert cnt[0] > 0
+    z = rmag[:, None] * np.exp(1j * rph)
+    S_ref = np.abs(z.sum(0)) / case.N
+    S = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
+    assert np.allclose(S, S_ref, rtol=0, atol=1e-9), (S, S_ref)
+    # the plain FP32 job in the same batch still equals a batch of its own
+    b2 = Batch(1536, 1)
+    j2 = b2.submit(b2.add_cyl(c), case.pos, imo.astype(np.uint8), near, **kw)
+    b2.run()
+    for a1, a2 in zip(b.get(j32, case.N), b2.get(j2, case.N)):
+        assert np.array_equal(np.asarray(a1).view(np.uint8), np.asarray(a2).view(np.uint8))
+    b.close()
+    b2.close()
