@@ -1237,7 +1237,7 @@ def main():
     ap.add_argument("--axons", type=int, default=400)
     ap.add_argument("--spins", type=int, default=1 << 20)
     ap.add_argument("--steps-per-launch", type=int, default=1000)
-    ap.add_argument("--accel", type=int, default=-1, help="fine grid cells per axis (-1 default, 0 reference grid)")
+    ap.add_argument("--accel", type=int, default=-1, help="fine grid cells per axis (-1: the default, 2.25 per reference cell)")
     ap.add_argument("--sort-every", type=int, default=-1, help="steps between spin reorderings (-1 default)")
     ap.add_argument("--kernel", type=int, default=0, help="step kernel variant (0 default)")
     ap.add_argument("--records", type=int, default=0, help="fine-grid record bytes (0 default)")

@@ -21,12 +21,12 @@ LIB = os.path.join(HERE, "lib")
 OBJ = os.path.join(LIB, "obj")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-EXACT = {"mesh.cu", "cyl.cu", "accel.cu", "coop.cu", "flat.cu", "batch.cu", "compartments.cu"}
+EXACT = {"mesh.cu", "cyl.cu", "accel.cu", "flat.cu", "batch.cu", "compartments.cu"}
 
-UNITS = ["mesh.cu", "accel.cu", "coop.cu", "flat.cu", "cyl.cu", "scan.cu", "reduce.cu", "api.cu", "compat3.cu", "compat2.cu",
+UNITS = ["mesh.cu", "accel.cu", "flat.cu", "cyl.cu", "scan.cu", "reduce.cu", "api.cu", "compat3.cu", "compat2.cu",
          "host_formats.cpp", "noalloc.cu", "batch.cu", "serve.cpp", "compartments.cu", "simulate.cpp"]
 LIBS = {
-    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "coop", "flat", "cyl", "scan", "reduce", "noalloc", "batch", "serve", "compartments", "simulate"],
+    "libdsim_gb300.so": ["api", "host_formats", "mesh", "accel", "flat", "cyl", "scan", "reduce", "noalloc", "batch", "serve", "compartments", "simulate"],
     "libdsim3.so": ["compat3", "mesh", "accel", "flat", "scan"],
     "libdsim2.so": ["compat2", "cyl", "scan"],
 }

@@ -1,23 +1,12 @@
-// accel.cu -- the fast mesh path: a fine acceleration grid, spin sorting by
-// cell, and the step kernel that uses them while keeping the reference's
-// collision semantics bit for bit.
+// accel.cu -- the fine acceleration grid of a mesh, spin sorting by fine
+// cell, and the reference-layout transposes of the dSim3 drop-in.
 //
-// Semantics (rfdougherty/dSim dSim3/src/spinKernelCpu.cpp:198-395): for one
-// sub-segment the reference visits the cells of its 50^3 grid in the box
-// between the start and end cells (x outer, z inner) and stops at the first
-// cell whose triangle list holds a hit; the result is the nearest hit in that
-// list (lowest index on ties, the last-hit triangle excluded).
-//
-// Here every triangle the sub-segment hits is first collected from a finer
-// grid whose lists hold each triangle in every fine cell it touches (a
-// separating-axis test against the cell widened by kAccelEps): a triangle
-// that the float test reports as hit lies within rounding of the segment, so
-// it is always found.  With no
-// hit (the common case) the step is done.  Otherwise the reference's
-// traversal is replayed over the found hits only: a hit counts for a
-// reference cell when the triangle is in that cell's (sorted) list, found by
-// binary search.  The hit tests use the same float expressions as the
-// reference grid path in mesh.cu, so results are identical.
+// Fine grid: every triangle is listed in every fine cell it touches (a
+// separating-axis test in double against the cell widened by kAccelEps), so a
+// triangle that the reference's float test reports as hit by a sub-segment is
+// always in the lists of the fine cells of the sub-segment's box.  The step
+// kernels (flat.cu, batch.cu) collect their hits from these lists and replay
+// the reference's grid traversal over them (dSim3/src/spinKernelCpu.cpp:198-395).
 //
 // Spins are reordered by the Morton code of their fine cell every few steps
 // so that the threads of a warp read the same cell records (broadcast loads)
@@ -190,170 +179,6 @@ int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, u
     if (rc) return rc;
     DSIM_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)nkeys * 4, st));
     k_sort_scatter<<<(S.N + 255) / 256, 256, 0, st>>>(S, D, keys, start, hist);
-    DSIM_CUDA_TRY(cudaGetLastError());
-    return kOk;
-}
-
-template <bool STATS>
-__global__ void __launch_bounds__(128) k_mesh_step_fast(MeshDev g, AccelDev acc, MeshStepArgs a,
-                                                         SpinsSorted S, int rng) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= S.N) return;
-    float x = S.x[i], y = S.y[i], z = S.z[i], mag = S.mag[i], phase = S.phase[i];
-    uint32_t meta = S.meta[i];
-    uint32_t comp = meta & 0xFFu, fiber = meta >> 8;
-    const uint32_t id = S.id[i];
-    uint32_t nrefl = 0, nperm = 0, ntested = 0, status = 0;
-    uint32_t k0 = a.key0, k1 = a.key1;
-    if (rng == kRngPhiloxPerSpinKey) { k0 = a.spinKeys[2 * id]; k1 = a.spinKeys[2 * id + 1]; }
-    const float invLf = acc.invLf;
-    const uint32_t nf = acc.nf;
-    for (uint32_t it = 0; it < a.iterations; it++) {
-        Draw d;
-        if (rng == kRngReplay) {
-            float4 q = __ldg(a.draws + (size_t)it * S.N + id);
-            d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
-        } else {
-            d = philox_draw(a.spinBase + id, a.step0 + it, a.stream, k0, k1);
-        }
-        float ox = x, oy = y, oz = z;
-        float sd = a.sd[comp & 3u];
-        float px = x + d.nx * sd, py = y + d.ny * sd, pz = z + d.nz * sd;
-        float ex = px, ey = py, ez = pz;
-        uint32_t excluded = 0xFFFFFFFFu;
-        float umax = 1.0f, umin = 0.0f;
-        if (STATS) {
-            // reference-grid entries in the step segment's cell box
-            uint32_t sx = ref_coord(ox, g.L, g.n), sy = ref_coord(oy, g.L, g.n), sz = ref_coord(oz, g.L, g.n);
-            uint32_t tx = ref_coord(px, g.L, g.n), ty = ref_coord(py, g.L, g.n), tz = ref_coord(pz, g.L, g.n);
-            for (uint32_t cx = min(sx, tx); cx <= max(sx, tx); cx++)
-                for (uint32_t cy = min(sy, ty); cy <= max(sy, ty); cy++)
-                    for (uint32_t cz = min(sz, tz); cz <= max(sz, tz); cz++) {
-                        uint32_t c = g.n * g.n * cz + g.n * cy + cx;
-                        ntested += __ldg(g.cell_start + c + 1) - __ldg(g.cell_start + c);
-                    }
-        }
-        for (uint32_t sub = 0;; sub++) {
-            if (sub >= a.maxSub) { status |= kStatusSubsegCap; ex = ox; ey = oy; ez = oz; break; }
-            float dx = px - ox, dy = py - oy, dz = pz - oz;
-            // 1. every hit triangle, from the fine grid
-            uint32_t lo0 = fine_coord(fminf(ox, px) - kAccelEps, invLf, nf);
-            uint32_t lo1 = fine_coord(fminf(oy, py) - kAccelEps, invLf, nf);
-            uint32_t lo2 = fine_coord(fminf(oz, pz) - kAccelEps, invLf, nf);
-            uint32_t hi0 = fine_coord(fmaxf(ox, px) + kAccelEps, invLf, nf);
-            uint32_t hi1 = fine_coord(fmaxf(oy, py) + kAccelEps, invLf, nf);
-            uint32_t hi2 = fine_coord(fmaxf(oz, pz) + kAccelEps, invLf, nf);
-            FastHit hits[kMaxHits];
-            int nh = 0;
-            bool overflow = false;
-            for (uint32_t cx = lo0; cx <= hi0; cx++)
-                for (uint32_t cy = lo1; cy <= hi1; cy++)
-                    for (uint32_t cz = lo2; cz <= hi2; cz++) {
-                        uint32_t key = morton3(cx, cy, cz);
-                        uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
-                        for (uint32_t k = b0; k < b1; k++) {
-                            FastHit h;
-                            if (!test_entry(g, acc, k, excluded, ox, oy, oz, dx, dy, dz, h)) continue;
-                            bool dup = false;
-                            for (int q = 0; q < nh; q++) dup |= (hits[q].t == h.t);
-                            if (dup) continue;
-                            if (nh < kMaxHits) hits[nh++] = h; else overflow = true;
-                        }
-                    }
-            if (nh == 0) break;
-            // 2. the reference's traversal over the hits
-            FastHit best;
-            bool found = false;
-            if (overflow) {
-                ref_scan(g, ox, oy, oz, px, py, pz, excluded, best, found);
-            } else {
-                const uint32_t n = g.n;
-                const float L = g.L;
-                uint32_t sx = ref_coord(ox, L, n), sy = ref_coord(oy, L, n), sz = ref_coord(oz, L, n);
-                uint32_t tx = ref_coord(px, L, n), ty = ref_coord(py, L, n), tz = ref_coord(pz, L, n);
-                uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
-                uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
-                uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
-                uint32_t cx = sx;
-                do {
-                    uint32_t cy = sy;
-                    do {
-                        uint32_t cz = sz;
-                        do {
-                            uint32_t c = n * n * cz + n * cy + cx;
-                            for (int q = 0; q < nh; q++) {
-                                if (!in_ref_cell(g, c, hits[q].t)) continue;
-                                if (!found || hits[q].d2 < best.d2 ||
-                                    (hits[q].d2 == best.d2 && hits[q].t < best.t)) {
-                                    best = hits[q];
-                                    found = true;
-                                }
-                            }
-                            cz += iz;
-                        } while ((cz != tz + iz) && !found);
-                        cy += iy;
-                    } while ((cy != ty + iy) && !found);
-                    cx += ix;
-                } while ((cx != tx + ix) && !found);
-            }
-            if (!found) break;
-            float thr = umax - (umax - umin) * a.perm;
-            if (d.u <= thr) {
-                if ((a.reflType == 0) | (best.type > 1)) {
-                    ex = ox; ey = oy; ez = oz;
-                } else {
-                    const float4 nn = __ldg(reinterpret_cast<const float4*>(g.plane + best.t));
-                    float nx = nn.x, ny = nn.y, nz = nn.z;
-                    float sx2 = px - best.x, sy2 = py - best.y, sz2 = pz - best.z;
-                    ex = (1.0f - 2.0f * nx * nx) * sx2 - 2.0f * nx * ny * sy2 - 2.0f * nx * nz * sz2 + best.x;
-                    ey = -2.0f * nx * ny * sx2 + (1.0f - 2.0f * ny * ny) * sy2 - 2.0f * ny * nz * sz2 + best.y;
-                    ez = -2.0f * nx * nz * sx2 - 2.0f * ny * nz * sy2 + (1.0f - 2.0f * nz * nz) * sz2 + best.z;
-                }
-                umax = thr;
-                nrefl++;
-            } else {
-                umin = thr;
-                nperm++;
-                uint32_t info = __ldg(&g.plane[best.t].info);
-                uint32_t membrane = info & 3u;
-                if (comp == 2) {
-                    if (membrane == 0) comp = 1;
-                    else { comp = 0; fiber = 0xFFFFu; }
-                } else if (comp == 1) {
-                    comp = 2;
-                } else if (comp == 3) {
-                    comp = 0; fiber = 0xFFFFu;
-                } else {
-                    fiber = (info >> 2) & 0xFFFFu;
-                    comp = (membrane == 1) ? 2u : 3u;
-                }
-            }
-            ox = best.x; oy = best.y; oz = best.z;
-            px = ex; py = ey; pz = ez;
-            excluded = best.t;
-        }
-        if (ex > a.clampHi) ex = a.clampHi; else if (ex < a.clampLo) ex = a.clampLo;
-        if (ey > a.clampHi) ey = a.clampHi; else if (ey < a.clampLo) ey = a.clampLo;
-        if (ez > a.clampHi) ez = a.clampHi; else if (ez < a.clampLo) ez = a.clampLo;
-        x = ex; y = ey; z = ez;
-        mag += -mag / a.T2[comp & 3u] * a.dt;
-        float gx = a.gx, gy = a.gy, gz = a.gz;
-        if (a.grad) { float4 G = __ldg(a.grad + it); gx = G.x; gy = G.y; gz = G.z; }
-        phase += (gx * x + gy * y + gz * z) * a.pc;
-    }
-    S.x[i] = x; S.y[i] = y; S.z[i] = z; S.mag[i] = mag; S.phase[i] = phase;
-    S.meta[i] = (comp & 0xFFu) | (fiber << 8);
-    if (a.counts) { a.counts[2 * id] += nrefl; a.counts[2 * id + 1] += nperm; }
-    if (STATS && a.tested) a.tested[id] += ntested;
-    if (status) atomicOr(a.status, status);
-}
-
-int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st) {
-    if (S.N == 0 || a.iterations == 0) return kOk;
-    dim3 block(128), grid((S.N + 127) / 128);
-    if (a.tested) k_mesh_step_fast<true><<<grid, block, 0, st>>>(g, acc, a, S, rng);
-    else k_mesh_step_fast<false><<<grid, block, 0, st>>>(g, acc, a, S, rng);
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

@@ -70,7 +70,7 @@ struct dsim_mesh {
     uint4* tri_cells = nullptr;  // each triangle's reference cells (up to 4)
     // fine acceleration grid (nf = 0: none; steps scan the reference grid)
     uint32_t nf = 0;
-    uint32_t kernel = 8;  // 1 per-thread lists, 2/3/4 warp-cooperative (4, 6, 8 blocks per SM), 5/6/7 warp-flattened
+    uint32_t kernel = 8;  // 5/6/7 warp-flattened (8, 6, 4 blocks per SM), 8 with the plane-survivor queue, 9 TMA staging
                           // (8, 6, 4), 8 flattened with queued plane survivors, 9 with staged records
     uint64_t accEntries = 0, accBytes = 0;
     uint32_t* acc_start = nullptr;
@@ -937,13 +937,10 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
     if (rc) return rc;
     int rng = replayDraws ? kRngReplay : kRngPhilox;
     if (m->nf == 0) {
-        // reference-grid scan: slot order = spin order
-        if ((rc = spins_unpermute(s))) return rc;
-        if (a.tested) { set_last_error(kErrInvalid, "entry counting needs the fine grid"); return kErrInvalid; }
-        s->launches += 1;
-        return launch_mesh_step(m->dev(), a, s->dev(), kLayoutSoA, rng, s->st);
+        set_last_error(kErrInvalid, "dsim_mesh_run: the mesh has no fine grid (dsim_mesh_set_accel failed)");
+        return kErrInvalid;
     }
-    // fast path: reorder by fine cell every sortEvery steps
+    // reorder by fine cell every sortEvery steps
     uint32_t chunk = s->sortEvery ? s->sortEvery : iterations;
     if (s->sortEvery && (rc = ensure_sort_buffers(s, m->nf))) return rc;
     const float4* grad0 = a.grad;
@@ -963,13 +960,8 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
         b.step0 = a.step0 + done;
         b.grad = grad0 ? grad0 + done : nullptr;
         b.draws = draws0 ? draws0 + (size_t)done * s->N : nullptr;
-        if (m->kernel == 1) rc = launch_mesh_step_fast(m->dev(), m->acc(), b, s->sorted(), rng, s->st);
-        else if (m->kernel >= 5)
-            rc = launch_mesh_step_flat(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
-                                       m->kernel == 5 ? 8 : (m->kernel == 7 ? 4 : 6), m->kernel == 8, m->kernel == 9);
-        else
-            rc = launch_mesh_step_coop(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
-                                       m->kernel == 2 ? 4 : (m->kernel == 3 ? 6 : 8));
+        rc = launch_mesh_step_flat(m->dev(), m->acc(), b, s->sorted(), rng, s->st,
+                                   m->kernel == 5 ? 8 : (m->kernel == 7 ? 4 : 6), m->kernel == 8, m->kernel == 9);
         if (rc) return rc;
         s->launches += 1;
     }
@@ -977,13 +969,17 @@ int dsim_mesh_run(dsim_mesh* m, dsim_spins* s, const dsim_mesh_params* p, const 
 }
 
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant) {
-    if (!m || variant < 1 || variant > 9) { set_last_error(kErrInvalid, "kernel variant must be 1..9"); return kErrInvalid; }
+    if (!m || variant < 5 || variant > 9) { set_last_error(kErrInvalid, "kernel variant must be 5..9"); return kErrInvalid; }
     m->kernel = variant;
     return kOk;
 }
 
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis) {
     if (!m) return kErrInvalid;
+    if (cellsPerAxis == 0) {
+        set_last_error(kErrInvalid, "dsim_mesh_set_accel: every step kernel needs a fine grid (cells per axis >= 1)");
+        return kErrInvalid;
+    }
     return accel_build(m, cellsPerAxis);
 }
 

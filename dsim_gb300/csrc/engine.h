@@ -111,15 +111,10 @@ int launch_accel_cells(bool fill, uint32_t nT, const TriPlane* plane, const TriB
                        uint32_t* tri, AccelRecWide* recw, cudaStream_t st, AccelRecFull* recf = nullptr);
 int launch_sort_spins(const SpinsSorted& S, const SpinsSorted& D, uint32_t nb, uint32_t* keys,
                       uint32_t* hist, uint32_t* start, uint32_t* scratch, cudaStream_t st);
-int launch_mesh_step_fast(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st);
 int launch_unpermute(const SpinsSorted& S, const SpinsSorted& D, cudaStream_t st);
-// coop.cu: warp-cooperative variant of the fast step (same results)
-// occupancy: minimum resident blocks of 128 threads per SM the kernel is
-// compiled for (4, 6 or 8: register budget 128, 85 or 64)
-int launch_mesh_step_coop(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
-                          const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 6);
-// flat.cu: warp-flattened candidate lists (same results); occupancy 6 or 8
+// flat.cu: the mesh step (warp-flattened candidate lists); occupancy 4, 6 or
+// 8 blocks per SM; queue: plane-test survivors finished 32 at a time; stage:
+// each cell's records staged in shared memory by bulk (TMA) copies
 int launch_mesh_step_flat(const MeshDev& g, const AccelDev& acc, const MeshStepArgs& a,
                           const SpinsSorted& S, int rng, cudaStream_t st, int occupancy = 8,
                           bool queue = false, bool stage = false);
@@ -147,8 +142,6 @@ int launch_sort_cells(uint32_t ncells, const uint32_t* start, uint32_t* cell_tri
 int launch_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT, const uint32_t* counter,
                         const uint32_t* dense, const uint32_t* start, uint32_t* cell_tri,
                         uint32_t* status, cudaStream_t st);
-int launch_mesh_step(const MeshDev& g, const MeshStepArgs& a, const SpinsDev& S, int layout,
-                     int rng, cudaStream_t st);
 
 // ---- compartments.cu ------------------------------------------------------
 int launch_compartments(const MeshDev& g, const AccelDev& acc, const SpinsSorted& S, const float maxabs[3],

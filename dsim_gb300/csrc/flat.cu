@@ -1,14 +1,16 @@
-// flat.cu -- mesh step with warp-flattened candidate lists (kernel variants 5-7).
+// flat.cu -- the mesh step with warp-flattened candidate lists (kernel
+// variants 5-9; 8 is the default).
 //
 // Same semantics as the reference's collision loop
-// (rfdougherty/dSim dSim3/src/spinKernelCpu.cpp:198-499) and as the other
-// step kernels; what changes is how a warp walks its candidates.  The
-// cooperative kernel (coop.cu) takes the (segment, fine cell) items of its 32
-// lanes one at a time, so every item pays two dependent global loads (the
-// cell's record range, then its records) in series.  Here a collision round
-// works in two flat passes over the whole warp:
+// (rfdougherty/dSim dSim3/src/spinKernelCpu.cpp:198-499): for one sub-segment
+// the first cell of the reference grid (in its x-outer, z-inner traversal of
+// the box between the start and end cells) whose list holds a hit gives the
+// nearest hit in that list, lowest index on ties, the last-hit triangle
+// excluded.  Candidates come from a finer grid whose lists hold each triangle
+// in every fine cell it touches; a collision round works in two flat passes
+// over the whole warp:
 //
-//   1. items: the lanes' cell boxes are concatenated by a warp prefix sum;
+//   1. items: the lanes' fine-cell boxes are concatenated by a warp prefix sum;
 //      32 items at a time, lane m finds its item's owner (binary search over
 //      the prefix by shuffle) and loads that cell's record range, so 32 range
 //      loads are in flight at once;
@@ -16,11 +18,12 @@
 //      records; lane j tests flat record j, j + 32, ... against the owner's
 //      sub-segment, read from a per-warp segment table in shared memory.
 //
-// Hits are filed in the owner's slots and resolved by the owner exactly as in
-// coop.cu (first reference cell with a hit, nearest, lowest index on ties).
-// Lanes do not advance through the steps in lockstep: a lane whose step ends
-// starts its next step in the next round, so one lane's chain of reflections
-// does not idle the other 31.
+// Hits are filed in the owner's slots and resolved by the owner: the first
+// reference cell (in the reference's order) whose list holds one of its hits,
+// the nearest there, the lowest index on ties; the exact reference-grid scan
+// when the slots overflowed.  Lanes do not advance through the steps in
+// lockstep: a lane whose step ends starts its next step in the next round, so
+// one lane's chain of reflections does not idle the other 31.
 #include "common.cuh"
 #include "engine.h"
 #include "mesh_common.cuh"

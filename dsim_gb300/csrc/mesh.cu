@@ -1,18 +1,13 @@
 // mesh.cu -- triangle-mesh substrate on the GPU: exact grid build, per-triangle
-// records, and the random-walk step with collision, reflection and permeation.
+// records (the step kernels are in flat.cu and batch.cu).
 //
 // Reference (rfdougherty/dSim):
-//   step             dSim3/src/spinKernelCpu.cpp:430-499 (cpuIntegrate)
-//   collision loop   dSim3/src/spinKernelCpu.cpp:198-301 (collDetectRectGrid)
-//   cell scan        dSim3/src/spinKernelCpu.cpp:311-337 (cubeCollDetect)
-//   triangle test    dSim3/src/spinKernelCpu.cpp:354-395 (triCollDetect)
-//   reflection       dSim3/src/spinKernelCpu.cpp:406-422 (reflectPos)
 //   cell of a point  dSim3/src/spinSystem.cpp:691-759 (calcCubePos/Hash)
 //   grid membership  dSim3/src/spinSystem.cpp:1094-1379 (populateCubes,
 //                    pointInCube, rayTriangleIntersect)
 //   triangle helpers dSim3/src/spinSystem.cpp:612-648
 // Compiled with -fmad=false: every float expression keeps the reference's
-// evaluation order and rounding, so replayed trajectories are bit-identical.
+// evaluation order and rounding, so the grid and records equal the reference's.
 #include "common.cuh"
 #include "engine.h"
 
@@ -240,226 +235,6 @@ __global__ void k_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT,
 }
 
 // ------------------------------------------------------------------------
-// The step
-// ------------------------------------------------------------------------
-struct Hit {
-    uint32_t type, idx;
-    float x, y, z, d2;
-};
-
-// cubeCollDetect + triCollDetect over one cell's list: nearest hit
-__device__ __forceinline__ void scan_cell(const MeshDev& g, uint32_t cell, float ox, float oy,
-                                          float oz, float dx, float dy, float dz,
-                                          uint32_t excluded, Hit& best, uint32_t& ntested) {
-    uint32_t b = __ldg(g.cell_start + cell), e = __ldg(g.cell_start + cell + 1);
-    ntested += e - b;
-    for (uint32_t k = b; k < e; k++) {
-        uint32_t t = __ldg(g.cell_tri + k);
-        if (t == excluded) continue;
-        const float4* pp = reinterpret_cast<const float4*>(g.plane + t);
-        float4 a = __ldg(pp), c = __ldg(pp + 1);
-        float num = a.x * (a.w - ox) + a.y * (c.x - oy) + a.z * (c.y - oz);
-        float den = a.x * dx + a.y * dy + a.z * dz;
-        // conservative test for 0 < num/den < 1 before the IEEE division
-        if (!(fabsf(num) <= fabsf(den)) || num == 0.0f ||
-            ((__float_as_uint(num) ^ __float_as_uint(den)) & 0x80000000u))
-            continue;
-        float r = num / den;
-        if (!((0.0f < r) & (r < 1.0f))) continue;
-        const float4* bb = reinterpret_cast<const float4*>(g.bary + t);
-        float4 u4 = __ldg(bb), v4 = __ldg(bb + 1);
-        float wx = ox + r * dx - a.w;
-        float wy = oy + r * dy - c.x;
-        float wz = oz + r * dz - c.y;
-        float wu = wx * u4.x + wy * u4.y + wz * u4.z;
-        float wv = wx * u4.w + wy * v4.x + wz * v4.y;
-        float uv = v4.z, uu = v4.w, vv = c.z;
-        float s = (uv * wv - vv * wu) / (uv * uv - uu * vv);
-        float tt = (uv * wu - uu * wv) / (uv * uv - uu * vv);
-        if ((s >= 0.0f) & (tt >= 0.0f) & (s + tt <= 1.0f)) {
-            float cx = ox + dx * r, cy = oy + dy * r, cz = oz + dz * r;
-            float d2 = (ox - cx) * (ox - cx) + (oy - cy) * (oy - cy) + (oz - cz) * (oz - cz);
-            if (d2 < best.d2) {
-                uint32_t type = 1;
-                if ((s == 0.0f) | (tt == 0.0f) | (s + tt == 1.0f)) {
-                    type = 2;
-                    if (((s == 0.0f) & (tt == 0.0f)) | ((s == 0.0f) & (tt == 1.0f)) |
-                        ((s == 1.0f) & (tt == 0.0f)))
-                        type = 3;
-                }
-                best.type = type; best.idx = t; best.x = cx; best.y = cy; best.z = cz; best.d2 = d2;
-            }
-        }
-    }
-}
-
-struct SpinRegs {
-    float x, y, z, mag, phase;
-    uint32_t comp, fiber;
-};
-
-// one step of one spin (cpuIntegrate); returns status bits
-__device__ __forceinline__ uint32_t mesh_step_one(const MeshDev& g, const MeshStepArgs& a,
-                                                  SpinRegs& s, Draw d, float gx, float gy, float gz,
-                                                  uint32_t& nrefl, uint32_t& nperm,
-                                                  uint32_t& ntested) {
-    uint32_t status = 0;
-    float ox = s.x, oy = s.y, oz = s.z;
-    float sd = a.sd[s.comp & 3u];
-    float px = s.x + d.nx * sd, py = s.y + d.ny * sd, pz = s.z + d.nz * sd;
-    // collDetectRectGrid
-    float ex = px, ey = py, ez = pz;
-    uint32_t excluded = 0xFFFFFFFFu;
-    float umax = 1.0f, umin = 0.0f;
-    const float perm = a.perm;
-    const uint32_t n = g.n;
-    const float L = g.L;
-    for (uint32_t sub = 0;; sub++) {
-        if (sub >= a.maxSub) { status |= kStatusSubsegCap; ex = ox; ey = oy; ez = oz; break; }
-        uint32_t sx = cube_coord(ox, L, n), sy = cube_coord(oy, L, n), sz = cube_coord(oz, L, n);
-        uint32_t tx = cube_coord(px, L, n), ty = cube_coord(py, L, n), tz = cube_coord(pz, L, n);
-        uint32_t ix = (uint32_t)((int)(tx > sx) - (int)(tx < sx));
-        uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
-        uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
-        float dx = px - ox, dy = py - oy, dz = pz - oz;
-        Hit best;
-        best.type = 0; best.idx = 0xFFFFFFFFu; best.d2 = 400000000.0f;
-        best.x = best.y = best.z = 0.0f;
-        uint32_t cx = sx;
-        do {
-            uint32_t cy = sy;
-            do {
-                uint32_t cz = sz;
-                do {
-                    best.type = 0; best.idx = 0xFFFFFFFFu; best.d2 = 400000000.0f;
-                    scan_cell(g, n * n * cz + n * cy + cx, ox, oy, oz, dx, dy, dz, excluded, best, ntested);
-                    cz += iz;
-                } while ((cz != tz + iz) && (best.type == 0));
-                cy += iy;
-            } while ((cy != ty + iy) && (best.type == 0));
-            cx += ix;
-        } while ((cx != tx + ix) && (best.type == 0));
-        if (best.type == 0) break;
-        float thr = umax - (umax - umin) * perm;
-        if (d.u <= thr) {
-            // reflectPos
-            if ((a.reflType == 0) | (best.type > 1)) {
-                ex = ox; ey = oy; ez = oz;
-            } else {
-                const float4 nn = __ldg(reinterpret_cast<const float4*>(g.plane + best.idx));
-                float nx = nn.x, ny = nn.y, nz = nn.z;
-                float sx2 = px - best.x, sy2 = py - best.y, sz2 = pz - best.z;
-                ex = (1.0f - 2.0f * nx * nx) * sx2 - 2.0f * nx * ny * sy2 - 2.0f * nx * nz * sz2 + best.x;
-                ey = -2.0f * nx * ny * sx2 + (1.0f - 2.0f * ny * ny) * sy2 - 2.0f * ny * nz * sz2 + best.y;
-                ez = -2.0f * nx * nz * sx2 - 2.0f * ny * nz * sy2 + (1.0f - 2.0f * nz * nz) * sz2 + best.z;
-            }
-            umax = thr;
-            nrefl++;
-        } else {
-            umin = thr;
-            nperm++;
-            uint32_t info = __ldg(&g.plane[best.idx].info);
-            uint32_t membrane = info & 3u;
-            // compartment transition table, spinKernelCpu.cpp:251-270
-            if (s.comp == 2) {
-                if (membrane == 0) s.comp = 1;
-                else { s.comp = 0; s.fiber = 0xFFFFu; }
-            } else if (s.comp == 1) {
-                s.comp = 2;
-            } else if (s.comp == 3) {
-                s.comp = 0; s.fiber = 0xFFFFu;
-            } else {
-                s.fiber = (info >> 2) & 0xFFFFu;
-                s.comp = (membrane == 1) ? 2u : 3u;
-            }
-        }
-        ox = best.x; oy = best.y; oz = best.z;
-        px = ex; py = ey; pz = ez;
-        excluded = best.idx;
-    }
-    // clamp to the box, spinKernelCpu.cpp:469-474
-    if (ex > a.clampHi) ex = a.clampHi; else if (ex < a.clampLo) ex = a.clampLo;
-    if (ey > a.clampHi) ey = a.clampHi; else if (ey < a.clampLo) ey = a.clampLo;
-    if (ez > a.clampHi) ez = a.clampHi; else if (ez < a.clampLo) ez = a.clampLo;
-    s.x = ex; s.y = ey; s.z = ez;
-    s.mag += -s.mag / a.T2[s.comp & 3u] * a.dt;
-    s.phase += (gx * ex + gy * ey + gz * ez) * a.pc;
-    return status;
-}
-
-// Layout of spin state in HBM: SoA (native) or the reference's AoS arrays
-// (float3 positions, 12-byte spinData records, uint2 seeds).
-template <int LAYOUT>
-struct SpinIO;
-
-template <>
-struct SpinIO<kLayoutSoA> {
-    static __device__ __forceinline__ void load(const SpinsDev& S, uint32_t i, SpinRegs& r) {
-        r.x = S.x[i]; r.y = S.y[i]; r.z = S.z[i];
-        r.mag = S.mag[i]; r.phase = S.phase[i];
-        uint32_t m = S.meta[i];
-        r.comp = m & 0xFFu; r.fiber = m >> 8;
-    }
-    static __device__ __forceinline__ void store(const SpinsDev& S, uint32_t i, const SpinRegs& r) {
-        S.x[i] = r.x; S.y[i] = r.y; S.z[i] = r.z;
-        S.mag[i] = r.mag; S.phase[i] = r.phase;
-        S.meta[i] = (r.comp & 0xFFu) | (r.fiber << 8);
-    }
-};
-
-template <>
-struct SpinIO<kLayoutAoS> {
-    static __device__ __forceinline__ void load(const SpinsDev& S, uint32_t i, SpinRegs& r) {
-        r.x = S.x[3 * i]; r.y = S.x[3 * i + 1]; r.z = S.x[3 * i + 2];
-        const unsigned char* rec = reinterpret_cast<const unsigned char*>(S.meta) + 12 * (size_t)i;
-        r.mag = *reinterpret_cast<const float*>(rec);
-        r.phase = *reinterpret_cast<const float*>(rec + 4);
-        r.comp = rec[8];
-        r.fiber = *reinterpret_cast<const uint16_t*>(rec + 10);
-    }
-    static __device__ __forceinline__ void store(const SpinsDev& S, uint32_t i, const SpinRegs& r) {
-        S.x[3 * i] = r.x; S.x[3 * i + 1] = r.y; S.x[3 * i + 2] = r.z;
-        unsigned char* rec = reinterpret_cast<unsigned char*>(S.meta) + 12 * (size_t)i;
-        *reinterpret_cast<float*>(rec) = r.mag;
-        *reinterpret_cast<float*>(rec + 4) = r.phase;
-        rec[8] = (unsigned char)r.comp;
-        *reinterpret_cast<uint16_t*>(rec + 10) = (uint16_t)r.fiber;
-    }
-};
-
-template <int LAYOUT, int RNG>
-__global__ void __launch_bounds__(256) k_mesh_step(MeshDev g, MeshStepArgs a, SpinsDev S) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= S.N) return;
-    SpinRegs r;
-    SpinIO<LAYOUT>::load(S, i, r);
-    uint32_t k0 = a.key0, k1 = a.key1;
-    if (RNG == kRngPhiloxPerSpinKey) { k0 = S.seed[2 * i]; k1 = S.seed[2 * i + 1]; }
-    uint32_t nrefl = 0, nperm = 0, ntested = 0, status = 0;
-    for (uint32_t it = 0; it < a.iterations; it++) {
-        Draw d;
-        if (RNG == kRngReplay) {
-            float4 q = __ldg(a.draws + (size_t)it * S.N + i);
-            d.nx = q.x; d.ny = q.y; d.nz = q.z; d.u = q.w;
-        } else {
-            d = philox_draw(a.spinBase + i, a.step0 + it, a.stream, k0, k1);
-        }
-        float gx = a.gx, gy = a.gy, gz = a.gz;
-        if (a.grad) { float4 G = __ldg(a.grad + it); gx = G.x; gy = G.y; gz = G.z; }
-        status |= mesh_step_one(g, a, r, d, gx, gy, gz, nrefl, nperm, ntested);
-    }
-    SpinIO<LAYOUT>::store(S, i, r);
-    if (RNG == kRngPhiloxPerSpinKey) {
-        // advance the per-spin key so the next call draws a fresh stream
-        u32x4 nk = philox4x32_10({i, a.iterations, 0xFFFFFFFFu, 0x5EEDu}, k0, k1);
-        S.seed[2 * i] = nk.x; S.seed[2 * i + 1] = nk.y;
-    }
-    if (a.counts) { a.counts[2 * i] += nrefl; a.counts[2 * i + 1] += nperm; }
-    if (a.tested) a.tested[i] += ntested;
-    if (status) atomicOr(a.status, status);
-}
-
-// ------------------------------------------------------------------------
 // Host launchers
 // ------------------------------------------------------------------------
 int launch_records_from_mesh(uint32_t nT, const float* V, const uint32_t* trgls,
@@ -537,25 +312,6 @@ int launch_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT, const uin
                         uint32_t* status, cudaStream_t st) {
     k_dense_to_csr<<<(ncells + 255) / 256, 256, 0, st>>>(ncells, maxTPC, nT, counter, dense, start,
                                                           cell_tri, status);
-    DSIM_CUDA_TRY(cudaGetLastError());
-    return kOk;
-}
-
-int launch_mesh_step(const MeshDev& g, const MeshStepArgs& a, const SpinsDev& S, int layout,
-                     int rng, cudaStream_t st) {
-    if (S.N == 0 || a.iterations == 0) return kOk;
-    dim3 block(128), grid((S.N + 127) / 128);
-#define DSIM_LAUNCH(L, R) k_mesh_step<L, R><<<grid, block, 0, st>>>(g, a, S)
-    if (layout == kLayoutSoA) {
-        if (rng == kRngReplay) DSIM_LAUNCH(kLayoutSoA, kRngReplay);
-        else if (rng == kRngPhilox) DSIM_LAUNCH(kLayoutSoA, kRngPhilox);
-        else DSIM_LAUNCH(kLayoutSoA, kRngPhiloxPerSpinKey);
-    } else {
-        if (rng == kRngReplay) DSIM_LAUNCH(kLayoutAoS, kRngReplay);
-        else if (rng == kRngPhilox) DSIM_LAUNCH(kLayoutAoS, kRngPhilox);
-        else DSIM_LAUNCH(kLayoutAoS, kRngPhiloxPerSpinKey);
-    }
-#undef DSIM_LAUNCH
     DSIM_CUDA_TRY(cudaGetLastError());
     return kOk;
 }

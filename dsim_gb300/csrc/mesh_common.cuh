@@ -1,7 +1,7 @@
-// mesh_common.cuh -- device helpers shared by the fast mesh step kernels
-// (accel.cu, coop.cu): fine-grid coordinates and Morton keys, the exact
-// triangle test on a fine-grid record, membership in a reference-grid cell,
-// and the reference grid scan used as the exact fallback.
+// mesh_common.cuh -- device helpers shared by the mesh step kernels (flat.cu,
+// batch.cu) and the compartment search: fine-grid coordinates and Morton
+// keys, the exact triangle test on a fine-grid record, membership in a
+// reference-grid cell, and the reference grid scan used as the exact fallback.
 #pragma once
 #include "common.cuh"
 #include "engine.h"

@@ -25,7 +25,7 @@ scratch copy in oracle/_ref/src{2,3}/:
 The host side of the C-ABI (allocateArray -> malloc, copy* -> memcpy) and the
 cutil timer macros are provided by oracle/refharness/.
 
-Usage: python3 oracle/build_ref.py [--reference /root/reference]
+Usage: python3 oracle/build_ref.py [--reference DIR]
 """
 import argparse
 import os
@@ -36,6 +36,15 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
+# where this recipe looks for the reference tree: DSIM_REFERENCE, else the
+# checkout that this build reads (absent on machines that only run the tests)
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_dir():
+    """The reference tree to build from, or None when it is not present."""
+    ref = os.environ.get("DSIM_REFERENCE", DEFAULT_REFERENCE)
+    return ref if os.path.isdir(ref) else None
 HARNESS = os.path.join(HERE, "refharness")
 
 DSIM3_FILES = ["spinSystem.cpp", "spinKernelCpu.cpp", "spinSystem.h", "spinSystem.cuh",
@@ -124,9 +133,11 @@ def build(reference):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None, help="the reference tree (default: DSIM_REFERENCE or %s)"
+                    % DEFAULT_REFERENCE)
     a = ap.parse_args()
-    if not os.path.isdir(a.reference):
+    a.reference = a.reference or reference_dir()
+    if not a.reference or not os.path.isdir(a.reference):
         print("reference tree not present; nothing to build")
         sys.exit(0)
     for p in build(a.reference):

@@ -34,10 +34,11 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
+import build_ref  # noqa: E402
 import oracle as O  # noqa: E402
 from dsim_gb300 import substrates as S  # noqa: E402
 
-REFERENCE = os.environ.get("DSIM_REFERENCE", "/root/reference")
+REFERENCE = build_ref.reference_dir()
 
 
 def run(exe, **kw):
@@ -126,8 +127,8 @@ def matlab_collision_case():
 
 
 def main():
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import build_ref
+    if REFERENCE is None:
+        raise SystemExit("the reference tree is not present (set DSIM_REFERENCE)")
     h3, h2 = build_ref.build(REFERENCE)
     with tempfile.TemporaryDirectory() as tmp:
         mesh_fixture("mesh_am", "AM", 0.05, 11, h3, tmp)

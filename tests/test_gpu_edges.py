@@ -98,7 +98,7 @@ def test_full_size_variants_agree(engine):
     m = bench.make_mesh(W)
     p = bench.mesh_params_of(W)
     outs = {}
-    for k in (6, 1, 4, 5, 7, 8, 9):
+    for k in (6, 5, 7, 8, 9):
         m.set_kernel(k)
         s = Spins(W.N)
         s.set(W.pos, np.ones(W.N, F), np.zeros(W.N, F), W.comp, W.fiber)

@@ -49,22 +49,23 @@ def test_grid_build_matches_reference_membership(engine, tmp_path, membranes):
 
 @pytest.mark.parametrize("membranes,perm,accel,sort,kernel,records", [
     ("AM", 0.05, None, 20, None, None), ("G", 0.0, None, 20, None, None),
-    ("G", 0.3, None, 7, None, None), ("AM", 0.05, 0, 0, None, None),
+    ("G", 0.3, None, 7, None, None), ("AM", 0.05, 13, 0, None, None),
     ("AM", 0.05, 37, 7, None, 16), ("AM", 0.05, 300, 0, None, None), ("G", 0.3, 13, 1, None, 16),
-    ("AM", 0.05, None, 20, 1, None), ("AM", 0.05, None, 20, 2, 16), ("AM", 0.05, 75, 20, 3, None),
+    ("AM", 0.05, None, 20, 7, None), ("AM", 0.05, None, 20, 6, 16), ("AM", 0.05, 75, 20, 7, None),
     ("AM", 0.05, None, 20, 5, None), ("G", 0.3, 37, 7, 6, 16), ("AM", 0.05, 300, 0, 5, None),
-    ("G", 0.0, 75, 20, 5, 16), ("G", 0.3, None, 7, 4, None), ("AM", 0.05, 100, 20, 7, None),
-    ("AM", 0.05, None, 20, None, 64), ("G", 0.3, 37, 7, 5, 64), ("AM", 0.05, 300, 0, 4, 64),
-    ("G", 0.3, 13, 1, 1, 64), ("AM", 0.05, None, 20, 8, None), ("G", 0.3, 37, 7, 8, None),
+    ("G", 0.0, 75, 20, 5, 16), ("G", 0.3, None, 7, 7, None), ("AM", 0.05, 100, 20, 7, None),
+    ("AM", 0.05, None, 20, None, 64), ("G", 0.3, 37, 7, 5, 64), ("AM", 0.05, 300, 0, 7, 64),
+    ("G", 0.3, 13, 1, 6, 64), ("AM", 0.05, None, 20, 8, None), ("G", 0.3, 37, 7, 8, None),
     ("G", 0.0, 300, 0, 8, None), ("AM", 0.05, None, 20, 9, None), ("G", 0.3, 37, 7, 9, None),
-    ("AM", 0.05, 300, 0, 9, None)])
+    ("AM", 0.05, 300, 0, 9, None), ("G", 0.3, 1, 0, 9, None)])
 def test_mesh_replay_bit_parity_native(engine, tmp_path, membranes, perm, accel, sort, kernel, records):
-    """accel None: default fine grid; 0: reference-grid scan; other: fine
-    cells per axis (coarser and finer than the reference grid).  sort: steps
-    between spin reorderings (0 = never).  kernel: step kernel variant;
-    records: fine-grid record bytes (kernel 8 queues the records that pass
-    the plane test, kernel 9 stages records in shared memory by asynchronous
-    copies; both on 32-byte records, kernel 6's path on the others)."""
+    """accel None: default fine grid; other: fine cells per axis (coarser and
+    finer than the reference grid; 1: one cell, every triangle in one list).
+    sort: steps between spin reorderings (0 = never).  kernel: step kernel
+    variant (5, 6, 7: 8, 6, 4 blocks per SM; 8: records past the plane test
+    queued and finished 32 at a time; 9: each cell's records staged in shared
+    memory by bulk copies; 8 and 9 on 32-byte records, kernel 6's path on the
+    others); records: fine-grid record bytes."""
     from dsim_gb300.engine import Mesh, Spins, mesh_params, mesh_run
     case = MeshCase(tmp_path, membranes=membranes, permeability=perm, N=1500)
     iters = 60
