@@ -28,6 +28,7 @@ enum StatusBits : uint32_t {
     kStatusBadCell = 2u,     // a cell index fell outside the grid (never expected)
     kStatusParityOverflow = 4u,  // compartment search: more than 32 membranes on one line
     kStatusUnresolved = 8u,      // compartment search: every line and position was ambiguous
+    kStatusStageTimeout = 16u,   // a bulk-copy wait ran out (the warp stopped; its spins are stale)
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

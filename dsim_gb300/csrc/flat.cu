@@ -33,8 +33,9 @@
 namespace dsim {
 
 // QUEUE (32-byte records): records past the plane test are finished 32 at a
-// time from a per-warp queue (flat_round_mode's Q); STAGE: records staged in
-// shared memory by double-buffered asynchronous copies (flat_round_mode's P)
+// time from a per-warp queue (flat_round_mode's Q); STAGE: each cell's records
+// staged in shared memory by bulk (TMA) copies, double-buffered
+// (flat_round_mode's P)
 template <bool STATS, int MINB, int LAYOUT, bool QUEUE = false, bool STAGE = false>
 __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g, AccelDev acc,
                                                                        MeshStepArgs a, SpinsSorted S,
@@ -45,6 +46,10 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     FlatWarp& H = wh[threadIdx.x >> 5];
+    if (STAGE) {
+        if (lane == 0) stage_init(&ws[threadIdx.x >> 5]);
+        __syncwarp();
+    }
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < S.N;
     float x = 0.0f, y = 0.0f, z = 0.0f, mag = 0.0f, phase = 0.0f;
@@ -130,6 +135,10 @@ __global__ void __launch_bounds__(kFlatThreads, MINB) k_mesh_step_flat(MeshDev g
                 }
             }
             __syncwarp();
+            if (STAGE && ws[threadIdx.x >> 5].abort) {  // warp-uniform: a staging wait ran out
+                if (valid) atomicOr(a.status, (uint32_t)kStatusStageTimeout);
+                return;
+            }
         }
     }
     if (!valid) return;

@@ -86,22 +86,65 @@ __device__ __forceinline__ bool test_wide_loaded(const MeshDev& g, float4 q, flo
     return test_split(g, q, pt, ox, oy, oz, dx, dy, dz, h);
 }
 
-// Double-buffered staging of 32-byte records in shared memory: while a warp
-// tests one 64-record window, each lane's two records of the next window are
-// already in flight by asynchronous copies (cp.async, 16 bytes each), so the
-// load latency of a window overlaps the tests of the previous one.  A lane
-// reads back only the copies it issued itself.
-struct FlatStage {
-    float4 rec[2][32][4];  // [buffer][lane][q0, pt0, q1, pt1]
+// Staging of 32-byte records in shared memory by bulk copies (the TMA engine,
+// cp.async.bulk): the records of a round's cells are taken in windows of 64;
+// for each window, every lane whose cell overlaps it issues one bulk copy of
+// its part (each cell's records are contiguous), completing on the warp's
+// mbarrier, whose expected byte count lane 0 posts first.  Two buffers: the
+// next window's copies are in flight while the current one is tested.  Waits
+// are bounded: past kStageSpinLimit polls the warp records kStatusStageTimeout
+// and stops stepping (its spins are not written back).
+static constexpr uint32_t kStageRecs = 64;
+static constexpr uint32_t kStageSpinLimit = 1u << 20;
+struct __align__(128) FlatStage {
+    float4 rec[2][kStageRecs][2];  // [buffer][record][q, pt]
+    unsigned long long bar[2];     // one mbarrier per buffer
+    uint32_t parity[2];            // the phase each buffer waits for next
+    uint32_t abort;                // a wait ran out
 };
 
-__device__ __forceinline__ void stage_copy16(float4* dst, const float4* src) {
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// lane 0 of a warp, once per kernel (before any copy)
+__device__ __forceinline__ void stage_init(FlatStage* P) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&P->bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&P->bar[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    P->parity[0] = P->parity[1] = 0u;
+    P->abort = 0u;
 }
-__device__ __forceinline__ void stage_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// lane 0: the window's total bytes, posted before the copies are issued
+__device__ __forceinline__ void stage_expect(FlatStage* P, uint32_t buf, uint32_t bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
+                 ::"r"(smem_u32(&P->bar[buf])), "r"(bytes) : "memory");
+}
+
+// one bulk copy of n 32-byte records (16-byte aligned source and destination)
+__device__ __forceinline__ void stage_copy(FlatStage* P, uint32_t buf, uint32_t at, const AccelRecWide* src,
+                                           uint32_t n) {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the buffer's earlier generic reads first
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(&P->rec[buf][at][0])),
+        "l"(src), "r"(n * 32u), "r"(smem_u32(&P->bar[buf]))
+        : "memory");
+}
+
+// every lane: wait for the buffer's copies (bounded); false when it timed out
+__device__ __forceinline__ bool stage_wait(FlatStage* P, uint32_t buf) {
+    const uint32_t bar = smem_u32(&P->bar[buf]), par = P->parity[buf];
+    uint32_t done = 0;
+    for (uint32_t k = 0; k < kStageSpinLimit && !done; k++) {
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(par)
+            : "memory");
+    }
+    __syncwarp();
+    return __all_sync(0xFFFFFFFFu, done != 0u);
+}
 
 // the rest of the exact test of queued record e for owner o (plane test passed)
 __device__ __forceinline__ void flat_test_queued(FlatWarp& H, const MeshDev& g, const AccelDev& acc, uint32_t e,
@@ -210,57 +253,47 @@ __device__ __forceinline__ void flat_round_mode(FlatWarp& H, const MeshDev& g, c
                     flat_file_hit(H, o1, h);
             }
         } else if (LAYOUT == 1 && P) {
-            // windows of 64 records, the next one staged while this one is tested
-            uint32_t e0 = 0, e1 = 0, o0 = 0, o1 = 0;
-            bool v0 = false, v1 = false;
-            auto locate = [&](uint32_t rb, uint32_t& a0, uint32_t& a1, uint32_t& w0_, uint32_t& w1_, bool& u0,
-                              bool& u1) {
-                const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
+            // windows of kStageRecs records staged by bulk copies, the next one in
+            // flight while this one is tested; lane k's cell holds the flat
+            // records [rincl - cnt, rincl) at global index b0
+            const uint32_t nwin = (rtotal + kStageRecs - 1) / kStageRecs;
+            const uint32_t rexcl = rincl - cnt;
+            auto issue = [&](uint32_t w, uint32_t buf) {
+                const uint32_t lo = w * kStageRecs, hi = min(lo + kStageRecs, rtotal);
+                if (lane == 0) stage_expect(P, buf, (hi - lo) * 32u);
+                __syncwarp();
+                const uint32_t a = max(rexcl, lo), z = min(rincl, hi);
+                if (a < z) stage_copy(P, buf, a - lo, acc.recw + b0 + (a - rexcl), z - a);
+            };
+            if (nwin > 0 && !P->abort) issue(0, 0);
+            for (uint32_t w = 0; w < nwin && !P->abort; w++) {
+                const uint32_t buf = w & 1u;
+                if (w + 1 < nwin) issue(w + 1, buf ^ 1u);
+                if (!stage_wait(P, buf)) {
+                    // a wait ran out: wait once more (bounded) for the copies in
+                    // flight to this buffer and the next, then stop the warp
+                    stage_wait(P, buf);
+                    if (w + 1 < nwin) stage_wait(P, buf ^ 1u);
+                    if (lane == 0) P->abort = 1u;
+                    __syncwarp();
+                    break;
+                }
+                if (lane == 0) P->parity[buf] ^= 1u;
+                const uint32_t lo = w * kStageRecs;
+                const uint32_t r0 = lo + lane, r1 = lo + 32 + lane;
                 const uint32_t j0 = min(warp_find(rincl, r0), 31u);
                 const uint32_t j1 = min(warp_find(rincl, r1), 31u);
-                a0 = __shfl_sync(FULL, rbase, j0) + r0;
-                a1 = __shfl_sync(FULL, rbase, j1) + r1;
-                w0_ = __shfl_sync(FULL, ow, j0);
-                w1_ = __shfl_sync(FULL, ow, j1);
-                u0 = r0 < rtotal;
-                u1 = r1 < rtotal;
-            };
-            auto stage = [&](uint32_t buf, uint32_t a0, uint32_t a1, bool u0, bool u1) {
-                float4* d = P->rec[buf][lane];
-                if (u0) {
-                    stage_copy16(d, &acc.recw[a0].q);
-                    stage_copy16(d + 1, &acc.recw[a0].pt);
-                }
-                if (u1) {
-                    stage_copy16(d + 2, &acc.recw[a1].q);
-                    stage_copy16(d + 3, &acc.recw[a1].pt);
-                }
-                stage_commit();
-            };
-            if (rtotal > 0) {
-                locate(0, e0, e1, o0, o1, v0, v1);
-                stage(0, e0, e1, v0, v1);
-            }
-            for (uint32_t rb = 0, buf = 0; rb < rtotal; rb += 64, buf ^= 1u) {
-                uint32_t n0 = 0, n1 = 0, p0 = 0, p1 = 0;
-                bool u0 = false, u1 = false;
-                const bool more = rb + 64 < rtotal;  // warp-uniform
-                if (more) {
-                    locate(rb + 64, n0, n1, p0, p1, u0, u1);
-                    stage(buf ^ 1u, n0, n1, u0, u1);
-                    stage_wait<1>();
-                } else {
-                    stage_wait<0>();
-                }
-                const float4* d = P->rec[buf][lane];
+                const uint32_t o0 = __shfl_sync(FULL, ow, j0);
+                const uint32_t o1 = __shfl_sync(FULL, ow, j1);
                 FastHit h;
-                if (v0 && test_wide_loaded(g, d[0], d[1], H.excl[o0], H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0],
-                                           H.dy[o0], H.dz[o0], h))
+                if (r0 < rtotal && test_wide_loaded(g, P->rec[buf][lane][0], P->rec[buf][lane][1], H.excl[o0],
+                                                    H.ox[o0], H.oy[o0], H.oz[o0], H.dx[o0], H.dy[o0], H.dz[o0], h))
                     flat_file_hit(H, o0, h);
-                if (v1 && test_wide_loaded(g, d[2], d[3], H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1],
-                                           H.dy[o1], H.dz[o1], h))
+                if (r1 < rtotal && test_wide_loaded(g, P->rec[buf][32 + lane][0], P->rec[buf][32 + lane][1],
+                                                    H.excl[o1], H.ox[o1], H.oy[o1], H.oz[o1], H.dx[o1], H.dy[o1],
+                                                    H.dz[o1], h))
                     flat_file_hit(H, o1, h);
-                e0 = n0; e1 = n1; o0 = p0; o1 = p1; v0 = u0; v1 = u1;
+                __syncwarp();  // the buffer's reads end before its next copies
             }
         } else if (LAYOUT == 1 || (LAYOUT == 0 && acc.wide)) {
             for (uint32_t rb = 0; rb < rtotal; rb += 64) {
