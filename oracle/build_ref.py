@@ -131,6 +131,34 @@ def build(reference):
     return [os.path.join(OUT, "harness3"), os.path.join(OUT, "harness2")]
 
 
+def build_dropin(libdir):
+    """The drop-in test programs: the reference's SpinSystem (the scratch copies
+    in oracle/_ref/src{3,2}, prepared by build()) with its GPU branch linked
+    against this project's libdsim3.so / libdsim2.so from `libdir`, in place
+    of the reference's spinSystem.cu.  Built where they run (the copies travel
+    with the tree; executables do not).  Returns (dropin3, dropin2) paths."""
+    src3, src2 = os.path.join(OUT, "src3"), os.path.join(OUT, "src2")
+    if not (os.path.exists(os.path.join(src3, "spinSystem.cpp")) and os.path.exists(os.path.join(src2, "spinSystem.cpp"))):
+        raise FileNotFoundError("the reference's scratch sources are not in oracle/_ref (run build() where the "
+                                "reference tree is present)")
+    cxx = os.environ.get("CXX", "g++")
+    # -fsigned-char: the reference's host code was written for x86-64, where char is signed
+    common = [cxx, "-O2", "-ffp-contract=off", "-fsigned-char", "-w", "-I", os.path.join(HARNESS, "include")]
+    rpath = ["-L", libdir, "-Wl,-rpath," + os.path.abspath(libdir)]
+    out3, out2 = os.path.join(OUT, "dropin3"), os.path.join(OUT, "dropin2")
+    jobs = [
+        common + ["-I", src3, os.path.join(src3, "spinSystem.cpp"), os.path.join(HARNESS, "dropin3.cpp"), "-o",
+                  out3] + rpath + ["-ldsim3"],
+        common + ["-I", src2, "-DDSIM2_ABI", os.path.join(src2, "spinSystem.cpp"), os.path.join(HARNESS, "dropin2.cpp"),
+                  "-o", out2] + rpath + ["-ldsim2"],
+    ]
+    procs = [subprocess.Popen(j, stderr=subprocess.PIPE) for j in jobs]
+    errs = [p.communicate()[1] for p in procs]
+    if any(p.returncode for p in procs):
+        raise RuntimeError("drop-in build failed:\n" + "\n".join(e.decode(errors="replace")[-3000:] for e in errs))
+    return out3, out2
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default=None, help="the reference tree (default: DSIM_REFERENCE or %s)"
