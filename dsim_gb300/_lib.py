@@ -195,6 +195,7 @@ def _declare_batch(L):
         "dsim_tensor_fit": (i32, [F32, F64, u32, F64, F64, F32, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                   C.POINTER(C.c_float)]),
         "dsim_simulate": (i32, [C.c_char_p, u64, u32, F64, u32, C.POINTER(u32), C.POINTER(C.c_double)]),
+        "dsim_write_results": (i32, [C.c_char_p, C.POINTER(Config), F32, F64, u32, C.c_double]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

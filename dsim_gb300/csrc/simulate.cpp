@@ -506,6 +506,106 @@ int dsim_tensor_fit(const float* rows, const double* signal, uint32_t nG, double
     return kOk;
 }
 
+int dsim_write_results(const char* outFile, const dsim_config* cfgp, const float* rowsp, const double* signals,
+                       uint32_t nG, double elapsed) {
+    if (!outFile || !cfgp || (nG && (!rowsp || !signals))) {
+        set_last_error(kErrInvalid, "dsim_write_results: null argument");
+        return kErrInvalid;
+    }
+    const dsim_config& cfg = *cfgp;
+    const std::vector<float> rows(rowsp, rowsp + 6 * (size_t)nG);
+    const float dt = cfg.timeStep;
+    // the reference keeps every signal in its float results table
+    // (gradientDataResults, dSim3/src/diffusion.cpp:575-577) before it fits
+    // and prints them
+    std::vector<double> sig32(5 * (size_t)nG);
+    for (size_t k = 0; k < sig32.size(); k++) sig32[k] = (double)(float)signals[k];
+    signals = sig32.data();
+    FILE* f = fopen(outFile, "at");
+    if (!f) { set_last_error(kErrFile, "cannot open %s", outFile); return kErrFile; }
+    time_t now = time(nullptr);
+    if (cfg.dialect == 3) {
+        // dSim3/src/diffusion.cpp:666-728
+        fprintf(f, "\n%% * * * %s", ctime(&now));
+        fprintf(f, "if (exist('m','var')), m=m+1; else, m=1; end\n");
+        fprintf(f, "s=0;\n");
+        fprintf(f, "\n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%% \n%% Input parameters \n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%\n");
+        fprintf(f, "numSpins(m) = %u;\n", cfg.numSpins);
+        fprintf(f, "useGpu(m) = %d;\n", 1);
+        fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
+        fprintf(f, "useDisplay(m) = %d;\n", 0);
+        fprintf(f, "stepsPerUpdate(m) = %i;\n", (int)cfg.stepsPerUpdate);
+        fprintf(f, "gyroMagneticRatio(m) = %g;\n", cfg.gamma);
+        fprintf(f, "timeStep(m) = %g;\n", cfg.timeStep);
+        fprintf(f, "extraAdc(m) = %g;\n", cfg.extraAdc);
+        fprintf(f, "intraAdc(m) = %g;\n", cfg.intraAdc);
+        fprintf(f, "myelinAdc(m) = %g;\n", cfg.myelinAdc);
+        fprintf(f, "spaceScale(m) = %g;\n", cfg.spaceScale);
+        fprintf(f, "permeability(m) = %g;\n", cfg.permeability);
+        fprintf(f, "\n\n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%% \n%% Simulation data \n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%\n\n");
+        fprintf(f, "%%The following variables give the diffusion tensor, eigenvector matrix, eigenvalues\n");
+        fprintf(f, "%%(eigenvalue no. i corresponds to column no. i in the eigenvector matrix), mean diffusivity,\n");
+        fprintf(f, "%%fractional anisotropy and radial diffusivity for the whole volume (index 1) and each\n");
+        fprintf(f, "%%compartment (index 2 for compartment 0, index 3 for compartment 1, etc).\n");
+        // the reference writes the fits of the total signal and compartments 0-2 as indices 1-4
+        for (int ci = 0; ci < 4; ci++) {
+            std::vector<double> sg(nG);
+            for (uint32_t g = 0; g < nG; g++) sg[g] = signals[5 * (size_t)g + ci];
+            double T[9] = {0}, E[9] = {0};
+            float ev[3] = {0, 0, 0}, mdv = 0, fav = 0, rdv = 0;
+            dsim_tensor_fit(rows.data(), sg.data(), nG, T, E, ev, &mdv, &fav, &rdv);
+            fprintf(f, "tensor{m}{%u} = [%g, %g, %g; %g, %g, %g; %g, %g, %g];\n", ci + 1, T[0], T[1], T[2], T[3], T[4], T[5], T[6], T[7], T[8]);
+            fprintf(f, "eigenvecs{m}{%u} = [%g, %g, %g; %g, %g, %g; %g, %g, %g];\n", ci + 1, E[0], E[1], E[2], E[3], E[4], E[5], E[6], E[7], E[8]);
+            fprintf(f, "eigenvals{m}{%u} = [%g,%g,%g];\n", ci + 1, ev[0], ev[1], ev[2]);
+            fprintf(f, "md{m}(%u) = %g;\n", ci + 1, mdv);
+            fprintf(f, "fa{m}(%u) = %g;\n", ci + 1, fav);
+            fprintf(f, "rd{m}(%u) = %g;\n", ci + 1, rdv);
+        }
+        fprintf(f, "%%The following variables give results for each gradient run.\n");
+        fprintf(f, "%%mrSigTotal{m}(c,s) is the total signal after gradient run s during diffusion simulation no. m\n");
+        fprintf(f, "%%mrSigCompartments{m}(c,s) is the contribution of compartment no. (c-2) to the \n");
+        fprintf(f, "%%total signal after gradient run s during diffusion simulation no. m. c=1 represents all compartments. \n");
+        for (uint32_t g = 0; g < nG; g++) {
+            const float* r = &rows[6 * g];
+            fprintf(f, "\ns=s+1;\n");
+            fprintf(f, "delta{m}(s) = %g;\n", r[0]);
+            fprintf(f, "Delta{m}(s) = %g;\n", r[1]);
+            fprintf(f, "readOut{m}(s) = %g;\n", r[2]);
+            fprintf(f, "dwGrads{m}(:,s) = [%g,%g,%g];\n\n", r[3], r[4], r[5]);
+            fprintf(f, "mrSigTotal{m}(s) = %g;\n\n", signals[5 * (size_t)g]);
+            for (int ci = 0; ci < 4; ci++)
+                fprintf(f, "mrSigCompartments{m}(%u,s) = %g;\n", ci + 1, signals[5 * (size_t)g + 1 + ci]);
+        }
+    } else {
+        // dSim2/src/diffusion.cpp:1756-1770 (header), 232-276 (per run, timing)
+        fprintf(f, "\n%% * * * %s", ctime(&now));
+        fprintf(f, "if(exist('m','var')), m=m+1; else, m=1; end\n");
+        fprintf(f, "s=0;\n");
+        fprintf(f, "spaceScale(m) = %g;\n", cfg.spaceScale);
+        fprintf(f, "numSpins(m) = %d;\n", (int)cfg.numSpins);
+        fprintf(f, "useGpu(m) = %d;\n", 1);
+        fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
+        double totalSteps = 0.0;
+        for (uint32_t g = 0; g < nG; g++) {
+            const float* r = &rows[6 * g];
+            uint32_t steps = 0;
+            dsim_pgse_schedule(r, dt, cfg.stepsPerUpdate, nullptr, 0, &steps);
+            totalSteps += steps;
+            fprintf(f, "s = s+1;\n");
+            fprintf(f, "delta{m}(s) = %g;\n", r[0]);
+            fprintf(f, "Delta{m}(s) = %g;\n", r[1]);
+            fprintf(f, "readOut{m}(s) = %g;\n", r[2]);
+            fprintf(f, "dwGrads{m}(:,s) = [%g;%g;%g];\n", r[3], r[4], r[5]);
+            fprintf(f, "mrSig{m}(s) = %g;\n", signals[5 * (size_t)g]);
+        }
+        fprintf(f, "%% Timing info:\n");
+        fprintf(f, "stepsPerSec(m) = %g;\n", elapsed > 0 ? totalSteps / elapsed : 0.0);
+        fprintf(f, "totalTime(m) = %g;\n", elapsed);
+    }
+    fclose(f);
+    return kOk;
+}
+
 int dsim_simulate(const char* cfgPath, uint64_t seed, uint32_t flags, double* signals, uint32_t cap, uint32_t* nGout,
                   double* seconds) {
     dsim_config cfg;
@@ -702,90 +802,8 @@ int dsim_simulate(const char* cfgPath, uint64_t seed, uint32_t flags, double* si
     if (seconds) *seconds = elapsed;
     cleanup();
     if (rc) return rc;
-    if ((flags & DSIM_SIM_WRITE_OUT) && cfg.outFile[0] && (cfg.dialect == 2 || cfg.writeOut)) {
-        FILE* f = fopen(cfg.outFile, "at");
-        if (!f) { set_last_error(kErrFile, "cannot open %s", cfg.outFile); return kErrFile; }
-        time_t now = time(nullptr);
-        if (cfg.dialect == 3) {
-            // dSim3/src/diffusion.cpp:666-728
-            fprintf(f, "\n%% * * * %s", ctime(&now));
-            fprintf(f, "if (exist('m','var')), m=m+1; else, m=1; end\n");
-            fprintf(f, "s=0;\n");
-            fprintf(f, "\n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%% \n%% Input parameters \n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%\n");
-            fprintf(f, "numSpins(m) = %u;\n", cfg.numSpins);
-            fprintf(f, "useGpu(m) = %d;\n", 1);
-            fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
-            fprintf(f, "useDisplay(m) = %d;\n", 0);
-            fprintf(f, "stepsPerUpdate(m) = %i;\n", (int)cfg.stepsPerUpdate);
-            fprintf(f, "gyroMagneticRatio(m) = %g;\n", cfg.gamma);
-            fprintf(f, "timeStep(m) = %g;\n", cfg.timeStep);
-            fprintf(f, "extraAdc(m) = %g;\n", cfg.extraAdc);
-            fprintf(f, "intraAdc(m) = %g;\n", cfg.intraAdc);
-            fprintf(f, "myelinAdc(m) = %g;\n", cfg.myelinAdc);
-            fprintf(f, "spaceScale(m) = %g;\n", cfg.spaceScale);
-            fprintf(f, "permeability(m) = %g;\n", cfg.permeability);
-            fprintf(f, "\n\n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%% \n%% Simulation data \n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%\n\n");
-            fprintf(f, "%%The following variables give the diffusion tensor, eigenvector matrix, eigenvalues\n");
-            fprintf(f, "%%(eigenvalue no. i corresponds to column no. i in the eigenvector matrix), mean diffusivity,\n");
-            fprintf(f, "%%fractional anisotropy and radial diffusivity for the whole volume (index 1) and each\n");
-            fprintf(f, "%%compartment (index 2 for compartment 0, index 3 for compartment 1, etc).\n");
-            // the reference writes the fits of the total signal and compartments 0-2 as indices 1-4
-            for (int ci = 0; ci < 4; ci++) {
-                std::vector<double> sg(nG);
-                for (uint32_t g = 0; g < nG; g++) sg[g] = signals[5 * (size_t)g + ci];
-                double T[9] = {0}, E[9] = {0};
-                float ev[3] = {0, 0, 0}, mdv = 0, fav = 0, rdv = 0;
-                dsim_tensor_fit(rows.data(), sg.data(), nG, T, E, ev, &mdv, &fav, &rdv);
-                fprintf(f, "tensor{m}{%u} = [%g, %g, %g; %g, %g, %g; %g, %g, %g];\n", ci + 1, T[0], T[1], T[2], T[3], T[4], T[5], T[6], T[7], T[8]);
-                fprintf(f, "eigenvecs{m}{%u} = [%g, %g, %g; %g, %g, %g; %g, %g, %g];\n", ci + 1, E[0], E[1], E[2], E[3], E[4], E[5], E[6], E[7], E[8]);
-                fprintf(f, "eigenvals{m}{%u} = [%g,%g,%g];\n", ci + 1, ev[0], ev[1], ev[2]);
-                fprintf(f, "md{m}(%u) = %g;\n", ci + 1, mdv);
-                fprintf(f, "fa{m}(%u) = %g;\n", ci + 1, fav);
-                fprintf(f, "rd{m}(%u) = %g;\n", ci + 1, rdv);
-            }
-            fprintf(f, "%%The following variables give results for each gradient run.\n");
-            fprintf(f, "%%mrSigTotal{m}(c,s) is the total signal after gradient run s during diffusion simulation no. m\n");
-            fprintf(f, "%%mrSigCompartments{m}(c,s) is the contribution of compartment no. (c-2) to the \n");
-            fprintf(f, "%%total signal after gradient run s during diffusion simulation no. m. c=1 represents all compartments. \n");
-            for (uint32_t g = 0; g < nG; g++) {
-                const float* r = &rows[6 * g];
-                fprintf(f, "\ns=s+1;\n");
-                fprintf(f, "delta{m}(s) = %g;\n", r[0]);
-                fprintf(f, "Delta{m}(s) = %g;\n", r[1]);
-                fprintf(f, "readOut{m}(s) = %g;\n", r[2]);
-                fprintf(f, "dwGrads{m}(:,s) = [%g,%g,%g];\n\n", r[3], r[4], r[5]);
-                fprintf(f, "mrSigTotal{m}(s) = %g;\n\n", signals[5 * (size_t)g]);
-                for (int ci = 0; ci < 4; ci++)
-                    fprintf(f, "mrSigCompartments{m}(%u,s) = %g;\n", ci + 1, signals[5 * (size_t)g + 1 + ci]);
-            }
-        } else {
-            // dSim2/src/diffusion.cpp:1756-1770 (header), 232-276 (per run, timing)
-            fprintf(f, "\n%% * * * %s", ctime(&now));
-            fprintf(f, "if(exist('m','var')), m=m+1; else, m=1; end\n");
-            fprintf(f, "s=0;\n");
-            fprintf(f, "spaceScale(m) = %g;\n", cfg.spaceScale);
-            fprintf(f, "numSpins(m) = %d;\n", (int)cfg.numSpins);
-            fprintf(f, "useGpu(m) = %d;\n", 1);
-            fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
-            double totalSteps = 0.0;
-            for (uint32_t g = 0; g < nG; g++) {
-                const float* r = &rows[6 * g];
-                uint32_t steps = 0;
-                dsim_pgse_schedule(r, dt, cfg.stepsPerUpdate, nullptr, 0, &steps);
-                totalSteps += steps;
-                fprintf(f, "s = s+1;\n");
-                fprintf(f, "delta{m}(s) = %g;\n", r[0]);
-                fprintf(f, "Delta{m}(s) = %g;\n", r[1]);
-                fprintf(f, "readOut{m}(s) = %g;\n", r[2]);
-                fprintf(f, "dwGrads{m}(:,s) = [%g;%g;%g];\n", r[3], r[4], r[5]);
-                fprintf(f, "mrSig{m}(s) = %g;\n", signals[5 * (size_t)g]);
-            }
-            fprintf(f, "%% Timing info:\n");
-            fprintf(f, "stepsPerSec(m) = %g;\n", elapsed > 0 ? totalSteps / elapsed : 0.0);
-            fprintf(f, "totalTime(m) = %g;\n", elapsed);
-        }
-        fclose(f);
-    }
+    if ((flags & DSIM_SIM_WRITE_OUT) && cfg.outFile[0] && (cfg.dialect == 2 || cfg.writeOut))
+        return dsim_write_results(cfg.outFile, &cfg, rows.data(), signals, nG, elapsed);
     return kOk;
 }
 

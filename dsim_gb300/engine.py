@@ -621,6 +621,19 @@ def tensor_fit(rows, signal):
             "rd": rd.value}
 
 
+def write_results(out_path, config, rows, signals, seconds=0.0):
+    """Append the reference's results block (dsim_write_results) for gradient
+    rows [n, 6] and signals [n, 5]; config: a dict as load_config returns."""
+    c = _lib.Config()
+    for name, _ in c._fields_:
+        if name in config:
+            v = config[name]
+            setattr(c, name, v.encode() if isinstance(v, str) else v)
+    r = np.ascontiguousarray(rows, F).reshape(-1)
+    sg = np.ascontiguousarray(signals, np.float64).reshape(-1)
+    check(native().dsim_write_results(str(out_path).encode(), C.byref(c), r, sg, len(r) // 6, float(seconds)))
+
+
 def simulate(cfg_path, seed=1, shared_walk=False, write_out=False, cap=4096):
     """Run a sim.cfg on the GPU: (signals [nG, 5], seconds)."""
     out = np.zeros(5 * cap, np.float64)

@@ -61,6 +61,17 @@ int dsim_pgse_schedule(const float row[6], float timeStep, uint32_t stepsPerUpda
 int dsim_tensor_fit(const float* rows, const double* signal, uint32_t nG, double tensor[9], double eigvecs[9],
                     float eigvals[3], float* md, float* fa, float* rd);
 
+/* Appends the reference's results block for one simulation to outFile.
+ * dSim3 dialect (dSim3/src/diffusion.cpp:666-728): the input parameters, the
+ * tensor fits of the total signal and of compartments 0-2 as indices 1-4 (the
+ * reference's indexing), then every row with its signals.  dSim2 dialect
+ * (dSim2/src/diffusion.cpp:1756-1770, 232-276): the header, one block per row
+ * and the stepsPerSec / totalTime timing from `seconds`.  rows [nG][6],
+ * signals [nG][5] as dsim_simulate returns them; like the reference, the
+ * signals are rounded to float before they are fitted and printed. */
+int dsim_write_results(const char* outFile, const dsim_config* cfg, const float* rows, const double* signals,
+                       uint32_t nG, double seconds);
+
 #define DSIM_SIM_SHARED_WALK 1u  /* one walk per (delta, Delta, readout) group, all its gradients from moments */
 #define DSIM_SIM_WRITE_OUT 2u    /* append the results file named by sim.outFile (if writeOut) */
 

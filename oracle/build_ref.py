@@ -21,7 +21,13 @@ scratch copy in oracle/_ref/src{2,3}/:
   * dSim3 HITARRAYSIZE (spinSystem.cpp:1608, a stack buffer of 2000 hits for
     compartment assignment) is raised to 65536;
   * dSim2 spinSystem.cpp includes the unused radix-sort header
-    (radixsort.cuh, never called); that include is dropped.
+    (radixsort.cuh, never called); that include is dropped;
+  * from dSim3/src/diffusion.cpp, whose main program needs OpenGL, GLUT and
+    libconfig, only three pieces are taken, unchanged: the gradStruct type,
+    computeTensor() and update() (oracle/_ref/src3/diffusion_parts.inc, with
+    the vendored JAMA/TNT headers copied beside it).  The sequencer harness
+    (refharness/seq3.cpp) defines the globals they use and stands in for the
+    SpinSystem they drive.
 The host side of the C-ABI (allocateArray -> malloc, copy* -> memcpy) and the
 cutil timer macros are provided by oracle/refharness/.
 
@@ -100,8 +106,45 @@ def patch_dsim2(src):
     return text
 
 
+def _cut(text, start):
+    """The text from `start` to its matching closing brace, through the end
+    of that line (a typedef's closing "} name;" included)."""
+    i = text.index(start)
+    depth, j, seen = 0, i, False
+    while True:
+        c = text[j]
+        if c == "{":
+            depth += 1
+            seen = True
+        elif c == "}":
+            depth -= 1
+            if seen and depth == 0:
+                break
+        j += 1
+    k = text.index("\n", j)
+    return text[i:k + 1]
+
+
+def diffusion_parts(reference):
+    """gradStruct, computeTensor() and update() of dSim3/src/diffusion.cpp, verbatim."""
+    with open(os.path.join(reference, "dSim3", "src", "diffusion.cpp")) as fh:
+        text = fh.read()
+    parts = [_cut(text, "typedef struct _gradStruct{"),
+             _cut(text, "void computeTensor(uint index, double tensors[][3][3]"),
+             _cut(text, "void update(){")]
+    return "/* taken unchanged from dSim3/src/diffusion.cpp by oracle/build_ref.py */\n" + "\n".join(parts)
+
+
 def build(reference):
     os.makedirs(OUT, exist_ok=True)
+    for sub in ("jama", "tnt"):
+        dst = os.path.join(OUT, sub)
+        if os.path.isdir(dst):
+            shutil.rmtree(dst)
+        shutil.copytree(os.path.join(reference, "dSim3", sub), dst)
+    os.makedirs(os.path.join(OUT, "src3"), exist_ok=True)
+    with open(os.path.join(OUT, "src3", "diffusion_parts.inc"), "w") as fh:
+        fh.write(diffusion_parts(reference))
     for tree, files, patch in (("dSim3", DSIM3_FILES, patch_dsim3),
                                ("dSim2", DSIM2_FILES, patch_dsim2)):
         dst = os.path.join(OUT, "src" + tree[-1])
@@ -123,12 +166,19 @@ def build(reference):
                   os.path.join(OUT, "src2", "spinSystem.cpp"),
                   os.path.join(HARNESS, "host_abi.cpp"), os.path.join(HARNESS, "harness2.cpp"),
                   "-o", os.path.join(OUT, "harness2")],
+        common + ["-I", os.path.join(OUT, "src3"), "-I", os.path.join(OUT, "jama"), "-I", os.path.join(OUT, "tnt"),
+                  os.path.join(HARNESS, "seq3.cpp"), "-o", os.path.join(OUT, "seq3")],
     ]
     procs = [subprocess.Popen(j) for j in jobs]
     rc = [p.wait() for p in procs]
     if any(rc):
         raise SystemExit("reference harness build failed: %r" % rc)
     return [os.path.join(OUT, "harness3"), os.path.join(OUT, "harness2")]
+
+
+def sequencer_harness():
+    """The sequencer harness that build() compiles (refharness/seq3.cpp)."""
+    return os.path.join(OUT, "seq3")
 
 
 def build_dropin(libdir):

@@ -126,6 +126,76 @@ def matlab_collision_case():
         json.dump(case, fh, indent=1)
 
 
+SEQ_CONFIG = dict(numSpins=20000, gamma=42576.0, extraAdc=2.0, intraAdc=1.8, myelinAdc=0.2, spaceScale=25.0,
+                  permeability=0.001, fiberFile="tubes.mesh")
+
+
+def _tensor_signals(rows):
+    """Per row and signal column (total, compartments 0-3): S0 exp(-b g^T D g)
+    for five anisotropic tensors D (um^2/ms) and five S0."""
+    rng = np.random.default_rng(17)
+    out = np.zeros((len(rows), 5))
+    for c in range(5):
+        A = rng.normal(size=(3, 3))
+        Q, _ = np.linalg.qr(A)
+        D = Q @ np.diag(np.sort(rng.uniform(0.2, 2.5, 3))) @ Q.T
+        s0 = rng.uniform(0.5, 1.0)
+        for k, r in enumerate(rows):
+            g = np.asarray(r[3:6], np.float64)
+            n = np.linalg.norm(g)
+            b = (2 * np.pi * 42576.0 * n * 1e-9 * r[0]) ** 2 * (r[1] - r[0] / 3.0)
+            u = g / n if n > 0 else g
+            out[k, c] = s0 * np.exp(-b * (u @ D @ u))
+    return out
+
+
+def seq_fixture(name, rows, timeStep, spu, seq, tmp):
+    """The reference's update() / computeTensor() / writer on a gradient table
+    (refharness/seq3.cpp): every updateSpins call with its gradient, the
+    resets and reads, the results table, the fits and the results file."""
+    rows = np.asarray(rows, np.float32).reshape(-1, 6)
+    sig = _tensor_signals(rows)
+    runs = O.sequencer_runs(rows, timeStep, spu)
+    read = [k for k in range(len(rows)) if runs[k] is not None]
+    g = os.path.join(tmp, name + ".g")
+    sg = os.path.join(tmp, name + ".s")
+    rows.tofile(g)
+    given = np.zeros_like(sig)           # returned in read order; rows never read get none
+    given[:len(read)] = sig[read]
+    given.tofile(sg)
+    outm = os.path.join(tmp, name + ".m")
+    r = run(seq, grads=g, signals=sg, timeStep=timeStep, stepsPerUpdate=spu, outm=outm,
+            out=os.path.join(tmp, name + ".bin"), **SEQ_CONFIG)
+    with open(outm, "rb") as fh:
+        mtext = fh.read()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), rows=rows, signals=sig, timeStep=np.float32(timeStep),
+                        stepsPerUpdate=np.uint32(spu), config=json.dumps(SEQ_CONFIG), calls=r["calls"],
+                        events=r["events"], results=r["results"], tensors=r["tensors"], eigenvecs=r["eigenvecs"],
+                        lambdas=r["lambdas"], md=r["md"], fa=r["fa"], rd=r["rd"],
+                        mfile=np.frombuffer(mtext, np.uint8))
+    return r
+
+
+def seq_fixtures(tmp):
+    from dsim_gb300.engine import parse_grads
+    from dsim_gb300.jobs import fibonacci_dirs, pgse_gmag
+    seq = build_ref.sequencer_harness()
+    # the reference's own gradient table
+    seq_fixture("seq_simgrads", parse_grads(path=os.path.join(REFERENCE, "dSim3", "sim.grads")), 0.01, 10, seq, tmp)
+    # Fibonacci directions at two b-values, with a row whose readout rounds to
+    # zero updates (its signal is never read) in the middle
+    rows = [[5.0, 20.0, 1.0, 0.0, 0.0, 0.0]]
+    for b in (0.5, 1.0):
+        for d in fibonacci_dirs(12):
+            rows.append([5.0, 20.0, 1.0, *(pgse_gmag(b, 5.0, 20.0) * d)])
+    rows.insert(7, [5.0, 20.0, 0.001, *(pgse_gmag(1.0, 5.0, 20.0) * fibonacci_dirs(12)[3])])
+    seq_fixture("seq_fib", rows, 0.005, 1, seq, tmp)
+    # six directions span five tensor components: the rank-deficient fit
+    rows = [[8.0, 25.0, 2.0, 0.0, 0.0, 0.0]] + [[8.0, 25.0, 2.0, *(pgse_gmag(1.5, 8.0, 25.0) * d)]
+                                               for d in fibonacci_dirs(6)]
+    seq_fixture("seq_rank6", rows, 0.01, 5, seq, tmp)
+
+
 def main():
     if REFERENCE is None:
         raise SystemExit("the reference tree is not present (set DSIM_REFERENCE)")
@@ -134,6 +204,7 @@ def main():
         mesh_fixture("mesh_am", "AM", 0.05, 11, h3, tmp)
         mesh_fixture("mesh_g", "G", 0.2, 12, h3, tmp)
         cyl_fixture("cyl", h2, tmp)
+        seq_fixtures(tmp)
     matlab_collision_case()
     print("fixtures written to", HERE)
 
