@@ -530,33 +530,30 @@ static int cyl_fine_build(dsim_cyl* c, uint32_t k) {
     return kOk;
 }
 
+// the fibers on the device, the reference's grid built there (addEntities,
+// cyl.cu) with each entry's fiber record inline, host mirrors of the grid for
+// the fine lists and dsim_cyl_info, then the fine filter grid
 static int cyl_upload(dsim_cyl* c) {
     int rc;
     CylHost& h = c->host;
-    if ((rc = dev_alloc(&c->fibers, h.nF, &c->bytes))) return rc;
-    if ((rc = dev_alloc(&c->cc, h.cubeCounter.size(), &c->bytes))) return rc;
-    if ((rc = dev_alloc(&c->cubes, h.cubes.size(), &c->bytes))) return rc;
+    if ((rc = cyl_grid_geometry(h))) return rc;
+    const size_t ncells = (size_t)h.numCubes * h.numCubes * h.numCubes;
+    const size_t slots = std::max<size_t>(1, ncells * h.maxFPC);
+    if ((rc = dev_alloc(&c->fibers, std::max<uint32_t>(1, h.nF), &c->bytes))) return rc;
+    if ((rc = dev_alloc(&c->cc, ncells, &c->bytes))) return rc;
+    if ((rc = dev_alloc(&c->cubes, slots, &c->bytes))) return rc;
+    if ((rc = dev_alloc(&c->cubeF, slots, &c->bytes))) return rc;
     if (h.nF) DSIM_CUDA_TRY(cudaMemcpy(c->fibers, h.fiberPos.data(), (size_t)h.nF * 16, cudaMemcpyHostToDevice));
-    DSIM_CUDA_TRY(cudaMemcpy(c->cc, h.cubeCounter.data(), h.cubeCounter.size() * 4, cudaMemcpyHostToDevice));
+    uint32_t mx = 0;
+    if ((rc = build_cyl_grid_gpu(c->fibers, h.nF, h.numCubes, h.maxFPC, h.cubeLength, h.maxR, c->cc, c->cubes,
+                                 c->cubeF, &mx, 0)))
+        return rc;
+    h.cubeCounter.resize(ncells);
+    h.cubes.resize(ncells * h.maxFPC);
+    DSIM_CUDA_TRY(cudaMemcpy(h.cubeCounter.data(), c->cc, ncells * 4, cudaMemcpyDeviceToHost));
     if (!h.cubes.empty())
-        DSIM_CUDA_TRY(cudaMemcpy(c->cubes, h.cubes.data(), h.cubes.size() * 4, cudaMemcpyHostToDevice));
-    // the fiber records inline in the grid, so a cell scan reads no index
-    // first; only for a grid whose listed entries all name a fiber
-    const size_t ncells = h.cubeCounter.size();
-    std::vector<float> inl(h.cubes.size() * 4, 0.0f);
-    bool ok = !h.cubes.empty();
-    for (size_t cell = 0; cell < ncells && ok; cell++)
-        for (uint32_t j = 0; j < h.cubeCounter[cell] && ok; j++) {
-            const size_t k = cell * h.maxFPC + j;
-            const uint32_t fi = h.cubes[k];
-            if (fi >= h.nF) { ok = false; break; }
-            for (int q = 0; q < 4; q++) inl[4 * k + q] = h.fiberPos[4 * (size_t)fi + q];
-        }
-    if (ok) {
-        if ((rc = dev_alloc(&c->cubeF, h.cubes.size(), &c->bytes))) return rc;
-        DSIM_CUDA_TRY(cudaMemcpy(c->cubeF, inl.data(), inl.size() * 4, cudaMemcpyHostToDevice));
-        if ((rc = cyl_fine_build(c, cyl_fine_default(h)))) return rc;
-    }
+        DSIM_CUDA_TRY(cudaMemcpy(h.cubes.data(), c->cubes, h.cubes.size() * 4, cudaMemcpyDeviceToHost));
+    if ((rc = cyl_fine_build(c, cyl_fine_default(h)))) return rc;
     return kOk;
 }
 
@@ -565,7 +562,6 @@ int dsim_cyl_load(const char* path, float spaceScale, dsim_cyl** out) {
     *out = nullptr;
     dsim_cyl* c = new dsim_cyl();
     int rc = parse_cyl_file(path, spaceScale, c->host);
-    if (!rc) rc = build_cyl_grid(c->host);
     if (!rc) rc = cyl_upload(c);
     if (rc) { cyl_release(c); return rc; }
     *out = c;
@@ -579,8 +575,7 @@ int dsim_cyl_create(const float* fiberPos4, uint32_t nFibers, float maxRadius, d
     c->host.nF = nFibers;
     c->host.fiberPos.assign(fiberPos4, fiberPos4 + (size_t)nFibers * 4);
     c->host.maxR = maxRadius;
-    int rc = build_cyl_grid(c->host);
-    if (!rc) rc = cyl_upload(c);
+    int rc = cyl_upload(c);
     if (rc) { cyl_release(c); return rc; }
     *out = c;
     return kOk;

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <vector>
 #include "common.cuh"
 #include "cyl_common.cuh"
 #include "engine.h"
@@ -85,6 +86,157 @@ int cyl_fine_lists(const float* fiberPos, uint32_t nF, uint32_t n, uint32_t maxF
             return kErrTooLarge;
         }
     }
+    return kOk;
+}
+
+// ---- the reference's cylinder grid, built on the GPU ----------------------
+// addEntities (dSim2/src/spinSystem.cpp:483-745): a fiber is listed in every
+// cell of the line of cells along its axis through its centre (the line's
+// cells found by stepping a point from -1 + 0.002 by one cell length), and in
+// the neighbouring lines that its radius plus a 1.1 halo can reach.  One
+// thread per fiber replays that insertion sequence with the same float
+// operations; pass 1 counts the entries per cell, pass 2 files each entry with
+// its tag (fiber << 10 | insertion index), and a per-cell sort of the tags
+// restores the reference's order (fibers in file order, each fiber's lines in
+// the order addEntities adds them, repeats kept).
+static constexpr uint32_t kCylSeqBits = 10;  // insertion index: at most 5 lines x 100 cells
+
+template <typename Emit>
+__device__ void cyl_fiber_insertions(float4 fr, uint32_t n, float L, float H, Emit emit) {
+    float fp[3] = {fr.x, fr.y, fr.z};
+    int a, f, s;
+    if (fp[0] == 2.0f) { a = 0; f = 2; s = 1; }
+    else if (fp[2] == 2.0f) { a = 2; f = 0; s = 1; }
+    else if (fp[1] == 2.0f) { a = 1; f = 2; s = 0; }
+    else return;
+    const float start = (float)(-1.0 + 0.002);
+    uint32_t seq = 0;
+    auto line = [&](float* cp) {
+        cp[a] = start;
+        for (uint32_t j = 0; j < n; j++) {
+            emit(cyl_cell(cp[0], cp[1], cp[2], L, n), seq++);
+            cp[a] += L;
+        }
+    };
+    float cp[3] = {fp[0], fp[1], fp[2]};
+    line(cp);
+    float tp[3] = {fp[0], fp[1], fp[2]};
+    tp[a] = start;
+    const float inv = 1.0f / L;
+    const float cpos_f = floorf((tp[f] + 1.0f) * inv), cpos_s = floorf((tp[s] + 1.0f) * inv);
+    const float dfc_f = tp[f] - cpos_f * L;
+    const float dfc_s = tp[s] - cpos_s * L;
+    if (dfc_f < H) {
+        cp[f] -= H;
+        if (cp[f] > -1) {
+            line(cp);
+            if ((cp[s] - L) > -1) { cp[s] -= L; line(cp); cp[s] += L; }
+            if ((cp[s] + L) < 1) { cp[s] += L; line(cp); cp[s] -= L; }
+        }
+        cp[f] += H;
+    } else if (dfc_f > (L - H)) {
+        cp[f] += H;
+        if (cp[f] < 1) {
+            line(cp);
+            if ((cp[s] - L) > -1) { cp[s] -= L; line(cp); cp[s] += L; }
+            if ((cp[s] + L) < 1) { cp[s] += L; line(cp); cp[s] -= L; }
+        }
+        cp[f] -= H;
+    }
+    if (dfc_s < H) {
+        if ((cp[s] - L) > -1) { cp[s] -= L; line(cp); cp[s] += L; }
+    } else if (dfc_s > (L - H)) {
+        if ((cp[s] + L) < 1) { cp[s] += L; line(cp); cp[s] -= L; }
+    }
+}
+
+__global__ void k_cyl_grid_count(const float4* __restrict__ fibers, uint32_t nF, uint32_t n, float L, float H,
+                                 uint32_t* counter) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nF) return;
+    cyl_fiber_insertions(fibers[i], n, L, H, [&](uint32_t cell, uint32_t) { atomicAdd(counter + cell, 1u); });
+}
+
+__global__ void k_cyl_grid_fill(const float4* __restrict__ fibers, uint32_t nF, uint32_t n, float L, float H,
+                                uint32_t maxFPC, uint32_t* counter, uint32_t* tags) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nF) return;
+    cyl_fiber_insertions(fibers[i], n, L, H, [&](uint32_t cell, uint32_t seq) {
+        const uint32_t slot = atomicAdd(counter + cell, 1u);
+        if (slot < maxFPC) tags[(size_t)cell * maxFPC + slot] = (i << kCylSeqBits) | seq;
+    });
+}
+
+// per cell: its tags in ascending order become the fiber list; the unused
+// slots stay 0 as the reference's memset leaves them
+__global__ void k_cyl_grid_order(uint32_t ncells, uint32_t maxFPC, const uint32_t* __restrict__ counter,
+                                 uint32_t* tags, uint32_t* cubes) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    uint32_t* t = tags + (size_t)c * maxFPC;
+    const uint32_t cnt = min(counter[c], maxFPC);
+    for (uint32_t k = 1; k < cnt; k++) {
+        const uint32_t v = t[k];
+        uint32_t j = k;
+        while (j > 0 && t[j - 1] > v) { t[j] = t[j - 1]; j--; }
+        t[j] = v;
+    }
+    uint32_t* out = cubes + (size_t)c * maxFPC;
+    for (uint32_t k = 0; k < maxFPC; k++) out[k] = k < cnt ? (t[k] >> kCylSeqBits) : 0u;
+}
+
+// each listed entry's fiber record beside it (the step reads one record per entry)
+__global__ void k_cyl_grid_inline(size_t slots, uint32_t maxFPC, const uint32_t* __restrict__ counter,
+                                  const uint32_t* __restrict__ cubes, const float4* __restrict__ fibers,
+                                  float4* cubeF) {
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= slots) return;
+    const uint32_t cell = (uint32_t)(k / maxFPC), j = (uint32_t)(k % maxFPC);
+    cubeF[k] = j < counter[cell] ? fibers[cubes[k]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+int build_cyl_grid_gpu(const float4* fibers, uint32_t nF, uint32_t n, uint32_t maxFPC, float L, float maxR,
+                       uint32_t* counter, uint32_t* cubes, float4* cubeF, uint32_t* maxCount, cudaStream_t st) {
+    if (nF >= (1u << (32 - kCylSeqBits)) || n > 100) {
+        set_last_error(kErrTooLarge, "cylinder grid: %u fibers or %u cells per axis above the build's limits", nF, n);
+        return kErrTooLarge;
+    }
+    const float H = 1.1f * maxR;
+    const uint32_t ncells = n * n * n;
+    const size_t slots = (size_t)ncells * maxFPC;
+    DSIM_CUDA_TRY(cudaMemsetAsync(counter, 0, (size_t)ncells * 4, st));
+    const uint32_t fb = (nF + 127) / 128;
+    if (nF) k_cyl_grid_count<<<fb, 128, 0, st>>>(fibers, nF, n, L, H, counter);
+    DSIM_CUDA_TRY(cudaGetLastError());
+    std::vector<uint32_t> cnt(ncells);
+    DSIM_CUDA_TRY(cudaMemcpyAsync(cnt.data(), counter, (size_t)ncells * 4, cudaMemcpyDeviceToHost, st));
+    DSIM_CUDA_TRY(cudaStreamSynchronize(st));
+    uint32_t mx = 0;
+    for (uint32_t v : cnt) mx = std::max(mx, v);
+    *maxCount = mx;
+    if (mx > maxFPC) {
+        set_last_error(kErrGridOverflow, "cylinder grid: %u fibers in one cell, limit %u (build() fails)", mx, maxFPC);
+        return kErrGridOverflow;
+    }
+    uint32_t* tags = nullptr;
+    DSIM_CUDA_TRY(cudaMalloc(&tags, std::max<size_t>(1, slots) * 4));
+    cudaError_t e = cudaMemsetAsync(counter, 0, (size_t)ncells * 4, st);
+    if (e == cudaSuccess && nF) {
+        k_cyl_grid_fill<<<fb, 128, 0, st>>>(fibers, nF, n, L, H, maxFPC, counter, tags);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        k_cyl_grid_order<<<(ncells + 127) / 128, 128, 0, st>>>(ncells, maxFPC, counter, tags, cubes);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && cubeF && slots) {
+        k_cyl_grid_inline<<<(unsigned)((slots + 255) / 256), 256, 0, st>>>(slots, maxFPC, counter, cubes, fibers,
+                                                                          cubeF);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(tags);
+    if (e != cudaSuccess) { set_last_cuda_error(e, "cylinder grid build", __FILE__, __LINE__); return kErrCuda; }
     return kOk;
 }
 

@@ -143,6 +143,13 @@ int launch_dense_to_csr(uint32_t ncells, uint32_t maxTPC, uint32_t nT, const uin
                         const uint32_t* dense, const uint32_t* start, uint32_t* cell_tri,
                         uint32_t* status, cudaStream_t st);
 
+// ---- cyl.cu: the reference's cylinder grid on the GPU ----------------------
+// counter[n^3] and cubes[n^3 * maxFPC] (addEntities order), cubeF (optional):
+// each entry's fiber record; *maxCount: the fullest cell.  kErrGridOverflow
+// when a cell needs more than maxFPC entries (the reference's build() fails).
+int build_cyl_grid_gpu(const float4* fibers, uint32_t nF, uint32_t n, uint32_t maxFPC, float L, float maxR,
+                       uint32_t* counter, uint32_t* cubes, float4* cubeF, uint32_t* maxCount, cudaStream_t st);
+
 // ---- compartments.cu ------------------------------------------------------
 int launch_compartments(const MeshDev& g, const AccelDev& acc, const SpinsSorted& S, const float maxabs[3],
                         float startBox, uint64_t seed, uint32_t maxTries, uint32_t maxMoves, uint32_t* status,

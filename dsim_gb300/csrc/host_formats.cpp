@@ -171,80 +171,9 @@ int parse_cyl_file(const char* path, float spaceScale, CylHost& h) {
     return kOk;
 }
 
-// calcCubeHash(calcCubePos(p)) of dSim2/src/spinSystem.cpp:413-433
-static inline uint32_t cyl_cell_host(const float p[3], float L, uint32_t n) {
-    float inv = 1.0f / L;
-    float c[3];
-    float hi = (float)(n - 1);
-    for (int k = 0; k < 3; k++) {
-        c[k] = floorf((p[k] + 1.0f) * inv);
-        c[k] = fmaxf(fminf(c[k], hi), 0.0f);
-    }
-    return (uint32_t)((int)((float)(n * n) * c[2]) + (int)((float)n * c[1]) + (int)c[0]);
-}
-
-struct CylGridBuild {
-    CylHost& h;
-    bool write;
-    // FILL_LIST_{X,Y,Z}: one entry per cell along the fiber axis
-    void line(float cp[3], int axis, uint32_t fib) {
-        cp[axis] = (float)(-1 + 0.002);
-        for (uint32_t j = 0; j < h.numCubes; j++) {
-            uint32_t index = cyl_cell_host(cp, h.cubeLength, h.numCubes);
-            uint32_t counter = h.cubeCounter[index];
-            h.cubeCounter[index] += 1;
-            if (write) h.cubes[(size_t)index * h.maxFPC + counter] = fib;
-            cp[axis] += h.cubeLength;
-        }
-    }
-    // addEntities body for a fiber along axis a; halo first tested on axis f
-    // (with neighbour lines along s), then on axis s.
-    void fiber(const float* fp, uint32_t fib, int a, int f, int s) {
-        const float L = h.cubeLength;
-        float cp[3] = {fp[0], fp[1], fp[2]};
-        line(cp, a, fib);
-        float tp[3] = {fp[0], fp[1], fp[2]};
-        tp[a] = (float)(-1 + 0.002);
-        float inv = 1.0f / L;
-        float cpos_f = floorf((tp[f] + 1.0f) * inv), cpos_s = floorf((tp[s] + 1.0f) * inv);
-        float dfc_f = tp[f] - cpos_f * L;
-        float dfc_s = tp[s] - cpos_s * L;
-        float H = 1.1f * h.maxR;
-        if (dfc_f < H) {
-            cp[f] -= H;
-            if (cp[f] > -1) {
-                line(cp, a, fib);
-                if ((cp[s] - L) > -1) { cp[s] -= L; line(cp, a, fib); cp[s] += L; }
-                if ((cp[s] + L) < 1) { cp[s] += L; line(cp, a, fib); cp[s] -= L; }
-            }
-            cp[f] += H;
-        } else if (dfc_f > (L - H)) {
-            cp[f] += H;
-            if (cp[f] < 1) {
-                line(cp, a, fib);
-                if ((cp[s] - L) > -1) { cp[s] -= L; line(cp, a, fib); cp[s] += L; }
-                if ((cp[s] + L) < 1) { cp[s] += L; line(cp, a, fib); cp[s] -= L; }
-            }
-            cp[f] -= H;
-        }
-        if (dfc_s < H) {
-            if ((cp[s] - L) > -1) { cp[s] -= L; line(cp, a, fib); cp[s] += L; }
-        } else if (dfc_s > (L - H)) {
-            if ((cp[s] + L) < 1) { cp[s] += L; line(cp, a, fib); cp[s] -= L; }
-        }
-    }
-    void all() {
-        for (uint32_t i = 0; i < h.nF; i++) {
-            const float* fp = &h.fiberPos[4 * (size_t)i];
-            if (fp[0] == 2.0f) fiber(fp, i, 0, 2, 1);
-            else if (fp[2] == 2.0f) fiber(fp, i, 2, 0, 1);
-            else if (fp[1] == 2.0f) fiber(fp, i, 1, 2, 0);
-        }
-    }
-};
-
-// build() dSim2/src/spinSystem.cpp:135-228 (grid size) + addEntities()
-int build_cyl_grid(CylHost& h) {
+// build() dSim2/src/spinSystem.cpp:135-228: the grid's size (cells per axis,
+// list capacity, cell length); addEntities fills it on the GPU (cyl.cu)
+int cyl_grid_geometry(CylHost& h) {
     if (!(h.maxR > 0.0f)) {
         set_last_error(kErrInvalid, "cylinder substrate has no fiber with positive radius");
         return kErrInvalid;
@@ -255,21 +184,6 @@ int build_cyl_grid(CylHost& h) {
     h.numCubes = t;
     h.maxFPC = (uint32_t)ceil((double)(h.nF / (t * t) * 10));
     h.cubeLength = 2.0f / t;
-    size_t total = (size_t)t * t * t;
-    h.cubeCounter.assign(total, 0u);
-    CylGridBuild count{h, false};
-    count.all();
-    uint32_t maxE = 0;
-    for (uint32_t v : h.cubeCounter) if (v > maxE) maxE = v;
-    if (maxE > h.maxFPC) {
-        set_last_error(kErrGridOverflow, "cylinder grid: %u fibers in one cell, limit %u (build() fails)",
-                       maxE, h.maxFPC);
-        return kErrGridOverflow;
-    }
-    h.cubes.assign(total * h.maxFPC, 0u);
-    h.cubeCounter.assign(total, 0u);
-    CylGridBuild fill{h, true};
-    fill.all();
     return kOk;
 }
 

@@ -29,7 +29,7 @@ struct CylHost {
     std::vector<uint32_t> cubes;        // numCubes^3 * maxFPC
 };
 int parse_cyl_file(const char* path, float spaceScale, CylHost& out);
-int build_cyl_grid(CylHost& h);
+int cyl_grid_geometry(CylHost& h);
 
 // sim.cfg subset (libconfig grammar: groups, name = value;, comments) and the
 // gradient table (lines of "delta Delta readout Gx Gy Gz")

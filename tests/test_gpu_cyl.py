@@ -315,3 +315,42 @@ def test_cyl_fine_grid_in_a_batch(engine):
     assert ca[0] > 0 and np.array_equal(ca, cb)
     for x, y in zip(a, b_):
         assert np.array_equal(np.asarray(x).view(np.uint8), np.asarray(y).view(np.uint8))
+
+
+@pytest.mark.parametrize("nfib,rmax,seed", [(64, 0.1, 1), (150, 0.1, 5), (560, 0.05, 2), (3500, 0.02, 3), (4000, 0.02, 3), (10, 0.05, 4)])
+def test_cyl_grid_built_on_the_gpu_equals_add_entities(engine, nfib, rmax, seed):
+    """The grid dsim_cyl_create builds on the GPU equals addEntities
+    (dSim2/src/spinSystem.cpp:483-745, restated by the oracle and pinned to the
+    reference's own grid by the golden fixture): the cell counts and every
+    list in the reference's order, for fibers along all three axes with radii
+    that reach the halo lines on both sides; a grid whose fullest cell exceeds
+    the reference's list capacity is refused as its build() refuses it."""
+    from dsim_gb300.engine import Cylinders
+    rng = np.random.default_rng(seed)
+    fp = np.zeros((nfib, 4), np.float32)
+    fp[:, :3] = rng.uniform(-1.0 + rmax, 1.0 - rmax, (nfib, 3)).astype(np.float32)
+    axis = rng.integers(0, 3, nfib)
+    fp[np.arange(nfib), axis] = 2.0
+    r = (rng.uniform(0.3, 1.0, nfib) * rmax).astype(np.float32)
+    fp[:, 3] = r * r
+    maxR = float(r.max())
+    fp = fp.reshape(-1)
+    L = O.lib()
+    geom = np.zeros(2, np.uint32)
+    cl = C.c_float(0)
+    L.or2_build_grid(nfib, fp, maxR, geom, C.byref(cl), None, None)
+    n, maxfpc = int(geom[0]), int(geom[1])
+    cc = np.zeros(n ** 3, np.uint32)
+    cubes = np.zeros(max(1, n ** 3 * maxfpc), np.uint32)
+    rc = L.or2_build_grid(nfib, fp, maxR, geom, C.byref(cl), cc, cubes)
+    if rc != 0:
+        with pytest.raises(Exception):
+            Cylinders.from_arrays(fp, maxR)
+        return
+    c = Cylinders.from_arrays(fp, maxR)
+    assert (c.numCubes, c.maxFPC, np.float32(c.cubeLength)) == (n, maxfpc, np.float32(cl.value))
+    gcc, gcubes, gfp = c.grid()
+    assert cc.sum() > nfib                          # halo lines were added
+    assert np.array_equal(gcc, cc)
+    assert np.array_equal(gcubes, cubes)
+    assert np.array_equal(gfp.view(np.uint32), fp.view(np.uint32))
