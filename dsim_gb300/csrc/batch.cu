@@ -617,61 +617,56 @@ __global__ void k_batch_gather64(BatchSpins S, uint32_t slot0, uint32_t len, dou
 }
 
 // FP64 signal of one job for nG gradients: partial records per (block, g)
-static constexpr int kSigThreads = 256;
-// fp64: the job keeps FP64 positions and magnitudes (precision and
-// cell-local forms), which the readout then uses
+static constexpr int kSigThreads = 128;
+// Readout of one job for nG gradients sharing its waveform.  Warp w takes
+// the 32 gradients [32 (w % gw), 32 (w % gw) + 32) and the spins of segment
+// w / gw (contiguous slots): its lanes read each spin once (one address: a
+// broadcast load) and each lane keeps its own gradient's sums in registers,
+// so no per-gradient reduction across threads is needed.  partials[segment]
+// [gradient][15] = {X, Y, n} for all spins and per compartment, each summed in
+// slot order; k_batch_signal_final adds the segments in order, so the result
+// does not depend on the launch.  fp64: the job keeps FP64 positions and
+// magnitudes (precision and cell-local forms), which the readout then uses.
 __global__ void __launch_bounds__(kSigThreads) k_batch_signal(BatchSpins S, uint32_t slot0, uint32_t len,
                                                               const double* __restrict__ kg, uint32_t nG,
+                                                              uint32_t gw, uint32_t nseg, uint32_t segLen,
                                                               double region, bool fp64, double* partials) {
-    __shared__ double sh[kSigThreads / 32][15];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (uint32_t gi = 0; gi < nG; gi++) {
-        const double gx = kg[3 * gi], gy = kg[3 * gi + 1], gz = kg[3 * gi + 2];
-        double acc[15];
-#pragma unroll
-        for (int k = 0; k < 15; k++) acc[k] = 0.0;
-        for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
-            const uint32_t i = slot0 + k;
-            if (S.u[U_ID][i] == 0xFFFFFFFFu) continue;
-            if (region > 0.0) {  // dSim2's readout box (dSim2/src/spinSystem.cpp:944-978)
-                const double x = fp64 ? S.d[D_X][i] : (double)S.f[F_X][i];
-                const double y = fp64 ? S.d[D_Y][i] : (double)S.f[F_Y][i];
-                const double z = fp64 ? S.d[D_Z][i] : (double)S.f[F_Z][i];
-                if (!(x > -region && x < region && y > -region && y < region && z > -region && z < region)) continue;
-            }
-            const double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
-            const double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
-            const double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
-            const double ph = gx * Mx + gy * My + gz * Mz;
-            const double m = fp64 ? S.d[D_MAG][i] : (double)S.f[F_MAG][i];
-            double s, c;
-            sincos(ph, &s, &c);
-            const double X = m * c, Y = m * s;
-            const uint32_t comp = S.u[U_META][i] & 3u;
-            acc[0] += X; acc[1] += Y; acc[2] += 1.0;
-#pragma unroll
-            for (uint32_t q = 0; q < 4; q++) {
-                const bool on = comp == q;
-                acc[3 + 3 * q] += on ? X : 0.0;
-                acc[4 + 3 * q] += on ? Y : 0.0;
-                acc[5 + 3 * q] += on ? 1.0 : 0.0;
-            }
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (warp >= gw * nseg) return;  // whole warps
+    const uint32_t gi = (warp % gw) * 32u + lane, sg = warp / gw;
+    const bool live = gi < nG;
+    const double gx = live ? kg[3 * gi] : 0.0, gy = live ? kg[3 * gi + 1] : 0.0, gz = live ? kg[3 * gi + 2] : 0.0;
+    double X = 0.0, Y = 0.0, cX[4] = {0.0, 0.0, 0.0, 0.0}, cY[4] = {0.0, 0.0, 0.0, 0.0};
+    uint32_t n = 0, cn[4] = {0u, 0u, 0u, 0u};
+    const uint32_t k0 = sg * segLen, k1 = min(len, k0 + segLen);
+    for (uint32_t k = k0; k < k1; k++) {  // the same spin on every lane: warp-uniform branches
+        const uint32_t i = slot0 + k;
+        if (S.u[U_ID][i] == 0xFFFFFFFFu) continue;
+        if (region > 0.0) {  // dSim2's readout box (dSim2/src/spinSystem.cpp:944-978)
+            const double x = fp64 ? S.d[D_X][i] : (double)S.f[F_X][i];
+            const double y = fp64 ? S.d[D_Y][i] : (double)S.f[F_Y][i];
+            const double z = fp64 ? S.d[D_Z][i] : (double)S.f[F_Z][i];
+            if (!(x > -region && x < region && y > -region && y < region && z > -region && z < region)) continue;
         }
-#pragma unroll
-        for (int k = 0; k < 15; k++) {
-            double v = acc[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-            if (lane == 0) sh[w][k] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < 15) {
-            double v = 0.0;
-            for (int j = 0; j < kSigThreads / 32; j++) v += sh[j][threadIdx.x];
-            partials[((size_t)blockIdx.x * nG + gi) * 15 + threadIdx.x] = v;
-        }
-        __syncthreads();
+        const double Mx = (double)S.f[F_MX][i] - (double)S.f[F_CX][i];
+        const double My = (double)S.f[F_MY][i] - (double)S.f[F_CY][i];
+        const double Mz = (double)S.f[F_MZ][i] - (double)S.f[F_CZ][i];
+        const double m = fp64 ? S.d[D_MAG][i] : (double)S.f[F_MAG][i];
+        const uint32_t comp = S.u[U_META][i] & 3u;
+        double sn, cs;
+        sincos(gx * Mx + gy * My + gz * Mz, &sn, &cs);
+        const double xs = m * cs, ys = m * sn;
+        X += xs; Y += ys; n++;
+        if (comp == 0) { cX[0] += xs; cY[0] += ys; cn[0]++; }
+        else if (comp == 1) { cX[1] += xs; cY[1] += ys; cn[1]++; }
+        else if (comp == 2) { cX[2] += xs; cY[2] += ys; cn[2]++; }
+        else { cX[3] += xs; cY[3] += ys; cn[3]++; }
     }
+    if (!live) return;
+    double* o = partials + ((size_t)sg * nG + gi) * 15;
+    o[0] = X; o[1] = Y; o[2] = (double)n;
+#pragma unroll
+    for (int q = 0; q < 4; q++) { o[3 + 3 * q] = cX[q]; o[4 + 3 * q] = cY[q]; o[5 + 3 * q] = (double)cn[q]; }
 }
 
 __global__ void k_batch_signal_final(const double* __restrict__ partials, uint32_t nb, uint32_t nG,
@@ -1302,7 +1297,11 @@ int dsim_batch_signal_region(dsim_batch* b, uint32_t jobId, const float* gradSca
         set_last_error(kErrInvalid, "dsim_batch_signal: bad argument");
         return kErrInvalid;
     }
-    const uint32_t nb = std::min<uint32_t>(608u, (j->pad + kSigThreads * 4 - 1) / (kSigThreads * 4));
+    // warps: 32 gradients x one spin segment each, about 16 warps per SM in all
+    const uint32_t gw = (nG + 31u) / 32u;
+    const uint32_t nseg = std::max<uint32_t>(1u, std::min<uint32_t>((j->pad + 63u) / 64u, std::max<uint32_t>(1u, 2432u / gw)));
+    const uint32_t segLen = (j->pad + nseg - 1u) / nseg;
+    const uint32_t nb = nseg;  // partial records per gradient
     std::vector<double> kg(3 * (size_t)nG);
     // phase = phaseConstant * (g . M); the job keeps phaseConstant in its descriptor
     for (uint32_t g = 0; g < nG; g++)
@@ -1317,8 +1316,10 @@ int dsim_batch_signal_region(dsim_batch* b, uint32_t jobId, const float* gradSca
     b->bytes -= kg.size() * 8 + (size_t)nb * nG * 15 * 8 + (size_t)nG * 15 * 8;
     cudaError_t e = cudaMemcpyAsync(dk, kg.data(), kg.size() * 8, cudaMemcpyHostToDevice, b->st);
     if (e == cudaSuccess) {
-        k_batch_signal<<<nb, kSigThreads, 0, b->st>>>(view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, region,
-                                                          j->d.flags != 0 && b->buf[b->cur].d[0] != nullptr, dp);
+        const uint32_t warps = gw * nseg;
+        k_batch_signal<<<(warps * 32u + kSigThreads - 1) / kSigThreads, kSigThreads, 0, b->st>>>(
+            view(b, b->cur), (uint32_t)j->slot0, j->pad, dk, nG, gw, nseg, segLen, region,
+            j->d.flags != 0 && b->buf[b->cur].d[0] != nullptr, dp);
         k_batch_signal_final<<<(nG * 15 + 127) / 128, 128, 0, b->st>>>(dp, nb, nG, dout);
         e = cudaGetLastError();
     }
