@@ -701,6 +701,12 @@ struct BatchJob {
 
 struct dsim_batch {
     cudaStream_t st = nullptr;
+    // the step kernels of a chunk (one per record layout and form) advance
+    // disjoint jobs: they run side by side on these streams, forked from st
+    // after the sort and joined before the step counter advances
+    static constexpr int kSide = 5;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t forkEv = nullptr, joinEv[kSide] = {};
     uint64_t cap = 0;
     uint32_t jobCap = 0;
     BatchBuf buf[2];
@@ -898,16 +904,16 @@ k_batch_step_cyl64(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
 }
 
 template <int LAYOUT>
-void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D) {
+void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D, cudaStream_t st) {
     if (b->occupancy >= 8)
-        k_batch_step<8, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts);
+        k_batch_step<8, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                             b->d_status, b->d_counts);
     else if (b->occupancy >= 6)
-        k_batch_step<6, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts);
+        k_batch_step<6, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                             b->d_status, b->d_counts);
     else
-        k_batch_step<4, LAYOUT><<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                 b->d_status, b->d_counts);
+        k_batch_step<4, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                             b->d_status, b->d_counts);
 }
 
 // one chunk: sort into the other buffer, step, advance the step counter
@@ -924,18 +930,41 @@ int enqueue_chunk(dsim_batch* b) {
     b->cur = 1 - b->cur;
     const uint32_t grid = (N + kFlatThreads - 1) / kFlatThreads;
     const uint32_t mask = step_layouts(b);
-    if (mask & (1u << 1)) launch_step_layout<1>(b, grid, D);
-    if (mask & (1u << 2)) launch_step_layout<2>(b, grid, D);
-    if (mask & (1u << 3)) launch_step_layout<3>(b, grid, D);
-    if (b->anyLocal)
-        k_batch_step_local<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                             b->d_status, b->d_counts);
-    if (b->anyPrecise)
-        k_batch_step64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk, b->d_status,
-                                                         b->d_counts);
-    if (b->anyPreciseCyl)
-        k_batch_step_cyl64<<<grid, kFlatThreads, 0, b->st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                             b->d_status, b->d_counts);
+    // the step kernels this chunk needs, each on its own stream when there
+    // are several (they advance disjoint jobs)
+    int kinds[8], nk = 0;
+    for (int L = 1; L <= 3; L++)
+        if (mask & (1u << L)) kinds[nk++] = L;
+    if (b->anyLocal) kinds[nk++] = 4;
+    if (b->anyPrecise) kinds[nk++] = 5;
+    if (b->anyPreciseCyl) kinds[nk++] = 6;
+    const bool fork = nk > 1;
+    if (fork) DSIM_CUDA_TRY(cudaEventRecord(b->forkEv, b->st));
+    for (int q = 0; q < nk; q++) {
+        cudaStream_t st = fork ? b->side[q % dsim_batch::kSide] : b->st;
+        if (fork) DSIM_CUDA_TRY(cudaStreamWaitEvent(st, b->forkEv, 0));
+        switch (kinds[q]) {
+            case 1: launch_step_layout<1>(b, grid, D, st); break;
+            case 2: launch_step_layout<2>(b, grid, D, st); break;
+            case 3: launch_step_layout<3>(b, grid, D, st); break;
+            case 4:
+                k_batch_step_local<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
+                break;
+            case 5:
+                k_batch_step64<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                              b->d_status, b->d_counts);
+                break;
+            default:
+                k_batch_step_cyl64<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
+                break;
+        }
+        if (fork) {
+            DSIM_CUDA_TRY(cudaEventRecord(b->joinEv[q % dsim_batch::kSide], st));
+            DSIM_CUDA_TRY(cudaStreamWaitEvent(b->st, b->joinEv[q % dsim_batch::kSide], 0));
+        }
+    }
     k_batch_advance<<<1, 1, 0, b->st>>>(b->d_stepNow, b->chunk);
     DSIM_CUDA_TRY(cudaGetLastError());
     b->launches += chunk_launches(b);  // keys, scan (3), scatter, step (per layout), advance
@@ -1015,6 +1044,11 @@ int dsim_batch_create(uint64_t spinCapacity, uint32_t jobCapacity, dsim_batch** 
     b->jobCap = jobCapacity;
     int rc = kOk;
     if (cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess) rc = kErrCuda;
+    for (int k = 0; k < dsim_batch::kSide && !rc; k++)
+        if (cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->joinEv[k], cudaEventDisableTiming) != cudaSuccess)
+            rc = kErrCuda;
+    if (!rc && cudaEventCreateWithFlags(&b->forkEv, cudaEventDisableTiming) != cudaSuccess) rc = kErrCuda;
     for (int k = 0; k < 2 && !rc; k++) {
         for (int f = 0; f < kBF && !rc; f++) rc = balloc(b, (void**)&b->buf[k].f[f], b->cap * 4);
         for (int u = 0; u < kBU && !rc; u++) rc = balloc(b, (void**)&b->buf[k].u[u], b->cap * 4);
@@ -1047,6 +1081,11 @@ void dsim_batch_free(dsim_batch* b) {
     cudaFree(b->d_jobs); cudaFree(b->d_subs); cudaFree(b->d_counts); cudaFree(b->d_status);
     cudaFree(b->d_stepNow);
     if (b->st) cudaStreamDestroy(b->st);
+    for (int k = 0; k < dsim_batch::kSide; k++) {
+        if (b->side[k]) cudaStreamDestroy(b->side[k]);
+        if (b->joinEv[k]) cudaEventDestroy(b->joinEv[k]);
+    }
+    if (b->forkEv) cudaEventDestroy(b->forkEv);
     for (const dsim_cyl* c : b->cylsHeld) cyl_hold(c, -1);
     delete b;
 }
