@@ -661,9 +661,10 @@ def _submit_kw(j, form="fp32"):
 
 def run_plain_mix(mix):
     """One job at a time through the plain path (dsim_mesh_run / dsim_cyl_run),
-    one walk with the job's first gradient; host clock from upload to signal."""
+    one walk with the job's first gradient; host clock from upload to signal.
+    Returns the times and the first gradient's signal of every job."""
     from dsim_gb300.engine import Spins, cyl_params, cyl_run, mesh_params, mesh_run, pgse_table
-    per = []
+    per, sig0 = [], []
     for k, j in enumerate([mix[0]] + list(mix)):  # the first job once untimed (module load)
         sub = j["sub"]
         w = pgse_table(j["steps"], float(j["dt"]), j["delta"], j["Delta"])
@@ -679,11 +680,32 @@ def run_plain_mix(mix):
             p = cyl_params(2.0, 2.0, 0.2, sub.spaceScale, 70.0, 8.0, 80.0, j["permeability"], j["inner"],
                            j["dt"], j["phase_constant"])
             cyl_run(sub.handle, s, p, grad_per_step=gps, iterations=j["steps"], seed=j["seed"])
-        s.signal()
+        sums = s.signal()
         if k > 0:
             per.append(time.perf_counter() - t0)
+            sig0.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
         del s
-    return per
+    return per, sig0
+
+
+def run_plain_bar_mix(subs, mix):
+    """One job at a time in the forms that hold the 1e-3 error bar (mesh jobs
+    cell-local, cylinder jobs FP64 positions): a batch holding that job alone,
+    from submission to its first gradient's signal."""
+    from dsim_gb300.engine import Batch
+    per, sig0 = [], []
+    for k, j in enumerate([mix[0]] + list(mix)):  # the first job once untimed (FP64 tables, module load)
+        b = Batch((j["n"] + 31) // 32 * 32, 1)
+        sid = b.add_mesh(j["sub"].handle) if j["sub"].kind == "mesh" else b.add_cyl(j["sub"].handle)
+        t0 = time.perf_counter()
+        jid = b.submit(sid, j["pos"], j["comp"], j["fiber"], **_submit_kw(j, "bar"))
+        b.run()
+        sums = b.signal(jid, j["grads"][:1])[0]
+        if k > 0:
+            per.append(time.perf_counter() - t0)
+            sig0.append(float(np.hypot(sums[0, 0], sums[0, 1]) / sums[0, 2]))
+        b.close()
+    return per, sig0
 
 
 def run_batched_mix(subs, mix, cfg, form="fp32"):
@@ -843,21 +865,31 @@ def run_forms(args, W, m):
         best, tune_ms = tune_mix(subs, mix)
         log("autotune: %s (%.1f ms for 60 steps of 8 jobs)" % (best, tune_ms))
     cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
-    per = run_plain_mix(mix)
+    per, psig = run_plain_mix(mix)
     plain_s = sum(per)
+    per_b, bsig = run_plain_bar_mix(subs, mix)
+    plainbar_s = sum(per_b)
     el, sigs, info, st = run_batched_mix(subs, mix, cfg)
     plain_rate = work / plain_s
+    plainbar_rate = work / plainbar_s
     t_err = time.time()
     ref, cyl_err = mix_fp64_reference(mix)
     batched_err = mix_err(mix, sigs, ref, cyl_err)
     batched_err["seconds"] = time.time() - t_err
+    first = lambda v: [np.array([[[x, 0.0, 1.0]] + [[0.0, 0.0, 0.0]] * 4]) for x in v]   # S as sums (X, Y=0, n=1)
     out = {
         "mix": {"jobs": n_jobs, "spins": list(spins_range), "steps": list(steps_range), "dt_us": [5, 10],
                 "substrates": "beaded tubes 400 and 100 axons (2.56M / 0.64M triangles), packed cylinders 64 and 256",
                 "gradients_per_job": "6-128 directions x 3 b-values (b <= 3000 s/mm2), one PGSE waveform",
                 "spin_steps": work},
         "plain": {"spin_steps_per_s": plain_rate, "seconds": plain_s,
-                  "note": "one job at a time (dsim_mesh_run / dsim_cyl_run), one walk per job"},
+                  "err_vs_fp64": mix_err(mix, first(psig), {i: r[:1] for i, r in ref.items()}, {}),
+                  "note": "one job at a time (dsim_mesh_run / dsim_cyl_run), one walk per job with its first "
+                          "gradient; the reference's FP32 step"},
+        "plain_bar": {"spin_steps_per_s": plainbar_rate, "seconds": plainbar_s,
+                      "err_vs_fp64": mix_err(mix, first(bsig), {i: r[:1] for i, r in ref.items()}, {}),
+                      "note": "one job at a time in the forms that hold the 1e-3 bar (a batch holding that job "
+                              "alone: mesh jobs cell-local, cylinder jobs FP64 positions), first gradient"},
         "batched": {"spin_steps_per_s": work / el, "seconds": el, "speedup_vs_plain": (work / el) / plain_rate,
                     "signals_speedup_vs_plain": (grad_work / el) / plain_rate,
                     "note": "all jobs in one batch; signals_speedup counts one plain walk per gradient, as the "
@@ -868,26 +900,32 @@ def run_forms(args, W, m):
     # the same mix in the forms that hold the 1e-3 error bar
     el_b, sigs_b, info_b, st_b = run_batched_mix(subs, mix, cfg, form="bar")
     out["batched_bar"] = {"spin_steps_per_s": work / el_b, "seconds": el_b,
+                          "speedup_vs_plain_bar": (work / el_b) / plainbar_rate,
                           "speedup_vs_plain": (work / el_b) / plain_rate,
-                          "signals_speedup_vs_plain": (grad_work / el_b) / plain_rate,
+                          "signals_speedup_vs_plain_bar": (grad_work / el_b) / plainbar_rate,
                           "status": st_b, "err_vs_fp64": mix_err(mix, sigs_b, ref, cyl_err),
                           "form": "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions "
                                   "(DSIM_JOB_PRECISE)"}
     # serving: the same substrates and ranges with permeable membranes (per-hit
-    # permeation log-uniform 1e-4 - 1e-2); arrival rates relative to the plain
-    # form's capacity on that mix
+    # permeation log-uniform 1e-4 - 1e-2), in the error-bar forms; arrival
+    # rates relative to the capacity of the plain form at the same bar (one
+    # job at a time) on that mix
     out["served"] = []
     if args.serve_rates:
         _, pmix = build_mix(W, m, n_jobs, 12, spins_range, steps_range, permeable=True, subs=subs)
-        pplain_s = sum(run_plain_mix(pmix))
-        cap_jobs = n_jobs / pplain_s
+        pwork = sum(j["n"] * j["steps"] for j in pmix)
+        pplain_s = sum(run_plain_mix(pmix)[0])
+        pbar_s = sum(run_plain_bar_mix(subs, pmix)[0])
+        cap_jobs = n_jobs / pbar_s
         out["served_mix"] = {"jobs": n_jobs, "seed": 12, "permeability": "log-uniform 1e-4 - 1e-2 per hit",
-                             "plain_spin_steps_per_s": sum(j["n"] * j["steps"] for j in pmix) / pplain_s,
-                             "plain_jobs_per_s": cap_jobs}
+                             "plain_spin_steps_per_s": pwork / pplain_s, "plain_jobs_per_s": n_jobs / pplain_s,
+                             "plain_bar_spin_steps_per_s": pwork / pbar_s, "plain_bar_jobs_per_s": cap_jobs,
+                             "rates_relative_to": "plain_bar_jobs_per_s"}
         pref, pcyl = mix_fp64_reference(pmix)
         for r in args.serve_rates:
             o, ssig = run_served_mix(subs, pmix, cfg, r * cap_jobs)
-            o["rate_x_plain_capacity"] = r
+            o["rate_x_plain_bar_capacity"] = r
+            o["speedup_vs_plain_bar"] = o["spin_steps_per_s"] / (pwork / pbar_s)
             o["err_vs_fp64"] = mix_err(pmix, ssig, pref, pcyl)
             o["form"] = "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
             out["served"].append(o)
@@ -1250,7 +1288,7 @@ def main():
     ap.add_argument("--mix-max-spins", type=int, default=1 << 18)
     ap.add_argument("--mix-min-steps", type=int, default=400)
     ap.add_argument("--mix-max-steps", type=int, default=2000)
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0, 1.5])
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[0.5, 1.0, 1.5, 3.0])
     ap.add_argument("--mix-config", type=int, nargs=2, default=None, metavar=("OCCUPANCY", "CHUNK"),
                     help="fixed batch occupancy and chunk for the job mix instead of autotuning")
     ap.add_argument("--no-precision", action="store_true", help="skip the precision-form comparison")
