@@ -69,14 +69,14 @@ int dsim_mesh_info(const dsim_mesh* m, uint64_t info[8]);
  * dsim_mesh_set_accel rebuilds it (0 = scan the reference grid directly).
  * info = {cells per axis, entries, device bytes}. */
 int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
-/* step kernel on the fine grid (all give the same results; default 8): 1 one thread per
- * spin walking its own candidate lists; 2, 3, 4 warp-cooperative candidate
- * tests compiled for 4, 6, 8 resident blocks of 128 threads per SM; 5, 6, 7 the
- * warp's candidate records flattened into one list, lanes stepping
- * independently (8, 6, 4 blocks per SM); 8 as 6, with the records that pass
- * the plane test queued and finished 32 at a time; 9 as 6, with each 64-record
- * window staged in shared memory by asynchronous copies while the previous
- * one is tested (8 and 9: 32-byte records) */
+/* step kernel on the fine grid (all give the same results; default 8; other
+ * values are refused): 5, 6, 7 the warp's candidate records flattened into one
+ * list, lanes stepping independently (8, 6, 4 resident blocks of 128 threads
+ * per SM); 8 as 6, with the records that pass the plane test queued and
+ * finished 32 at a time; 9 as 6, with each lane's part of every 64-record
+ * window copied into shared memory by TMA bulk copies (cp.async.bulk,
+ * mbarrier completion) while the previous window is tested (8 and 9: 32-byte
+ * records) */
 int dsim_mesh_set_kernel(dsim_mesh* m, uint32_t variant);
 /* fine-grid record size: 32 (default) holds the plane data for the exact
  * plane test; 16 holds a prefilter record only (half the bytes, one more
