@@ -497,6 +497,8 @@ def run_ours(args, rank, world):
         res["precision"] = run_precision(args, W, m)
     if rank == 0 and args.c5_full:
         res["precision_full"] = run_precision_full(args, W, m)
+    if rank == 0 and args.c4_full:
+        res["serving_full"] = run_c4_full(args, W, m)
     if rank == 0 and not args.no_cylinders:
         res["cylinders"] = run_cylinders(args)
     if rank == 0 and not args.no_cpu:
@@ -633,12 +635,19 @@ def run_headline_error(args, W, m):
 # --------------------------------------------------------------------------
 # batched and served forms on a seeded job mix
 # --------------------------------------------------------------------------
+def mix_substrates(W, m):
+    """The job mixes' substrates, resident for every job: the headline mesh, a
+    100-axon mesh, packed cylinders of 64 and 256."""
+    from dsim_gb300 import jobs as JB
+    return [JB.mesh_substrate(W.axons, 1, mesh=m, tube=W.tube), JB.mesh_substrate(100, 7),
+            JB.cyl_substrate(64, 1), JB.cyl_substrate(256, 2)]
+
+
 def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False, subs=None):
     from dsim_gb300 import jobs as JB
     t0 = time.time()
     if subs is None:
-        subs = [JB.mesh_substrate(W.axons, 1, mesh=m, tube=W.tube), JB.mesh_substrate(100, 7),
-                JB.cyl_substrate(64, 1), JB.cyl_substrate(256, 2)]
+        subs = mix_substrates(W, m)
     rng = np.random.default_rng(seed)
     mix = [JB.make_job(rng, subs, spins_range=spins_range, steps_range=steps_range, permeable=permeable,
                        seed=1000 + k) for k in range(n_jobs)]
@@ -739,41 +748,141 @@ def tune_mix(subs, mix):
     return best, ms
 
 
-def run_served_mix(subs, mix, cfg, rate, seed=3, form="bar"):
-    """Poisson arrivals at `rate` jobs/s into the request loop."""
+def serve_stream(subs, get_job, n_jobs, cfg, rate, form, spin_capacity, seed=3, ahead=0, keep=None):
+    """Poisson arrivals at `rate` jobs/s of jobs get_job(0..n_jobs-1) into the
+    request loop (150 GB HBM cap).  With `ahead` > 0, host threads generate the
+    jobs that many arrivals early and each job's arrays are dropped once it is
+    submitted (the server releases its copy on admission).  Returns the
+    summary and the signal sums of the jobs in `keep` (all if None)."""
+    from concurrent.futures import ThreadPoolExecutor
     from dsim_gb300.engine import Server
-    cap = max(sum((j["n"] + 31) // 32 * 32 for j in mix) // 2, max((j["n"] + 31) // 32 * 32 for j in mix))
-    srv = Server(spin_capacity=cap, job_capacity=len(mix), hbm_cap=150e9)
+    srv = Server(spin_capacity=spin_capacity, job_capacity=n_jobs, hbm_cap=150e9)
     sids = {id(sb): (srv.add_mesh(sb.handle) if sb.kind == "mesh" else srv.add_cyl(sb.handle)) for sb in subs}
     srv.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
+    pool = ThreadPoolExecutor(8) if ahead else None
+    futs = {}
+
+    def fetch(k):
+        if pool is None:
+            return get_job(k)
+        for a in range(k, min(n_jobs, k + ahead)):
+            if a not in futs:
+                futs[a] = pool.submit(get_job, a)
+        return futs.pop(k).result()
+
+    if pool is not None:
+        # the first window is generated before the clock starts
+        for a in range(min(n_jobs, ahead)):
+            futs[a] = pool.submit(get_job, a)
+        for a in range(min(n_jobs, ahead)):
+            futs[a].result()
     srv.start()
-    rng = np.random.default_rng(seed)
-    gaps = rng.exponential(1.0 / rate, len(mix))
+    gaps = np.random.default_rng(seed).exponential(1.0 / rate, n_jobs)
     t0 = time.perf_counter()
-    tickets = []
+    tickets, work, late = [], 0.0, 0
     t_next = t0
-    for j, gap in zip(mix, gaps):
-        t_next += gap
+    for k in range(n_jobs):
+        j = fetch(k)
+        t_next += gaps[k]
         d = t_next - time.perf_counter()
         if d > 0:
             time.sleep(d)
+        elif d < -0.05:
+            late += 1
         tickets.append(srv.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], j["grads"],
                                   **_submit_kw(j, form)))
+        work += j["n"] * j["steps"]
+        del j
     srv.drain()
     st = srv.stats()
     srv.stop()
-    lat, first, last, sigs = [], None, None, []
-    for t in tickets:
+    if pool is not None:
+        pool.shutdown()
+    lat, first, last, sigs = [], None, None, {}
+    for k, t in enumerate(tickets):
         done, sig, tm = srv.poll(t)
-        sigs.append(sig)
+        if keep is None or k in keep:
+            sigs[k] = sig
         lat.append(tm[2] - tm[0])
         first = tm[0] if first is None else min(first, tm[0])
         last = tm[2] if last is None else max(last, tm[2])
     srv.close()
-    work = sum(j["n"] * j["steps"] for j in mix)
     return {"rate_jobs_per_s": rate, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "spin_steps_per_s": work / (last - first), "max_jobs_in_flight": int(st["max_inflight"]),
-            "errors": int(st["errors"])}, sigs
+            "errors": int(st["errors"]), "hbm_peak_GB": st["hbm_peak"] / 1e9, "late_submissions": late,
+            "wall_s": last - first}, sigs
+
+
+def run_served_mix(subs, mix, cfg, rate, seed=3, form="bar"):
+    """Poisson arrivals at `rate` jobs/s of the jobs of `mix` into the request loop."""
+    cap = max(sum((j["n"] + 31) // 32 * 32 for j in mix) // 2, max((j["n"] + 31) // 32 * 32 for j in mix))
+    o, sigs = serve_stream(subs, mix.__getitem__, len(mix), cfg, rate, form, cap, seed=seed)
+    return o, [sigs[k] for k in range(len(mix))]
+
+
+def run_c4_full(args, W, m):
+    """The serving configuration at its full size: a Poisson stream of
+    --c4-jobs (2,000) jobs drawn from the batching mix's full ranges (spins
+    log-uniform 4k-1M, 2k-10k steps, dt 5-10 us, 6-128 directions x 3
+    b-values <= 3000 s/mm2) on the mixes' four resident substrates, permeable
+    membranes (per-hit permeation log-uniform 1e-4 - 1e-2), HBM admission cap
+    150 GB, at multiples of the plain form's capacity.  Job k comes from its own
+    generator seeded (--c4-seed, k), so the stream is fixed; the plain capacity
+    is measured on the stream's first --c4-plain-jobs jobs, one at a time, in
+    the same form; the signal error against FP64 walks on the same draws is
+    taken on --c4-err-jobs jobs spread over the stream."""
+    from dsim_gb300 import jobs as JB
+    t0 = time.time()
+    subs = mix_substrates(W, m)
+    n_jobs, seed, form = args.c4_jobs, args.c4_seed, args.c4_form
+    spins_range, steps_range = (4096, 1 << 20), (2000, 10000)
+
+    def job(k):
+        return JB.make_job(np.random.default_rng([seed, k]), subs, spins_range=spins_range, steps_range=steps_range,
+                           permeable=True, seed=100000 + k)
+
+    shapes = [JB.job_shape(np.random.default_rng([seed, k]), subs, spins_range, steps_range) for k in range(n_jobs)]
+    work = np.array([float(n) * st for _, n, st in shapes])
+    K = min(args.c4_plain_jobs, n_jobs)
+    sample = [job(k) for k in range(K)]
+    best, _ = tune_mix(subs, sample)
+    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+    per = (run_plain_bar_mix(subs, sample) if form == "bar" else run_plain_mix(sample))[0]
+    plain_rate = work[:K].sum() / sum(per)
+    cap_jobs = plain_rate / work.mean()
+    step = max(1, n_jobs // max(1, args.c4_err_jobs))
+    err_ids = list(range(step // 2, n_jobs, step))[:args.c4_err_jobs]
+    log("c4 full: %d jobs, %.3g spin-steps, plain %.3g spin-steps/s = %.3f jobs/s; setup %.0f s" % (
+        n_jobs, work.sum(), plain_rate, cap_jobs, time.time() - t0))
+    out = {"jobs": n_jobs, "seed": seed, "spins": list(spins_range), "steps": list(steps_range),
+           "spin_steps": float(work.sum()), "mesh_jobs": int(sum(sb.kind == "mesh" for sb, _, _ in shapes)),
+           "permeability": "log-uniform 1e-4 - 1e-2 per hit", "hbm_cap_GB": 150,
+           "form": ("mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
+                    if form == "bar" else "fp32: the plain FP32 step, Kahan moments"),
+           "plain": {"spin_steps_per_s": plain_rate, "jobs_per_s": cap_jobs, "sample_jobs": K,
+                     "note": "one job at a time, same form, on the stream's first jobs; jobs/s = spin-steps/s over "
+                             "the stream's mean job"},
+           "autotuned": best, "spin_capacity": args.c4_spin_capacity, "rates": []}
+    keep = set(err_ids)
+    sigs_by_rate = []
+    for r in args.c4_rates:
+        log("c4 full: rate %.2f x plain (%.3f jobs/s), about %.0f s of arrivals" % (r, r * cap_jobs,
+                                                                                    n_jobs / (r * cap_jobs)))
+        o, sigs = serve_stream(subs, job, n_jobs, cfg, r * cap_jobs, form, args.c4_spin_capacity, ahead=24,
+                               keep=keep)
+        o["rate_x_plain_capacity"] = r
+        o["speedup_vs_plain"] = o["spin_steps_per_s"] / plain_rate
+        out["rates"].append(o)
+        sigs_by_rate.append(sigs)
+        log("c4 full: %s" % o)
+    if err_ids and sigs_by_rate:
+        ejobs = [job(k) for k in err_ids]
+        ref, cyl_err = mix_fp64_reference(ejobs, ns_cyl=512)
+        for o, sigs in zip(out["rates"], sigs_by_rate):
+            o["err_vs_fp64"] = mix_err(ejobs, [sigs[k] for k in err_ids], ref, cyl_err)
+            o["err_vs_fp64"]["jobs"] = err_ids
+    out["seconds"] = time.time() - t0
+    return out
 
 
 def mix_fp64_reference(mix, ns_cyl=2048):
@@ -1300,6 +1409,16 @@ def main():
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
     ap.add_argument("--c5-full", action="store_true",
                     help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
+    ap.add_argument("--c4-full", action="store_true",
+                    help="also run the serving configuration at full size (--c4-jobs Poisson jobs of the full "
+                         "batching ranges, permeable, 150 GB cap, at --c4-rates x the plain capacity)")
+    ap.add_argument("--c4-jobs", type=int, default=2000)
+    ap.add_argument("--c4-rates", type=float, nargs="+", default=[0.5, 1.0, 1.5])
+    ap.add_argument("--c4-form", default="fp32", choices=["fp32", "bar"])
+    ap.add_argument("--c4-seed", type=int, default=13)
+    ap.add_argument("--c4-plain-jobs", type=int, default=24)
+    ap.add_argument("--c4-err-jobs", type=int, default=8)
+    ap.add_argument("--c4-spin-capacity", type=int, default=1 << 26)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -53,6 +53,12 @@ struct dsim_server {
     dsim_batch* b = nullptr;
     int device = 0;
     uint64_t spinCap = 0, hbmCap = 0, hbmSubs = 0, hbmJobs = 0, hbmPeak = 0;
+    // device bytes allocated on the first job of a precision form: a mesh's
+    // FP64 triangle table (128 B per triangle, per substrate) and the arena's
+    // four FP64 fields in both buffers (64 B per spin slot, once)
+    std::vector<uint64_t> tri64Bytes;
+    std::vector<bool> tri64Held;
+    bool fp64Arena = false;
     uint32_t jobCap = 0;
     uint32_t chunk = 20, graphChunks = 8;
     std::mutex mu;
@@ -82,14 +88,25 @@ void worker_loop(dsim_server* s) {
                 s->cv.wait_for(lk, std::chrono::milliseconds(2));
                 continue;
             }
-            uint64_t used = s->hbmJobs;
+            uint64_t used = s->hbmJobs, subs = s->hbmSubs;
+            std::vector<bool> held = s->tri64Held;
+            bool arena = s->fp64Arena;
             uint64_t slots = 0;
             for (uint32_t t : s->inflight) slots += (s->reqs[t]->d.nSpins + 31u) & ~31u;
             size_t jobs = s->inflight.size();
             for (auto it = s->pending.begin(); it != s->pending.end();) {
                 Request& r = *s->reqs[*it];
                 const uint64_t pad = (r.d.nSpins + 31u) & ~31u;
-                if (s->hbmSubs + used + r.footprint <= s->hbmCap && slots + pad <= s->spinCap && jobs < s->jobCap) {
+                uint64_t extra = 0;
+                const bool fp64 = (r.d.flags & (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL)) != 0;
+                if (fp64 && !arena) extra += s->spinCap * 64;
+                if (fp64 && !held[r.d.substrate]) extra += s->tri64Bytes[r.d.substrate];
+                if (subs + extra + used + r.footprint <= s->hbmCap && slots + pad <= s->spinCap && jobs < s->jobCap) {
+                    if (fp64) {
+                        arena = true;
+                        held[r.d.substrate] = true;
+                    }
+                    subs += extra;
                     used += r.footprint;
                     slots += pad;
                     jobs++;
@@ -99,6 +116,10 @@ void worker_loop(dsim_server* s) {
                     ++it;
                 }
             }
+            // the precision-form allocations stay for the server's life
+            s->hbmSubs = subs;
+            s->tri64Held = held;
+            s->fp64Arena = arena;
         }
         for (uint32_t t : toAdmit) {
             Request& r = *s->reqs[t];
@@ -114,6 +135,13 @@ void worker_loop(dsim_server* s) {
                 s->doneCv.notify_all();
                 continue;
             }
+            // the batch holds the job's state on the device now (dsim_batch_submit
+            // returns after its uploads): a long stream keeps no host copy of it
+            std::vector<float>().swap(r.pos);
+            std::vector<uint8_t>().swap(r.comp);
+            std::vector<uint32_t>().swap(r.fiber);
+            std::vector<float>().swap(r.table);
+            r.d.table = nullptr;
             r.admitted = true;
             r.tAdmit = s->now();
             s->hbmJobs += r.footprint;
@@ -206,10 +234,13 @@ int dsim_server_add_mesh(dsim_server* s, const dsim_mesh* m, uint32_t* sub) {
     if (!s || s->started) { set_last_error(kErrInvalid, "dsim_server_add_mesh: add substrates before start"); return kErrInvalid; }
     int rc = dsim_batch_add_mesh(s->b, m, sub);
     if (rc) return rc;
-    uint64_t info[8];
+    uint64_t info[8] = {0};
     if (dsim_mesh_info(m, info) == 0) s->hbmSubs += info[6];
     uint64_t acc[3];
     if (dsim_mesh_accel_info(m, acc) == 0) s->hbmSubs += acc[2];
+    s->tri64Bytes.resize(*sub + 1, 0);
+    s->tri64Held.resize(*sub + 1, false);
+    s->tri64Bytes[*sub] = 128ull * info[1];
     return kOk;
 }
 
@@ -221,6 +252,8 @@ int dsim_server_add_cyl(dsim_server* s, const dsim_cyl* c, uint32_t* sub) {
     float L;
     if (dsim_cyl_info(c, geom, &L, nullptr, nullptr, nullptr) == 0)
         s->hbmSubs += (uint64_t)geom[2] * 16 + (uint64_t)geom[0] * geom[0] * geom[0] * (4ull + 4ull * geom[1]);
+    s->tri64Bytes.resize(*sub + 1, 0);
+    s->tri64Held.resize(*sub + 1, false);
     return kOk;
 }
 
@@ -244,7 +277,7 @@ int dsim_server_start(dsim_server* s) {
 int dsim_server_submit(dsim_server* s, const dsim_job_desc* d, const float* pos3, const uint8_t* comp,
                        const uint32_t* fiber, const float* gradScaled, uint32_t nG, uint32_t* ticket) {
     if (!s || !d || !pos3 || !comp || !gradScaled || !nG || !ticket || !d->nSpins || !d->steps ||
-        (d->waveform == DSIM_WAVE_TABLE && !d->table)) {
+        (d->waveform == DSIM_WAVE_TABLE && !d->table) || d->substrate >= s->tri64Bytes.size()) {
         set_last_error(kErrInvalid, "dsim_server_submit: bad argument");
         return kErrInvalid;
     }

@@ -61,15 +61,37 @@ def cyl_substrate(n, seed):
 
 def tube_compartments(tube, pos, spaceScale):
     """Compartment 3 (inside a glia-type tube) or 0, with the tube index."""
-    um = pos.astype(np.float64) * spaceScale
-    comp = np.zeros(len(pos), np.uint8)
-    fib = np.full(len(pos), 0xFFFF, np.uint32)
+    um = np.asarray(pos, np.float32).reshape(-1, 3).astype(np.float64) * spaceScale
+    n = len(um)
+    comp = np.zeros(n, np.uint8)
+    fib = np.full(n, 0xFFFF, np.uint32)
+    if n == 0:
+        return comp, fib
+    # Spins binned on a 2 um xy grid; each tube tests only the spins of the
+    # cells under its widest cross-section (radius <= 1.2 r0, one cell of
+    # margin), with the same expressions, so lower tube indices still win.
+    cs = 2.0
+    lo = um[:, :2].min(0)
+    ix = np.floor((um[:, 0] - lo[0]) / cs).astype(np.int64)
+    iy = np.floor((um[:, 1] - lo[1]) / cs).astype(np.int64)
+    nx, ny = int(ix.max()) + 1, int(iy.max()) + 1
+    order = np.argsort(ix * ny + iy, kind="stable")
+    starts = np.searchsorted((ix * ny + iy)[order], np.arange(nx * ny + 1))
     for i, ((cx, cy), r0) in enumerate(zip(tube["centres"], tube["radii"])):
-        rz = r0 * (1 + 0.2 * np.sin(2 * np.pi * um[:, 2] / 10.0))
-        sel = (np.abs(um[:, 0] - cx) < rz) & (np.abs(um[:, 1] - cy) < rz) & (comp == 0)
-        sel &= np.hypot(um[:, 0] - cx, um[:, 1] - cy) < rz * np.cos(np.pi / 32)
-        comp[sel] = 3
-        fib[sel] = i
+        rmax = 1.2 * r0
+        x0 = max(int(np.floor((cx - rmax - lo[0]) / cs)) - 1, 0)
+        x1 = min(int(np.floor((cx + rmax - lo[0]) / cs)) + 1, nx - 1)
+        y0 = max(int(np.floor((cy - rmax - lo[1]) / cs)) - 1, 0)
+        y1 = min(int(np.floor((cy + rmax - lo[1]) / cs)) + 1, ny - 1)
+        if x0 > x1 or y0 > y1:
+            continue
+        idx = np.concatenate([order[starts[a * ny + y0]:starts[a * ny + y1 + 1]] for a in range(x0, x1 + 1)])
+        u = um[idx]
+        rz = r0 * (1 + 0.2 * np.sin(2 * np.pi * u[:, 2] / 10.0))
+        sel = (np.abs(u[:, 0] - cx) < rz) & (np.abs(u[:, 1] - cy) < rz) & (comp[idx] == 0)
+        sel &= np.hypot(u[:, 0] - cx, u[:, 1] - cy) < rz * np.cos(np.pi / 32)
+        comp[idx[sel]] = 3
+        fib[idx[sel]] = i
     return comp, fib
 
 
@@ -89,13 +111,20 @@ def cyl_regions(geom, pos, spaceScale, inner=0.7):
     return imo, nearest
 
 
+def job_shape(rng, subs, spins_range=(4096, 1 << 20), steps_range=(2000, 10000)):
+    """The first draws of make_job: substrate, spin count (log-uniform), steps
+    (uniform).  A stream can size its jobs from these without generating them."""
+    sub = subs[int(rng.integers(len(subs)))]
+    n = int(round(math.exp(rng.uniform(math.log(spins_range[0]), math.log(spins_range[1])))))
+    steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+    return sub, n, steps
+
+
 def make_job(rng, subs, spins_range=(4096, 1 << 20), steps_range=(2000, 10000), dirs_range=(6, 128),
              bmax=3.0, permeable=False, seed=0):
     """One job of the batching mix: substrate, spins log-uniform, steps uniform,
     dt 5-10 us, PGSE filling the walk, directions x b-values with b <= bmax."""
-    sub = subs[int(rng.integers(len(subs)))]
-    n = int(round(math.exp(rng.uniform(math.log(spins_range[0]), math.log(spins_range[1])))))
-    steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+    sub, n, steps = job_shape(rng, subs, spins_range, steps_range)
     dt = float(rng.uniform(0.005, 0.010))
     T = steps * dt
     delta, Delta = 0.3 * T, 0.6 * T

@@ -26,7 +26,10 @@ extern "C" {
 typedef struct dsim_server dsim_server;
 
 /* spinCapacity / jobCapacity: the batch arena; hbmCapBytes: admission cap on
- * substrates + admitted jobs' footprint */
+ * substrates + admitted jobs' footprint, counting, from the first job of a
+ * precision form (DSIM_JOB_PRECISE / DSIM_JOB_LOCAL) on, the arena's FP64
+ * fields (64 B per spin slot) and each such job's mesh FP64 triangle table
+ * (128 B per triangle).  A job's host arrays are released once it is admitted. */
 int dsim_server_create(uint64_t spinCapacity, uint32_t jobCapacity, uint64_t hbmCapBytes,
                        dsim_server** out);
 void dsim_server_free(dsim_server* s);

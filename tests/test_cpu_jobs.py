@@ -69,3 +69,49 @@ def test_fibonacci_directions_are_unit_and_spread():
         # no two directions coincide
         c = d @ d.T - np.eye(n) * 2
         assert c.max() < 0.999
+
+
+def _tube_compartments_every_tube(tube, pos, spaceScale):
+    """Every spin against every tube in index order (the first tube holding a
+    spin wins): the definition the binned tube_compartments must equal."""
+    um = pos.astype(np.float64) * spaceScale
+    comp = np.zeros(len(pos), np.uint8)
+    fib = np.full(len(pos), 0xFFFF, np.uint32)
+    for i, ((cx, cy), r0) in enumerate(zip(tube["centres"], tube["radii"])):
+        rz = r0 * (1 + 0.2 * np.sin(2 * np.pi * um[:, 2] / 10.0))
+        sel = (np.abs(um[:, 0] - cx) < rz) & (np.abs(um[:, 1] - cy) < rz) & (comp == 0)
+        sel &= np.hypot(um[:, 0] - cx, um[:, 1] - cy) < rz * np.cos(np.pi / 32)
+        comp[sel] = 3
+        fib[sel] = i
+    return comp, fib
+
+
+def test_binned_tube_compartments_equal_every_tube_scan():
+    tube = S.beaded_tubes(n_axons=60, verts_per_ring=12, ring_spacing=1.0, length=50.0, box=50.0, seed=5,
+                          allow_overlap=True)
+    rng = np.random.default_rng(11)
+    pos = rng.uniform(-0.99, 0.99, (60000, 3)).astype(np.float32)
+    # spins on tube surfaces and axes too
+    c = np.asarray(tube["centres"], np.float64)[:, None, :]
+    r = np.asarray(tube["radii"], np.float64)[:, None]
+    a = rng.uniform(0, 2 * np.pi, (len(c), 50))
+    z = rng.uniform(-24.0, 24.0, (len(c), 50))
+    rz = r * (1 + 0.2 * np.sin(2 * np.pi * z / 10.0))
+    for k in (0.0, 0.5, np.cos(np.pi / 32), 1.0, 1.2):
+        p = np.stack([c[..., 0] + k * rz * np.cos(a), c[..., 1] + k * rz * np.sin(a), z], -1).reshape(-1, 3)
+        pos = np.concatenate([pos, (p / 25.0).astype(np.float32)])
+    got = JB.tube_compartments(tube, pos, 25.0)
+    want = _tube_compartments_every_tube(tube, pos, 25.0)
+    assert (want[0] == 3).sum() > 1000
+    assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    e = JB.tube_compartments(tube, np.zeros((0, 3), np.float32), 25.0)
+    assert len(e[0]) == 0 and len(e[1]) == 0
+
+
+def test_job_shape_is_make_jobs_first_draws():
+    subs = _subs()
+    for k in range(20):
+        sub, n, steps = JB.job_shape(np.random.default_rng([9, k]), subs, (4096, 1 << 20), (2000, 10000))
+        j = JB.make_job(np.random.default_rng([9, k]), subs, spins_range=(4096, 1 << 20), steps_range=(2000, 10000),
+                        permeable=True, seed=k)
+        assert j["sub"] is sub and j["n"] == n and j["steps"] == steps
