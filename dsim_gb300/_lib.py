@@ -138,7 +138,8 @@ class Config(C.Structure):
                 ("myelinT2", C.c_float), ("spaceScale", C.c_float), ("startBox", C.c_float),
                 ("permeability", C.c_float), ("innerRadiusFraction", C.c_float),
                 ("gradsFile", C.c_char * 512), ("gradsStr", C.c_char * 512), ("outFile", C.c_char * 512),
-                ("fiberFile", C.c_char * 512)]
+                ("fiberFile", C.c_char * 512), ("fiberRadius", C.c_float), ("fiberSpace", C.c_float),
+                ("crossFraction", C.c_float)]
 
 
 class JobDesc(C.Structure):

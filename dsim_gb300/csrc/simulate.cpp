@@ -382,7 +382,7 @@ int dsim_config_load(const char* path, dsim_config* out) {
     const bool d2 = has("sim.timestep") || has("fibers.file") || has("sim.gyromagneticRatio");
     out->dialect = d2 ? 2 : 3;
     out->stepsPerUpdate = u("app.stepsPerUpdate", 10);
-    out->useGpu = b("app.useGpu", 0);
+    out->useGpu = b("app.useGpu", 1);   // both reference mains default to the GPU
     out->useDisplay = b("app.useDisplay", 0);
     out->writeOut = b("app.writeOut", 1);
     out->numSpins = u("sim.numSpins", 1000);
@@ -397,6 +397,9 @@ int dsim_config_load(const char* path, dsim_config* out) {
     out->spaceScale = f("sim.spaceScale", d2 ? 20.0f : 60.0f);
     out->startBox = f("sim.startBox", 1.0f);
     out->innerRadiusFraction = f("fibers.innerRadiusFraction", 0.7f);
+    out->fiberRadius = f("fibers.radiusMean", 1.0f);
+    out->fiberSpace = f("fibers.spacingMean", 0.2f);
+    out->crossFraction = f("fibers.crossFraction", 0.0f);
     if (d2) out->permeability = (float)pow(10.0, (double)f("sim.permeability", -4.0f));
     else out->permeability = f("sim.permeability", 0.0f);
     set_str(out->gradsFile, str("sim.gradsFile"));
@@ -515,12 +518,13 @@ int dsim_write_results(const char* outFile, const dsim_config* cfgp, const float
     const dsim_config& cfg = *cfgp;
     const std::vector<float> rows(rowsp, rowsp + 6 * (size_t)nG);
     const float dt = cfg.timeStep;
-    // the reference keeps every signal in its float results table
-    // (gradientDataResults, dSim3/src/diffusion.cpp:575-577) before it fits
-    // and prints them
+    // dSim3 keeps every signal in its float results table (gradientDataResults,
+    // dSim3/src/diffusion.cpp:575-577), zeroed for the rows it never reads,
+    // before it fits and prints them
     std::vector<double> sig32(5 * (size_t)nG);
-    for (size_t k = 0; k < sig32.size(); k++) sig32[k] = (double)(float)signals[k];
-    signals = sig32.data();
+    for (size_t k = 0; k < sig32.size(); k++) sig32[k] = std::isnan(signals[k]) ? 0.0 : (double)(float)signals[k];
+    const double* signals64 = signals;
+    if (cfg.dialect == 3) signals = sig32.data();
     FILE* f = fopen(outFile, "at");
     if (!f) { set_last_error(kErrFile, "cannot open %s", outFile); return kErrFile; }
     time_t now = time(nullptr);
@@ -531,7 +535,7 @@ int dsim_write_results(const char* outFile, const dsim_config* cfgp, const float
         fprintf(f, "s=0;\n");
         fprintf(f, "\n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%% \n%% Input parameters \n%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%%\n");
         fprintf(f, "numSpins(m) = %u;\n", cfg.numSpins);
-        fprintf(f, "useGpu(m) = %d;\n", 1);
+        fprintf(f, "useGpu(m) = %d;\n", cfg.useGpu);
         fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
         fprintf(f, "useDisplay(m) = %d;\n", 0);
         fprintf(f, "stepsPerUpdate(m) = %i;\n", (int)cfg.stepsPerUpdate);
@@ -581,22 +585,25 @@ int dsim_write_results(const char* outFile, const dsim_config* cfgp, const float
         fprintf(f, "\n%% * * * %s", ctime(&now));
         fprintf(f, "if(exist('m','var')), m=m+1; else, m=1; end\n");
         fprintf(f, "s=0;\n");
+        fprintf(f, "radiusMean(m) = %g;\n", cfg.fiberRadius);
+        fprintf(f, "radiusSpace(m) = %g;\n", cfg.fiberSpace);
         fprintf(f, "spaceScale(m) = %g;\n", cfg.spaceScale);
         fprintf(f, "numSpins(m) = %d;\n", (int)cfg.numSpins);
-        fprintf(f, "useGpu(m) = %d;\n", 1);
+        fprintf(f, "crossFraction(m) = %g;\n", cfg.crossFraction);
+        fprintf(f, "useGpu(m) = %d;\n", cfg.useGpu);
         fprintf(f, "fibersFile{m} = '%s';\n", cfg.fiberFile);
         double totalSteps = 0.0;
         for (uint32_t g = 0; g < nG; g++) {
             const float* r = &rows[6 * g];
             uint32_t steps = 0;
-            dsim_pgse_schedule(r, dt, cfg.stepsPerUpdate, nullptr, 0, &steps);
+            const bool read = dsim_pgse_schedule(r, dt, cfg.stepsPerUpdate, nullptr, 0, &steps) == kOk;
             totalSteps += steps;
             fprintf(f, "s = s+1;\n");
             fprintf(f, "delta{m}(s) = %g;\n", r[0]);
             fprintf(f, "Delta{m}(s) = %g;\n", r[1]);
             fprintf(f, "readOut{m}(s) = %g;\n", r[2]);
             fprintf(f, "dwGrads{m}(:,s) = [%g;%g;%g];\n", r[3], r[4], r[5]);
-            fprintf(f, "mrSig{m}(s) = %g;\n", signals[5 * (size_t)g]);
+            if (read) fprintf(f, "mrSig{m}(s) = %g;\n", signals64[5 * (size_t)g]);
         }
         fprintf(f, "%% Timing info:\n");
         fprintf(f, "stepsPerSec(m) = %g;\n", elapsed > 0 ? totalSteps / elapsed : 0.0);

@@ -34,6 +34,9 @@ typedef struct {
     float permeability;        /* probability per hit (dSim2's log10 value converted) */
     float innerRadiusFraction; /* dSim2 fibers.innerRadiusFraction */
     char gradsFile[512], gradsStr[512], outFile[512], fiberFile[512];
+    /* dSim2 fibers.radiusMean, fibers.spacingMean, fibers.crossFraction (its
+     * fiber generator's parameters, written in its results header) */
+    float fiberRadius, fiberSpace, crossFraction;
 } dsim_config;
 
 /* libconfig subset (groups, scalars, strings, booleans, comments); relative
@@ -67,8 +70,11 @@ int dsim_tensor_fit(const float* rows, const double* signal, uint32_t nG, double
  * reference's indexing), then every row with its signals.  dSim2 dialect
  * (dSim2/src/diffusion.cpp:1756-1770, 232-276): the header, one block per row
  * and the stepsPerSec / totalTime timing from `seconds`.  rows [nG][6],
- * signals [nG][5] as dsim_simulate returns them; like the reference, the
- * signals are rounded to float before they are fitted and printed. */
+ * signals [nG][5] as dsim_simulate returns them.  dSim3: like the reference,
+ * the signals are rounded to float before they are fitted and printed, and a
+ * row whose signal the sequencer never reads (NaN from dsim_simulate) holds 0,
+ * as in the reference's zeroed results table.  dSim2: the total signal is
+ * printed as the double it is, and a row never read gets no signal line. */
 int dsim_write_results(const char* outFile, const dsim_config* cfg, const float* rows, const double* signals,
                        uint32_t nG, double seconds);
 

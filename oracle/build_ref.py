@@ -27,7 +27,10 @@ scratch copy in oracle/_ref/src{2,3}/:
     computeTensor() and update() (oracle/_ref/src3/diffusion_parts.inc, with
     the vendored JAMA/TNT headers copied beside it).  The sequencer harness
     (refharness/seq3.cpp) defines the globals they use and stands in for the
-    SpinSystem they drive.
+    SpinSystem they drive;
+  * from dSim2/src/diffusion.cpp, likewise, the gradStruct type, update() and
+    the results-file header statements of its main() (oracle/_ref/src2/
+    diffusion2_*.inc), driven by refharness/seq2.cpp.
 The host side of the C-ABI (allocateArray -> malloc, copy* -> memcpy) and the
 cutil timer macros are provided by oracle/refharness/.
 
@@ -135,6 +138,27 @@ def diffusion_parts(reference):
     return "/* taken unchanged from dSim3/src/diffusion.cpp by oracle/build_ref.py */\n" + "\n".join(parts)
 
 
+def _lines_between(text, first, last):
+    """The lines from the one containing `first` through the one containing
+    `last`, unchanged."""
+    i = text.index(first)
+    i = text.rindex("\n", 0, i) + 1
+    j = text.index(last, i)
+    return text[i:text.index("\n", j) + 1]
+
+
+def dsim2_parts(reference):
+    """The gradStruct type and update() of dSim2/src/diffusion.cpp, verbatim,
+    and the results-file header that its main() writes (the statements from
+    the fopen of the results file through the fibers line)."""
+    with open(os.path.join(reference, "dSim2", "src", "diffusion.cpp")) as fh:
+        text = fh.read()
+    note = "/* taken unchanged from dSim2/src/diffusion.cpp by oracle/build_ref.py */\n"
+    header = _lines_between(text, 'outFilePtr = fopen(outFilename,"at");',
+                            """fprintf(outFilePtr,"fibersFile{m} = '%s';\\n", fiberFileConst);""")
+    return (note + _cut(text, "typedef struct _gradStruct"), note + _cut(text, "void update(){"), note + header)
+
+
 def build(reference):
     os.makedirs(OUT, exist_ok=True)
     for sub in ("jama", "tnt"):
@@ -145,6 +169,11 @@ def build(reference):
     os.makedirs(os.path.join(OUT, "src3"), exist_ok=True)
     with open(os.path.join(OUT, "src3", "diffusion_parts.inc"), "w") as fh:
         fh.write(diffusion_parts(reference))
+    os.makedirs(os.path.join(OUT, "src2"), exist_ok=True)
+    for name, part in zip(("diffusion2_types.inc", "diffusion2_update.inc", "diffusion2_header.inc"),
+                          dsim2_parts(reference)):
+        with open(os.path.join(OUT, "src2", name), "w") as fh:
+            fh.write(part)
     for tree, files, patch in (("dSim3", DSIM3_FILES, patch_dsim3),
                                ("dSim2", DSIM2_FILES, patch_dsim2)):
         dst = os.path.join(OUT, "src" + tree[-1])
@@ -168,6 +197,7 @@ def build(reference):
                   "-o", os.path.join(OUT, "harness2")],
         common + ["-I", os.path.join(OUT, "src3"), "-I", os.path.join(OUT, "jama"), "-I", os.path.join(OUT, "tnt"),
                   os.path.join(HARNESS, "seq3.cpp"), "-o", os.path.join(OUT, "seq3")],
+        common + ["-I", os.path.join(OUT, "src2"), os.path.join(HARNESS, "seq2.cpp"), "-o", os.path.join(OUT, "seq2")],
     ]
     procs = [subprocess.Popen(j) for j in jobs]
     rc = [p.wait() for p in procs]
@@ -176,9 +206,10 @@ def build(reference):
     return [os.path.join(OUT, "harness3"), os.path.join(OUT, "harness2")]
 
 
-def sequencer_harness():
-    """The sequencer harness that build() compiles (refharness/seq3.cpp)."""
-    return os.path.join(OUT, "seq3")
+def sequencer_harness(dialect=3):
+    """The sequencer harness that build() compiles (refharness/seq3.cpp, or
+    refharness/seq2.cpp for dSim2)."""
+    return os.path.join(OUT, "seq3" if dialect == 3 else "seq2")
 
 
 def build_dropin(libdir):

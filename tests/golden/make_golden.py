@@ -18,7 +18,13 @@ reference's final seeds), and the reference's state and signal after the
 steps.  Also extracts the hand collision case of the reference's MATLAB test
 dSim3/matlab_tests/run_tests/collisions01.m into matlab_collisions.json.
 
+The sequencer fixtures hold the reference's own update(), computeTensor() and
+results writer run on gradient tables: seq_*.npz from dSim3/src/diffusion.cpp
+(refharness/seq3.cpp), seq2_*.npz from dSim2/src/diffusion.cpp
+(refharness/seq2.cpp).
+
 Run here (needs the reference tree):  python3 tests/golden/make_golden.py
+[--only seq2]  (--only regenerates one group of fixtures)
 """
 import json
 import os
@@ -196,16 +202,65 @@ def seq_fixtures(tmp):
     seq_fixture("seq_rank6", rows, 0.01, 5, seq, tmp)
 
 
+SEQ2_CONFIG = dict(numSpins=999, spaceScale=50.0, radiusMean=1.5, spacingMean=0.3, crossFraction=0.1, useGpu=1,
+                   fiberFile="sim.fibers")
+
+
+def seq2_fixture(name, rows, timestep, iterations, seq, tmp):
+    """The reference's dSim2 update() and results writer on a gradient table
+    (refharness/seq2.cpp): every update call with its gradient, the resets and
+    reads, and the results file (header, one block per run, timing)."""
+    rows = np.asarray(rows, np.float32).reshape(-1, 6)
+    sig = _tensor_signals(rows)[:, 0]
+    runs = O.sequencer_runs(rows, timestep, iterations)
+    read = [k for k in range(len(rows)) if runs[k] is not None]
+    g = os.path.join(tmp, name + ".g")
+    sg = os.path.join(tmp, name + ".s")
+    rows.tofile(g)
+    np.ascontiguousarray(sig[read], np.float64).tofile(sg)   # returned in read order
+    outm = os.path.join(tmp, name + ".m")
+    r = run(seq, grads=g, signals=sg, timestep=timestep, iterations=iterations, outm=outm,
+            out=os.path.join(tmp, name + ".bin"), **SEQ2_CONFIG)
+    with open(outm, "rb") as fh:
+        mtext = fh.read()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), rows=rows, signals=sig, timeStep=np.float32(timestep),
+                        stepsPerUpdate=np.uint32(iterations), config=json.dumps(SEQ2_CONFIG), calls=r["calls"],
+                        events=r["events"], mfile=np.frombuffer(mtext, np.uint8))
+    return r
+
+
+def seq2_fixtures(tmp):
+    from dsim_gb300.engine import parse_grads
+    from dsim_gb300.jobs import fibonacci_dirs, pgse_gmag
+    seq = build_ref.sequencer_harness(2)
+    # the reference's own dSim2 gradient table
+    seq2_fixture("seq2_simgrads", parse_grads(path=os.path.join(REFERENCE, "dSim2", "sim.grads")), 0.005, 10, seq,
+                 tmp)
+    # Fibonacci directions, a b = 0 row, and a row whose readout rounds to
+    # zero updates (its signal is never read)
+    rows = [[6.0, 15.0, 1.5, 0.0, 0.0, 0.0]] + [[6.0, 15.0, 1.5, *(pgse_gmag(1.0, 6.0, 15.0) * d)]
+                                               for d in fibonacci_dirs(9)]
+    rows.insert(4, [6.0, 15.0, 0.001, *(pgse_gmag(0.5, 6.0, 15.0) * fibonacci_dirs(9)[2])])
+    seq2_fixture("seq2_fib", rows, 0.01, 3, seq, tmp)
+
+
 def main():
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", choices=["seq2"], default=None)
+    args = ap.parse_args()
     if REFERENCE is None:
         raise SystemExit("the reference tree is not present (set DSIM_REFERENCE)")
     h3, h2 = build_ref.build(REFERENCE)
     with tempfile.TemporaryDirectory() as tmp:
-        mesh_fixture("mesh_am", "AM", 0.05, 11, h3, tmp)
-        mesh_fixture("mesh_g", "G", 0.2, 12, h3, tmp)
-        cyl_fixture("cyl", h2, tmp)
-        seq_fixtures(tmp)
-    matlab_collision_case()
+        if args.only is None:
+            mesh_fixture("mesh_am", "AM", 0.05, 11, h3, tmp)
+            mesh_fixture("mesh_g", "G", 0.2, 12, h3, tmp)
+            cyl_fixture("cyl", h2, tmp)
+            seq_fixtures(tmp)
+        seq2_fixtures(tmp)
+    if args.only is None:
+        matlab_collision_case()
     print("fixtures written to", HERE)
 
 

@@ -15,6 +15,11 @@ wrote them.
   JAMA eigen-decomposition) within 1e-4;
 * dsim_write_results writes the reference's results file: every line equal,
   the fitted numbers within 1e-4 (eigenvector columns up to sign).
+
+The same for dSim2 (dSim2/src/diffusion.cpp:183-287 and its results header
+1756-1770, run unchanged by oracle/refharness/seq2.cpp; fixtures
+tests/golden/seq2_*.npz): the schedule of every run, and the results file line
+for line (date and timing values aside).
 """
 import json
 import os
@@ -118,3 +123,55 @@ def test_results_file_equals_the_reference_writer(name, tmp_path):
             assert np.allclose(x, y, rtol=1e-4, atol=2e-6), (a, b)
         else:
             assert a == b, (a, b)
+
+
+# ---- dSim2: update() and the results file of dSim2/src/diffusion.cpp -------
+# (oracle/refharness/seq2.cpp: the reference's update() and results header,
+# unchanged, on the gradient tables of tests/golden/seq2_*.npz: dSim2's own
+# sim.grads, and Fibonacci directions with a row whose readout rounds to zero
+# updates)
+FIXTURES2 = ["seq2_simgrads", "seq2_fib"]
+
+
+@pytest.mark.parametrize("name", FIXTURES2)
+def test_dsim2_schedule_equals_the_reference_update(name):
+    from dsim_gb300.engine import pgse_schedule
+    g = _load(name)
+    dt, its = float(g["timeStep"]), int(g["stepsPerUpdate"])
+    walks = _walks(g)
+    assert len(walks) < len(g["rows"]) or name == "seq2_simgrads"
+    for k, row in enumerate(g["rows"]):
+        if k not in walks:
+            with pytest.raises(Exception):
+                pgse_schedule(row, dt, its)
+            continue
+        w = walks[k]
+        assert np.all(w[:, 6] == its) and np.all(w[:, 5] == np.float32(dt))
+        got = pgse_schedule(row, dt, its)
+        assert np.array_equal(got, np.repeat(w[:, 2:5], its, axis=0)), k
+
+
+@pytest.mark.parametrize("name", FIXTURES2)
+def test_dsim2_results_file_equals_the_reference_writer(name, tmp_path):
+    from dsim_gb300.engine import write_results
+    g = _load(name)
+    c = json.loads(str(g["config"]))
+    cfg = dict(dialect=2, stepsPerUpdate=int(g["stepsPerUpdate"]), timeStep=float(g["timeStep"]),
+               numSpins=c["numSpins"], spaceScale=c["spaceScale"], fiberRadius=c["radiusMean"],
+               fiberSpace=c["spacingMean"], crossFraction=c["crossFraction"], useGpu=c["useGpu"],
+               fiberFile=c["fiberFile"])
+    sig = np.zeros((len(g["rows"]), 5))
+    sig[:, 0] = g["signals"]
+    sig[[k for k in range(len(sig)) if k not in _walks(g)], 0] = np.nan   # as dsim_simulate reports them
+    out = tmp_path / "results.m"
+    write_results(out, cfg, g["rows"], sig, seconds=1.0)
+    ours = out.read_text().split("\n")
+    ref = g["mfile"].tobytes().decode().split("\n")
+    assert len(ours) == len(ref), (len(ours), len(ref))
+    for a, b in zip(ours, ref):
+        if a.startswith("% * * *") and b.startswith("% * * *"):
+            continue                                   # the date of the run
+        if a.startswith(("stepsPerSec(m)", "totalTime(m)")):
+            assert a.split("=")[0] == b.split("=")[0]  # the run's timing
+            continue
+        assert a == b, (a, b)
