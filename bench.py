@@ -827,10 +827,13 @@ def run_c4_full(args, W, m):
     b-values <= 3000 s/mm2) on the mixes' four resident substrates, permeable
     membranes (per-hit permeation log-uniform 1e-4 - 1e-2), HBM admission cap
     150 GB, at multiples of the plain form's capacity.  Job k comes from its own
-    generator seeded (--c4-seed, k), so the stream is fixed; the plain capacity
-    is measured on the stream's first --c4-plain-jobs jobs, one at a time, in
-    the same form; the signal error against FP64 walks on the same draws is
-    taken on --c4-err-jobs jobs spread over the stream."""
+    generator seeded (--c4-seed, k), so the stream is fixed.  The plain form
+    runs the stream's first --c4-plain-jobs jobs one at a time, in the same
+    form; its capacity for the whole stream is the stream's work on each
+    substrate over that substrate's plain rate (spin-steps/s of the sample's
+    jobs on it), summed, so a sample that holds more of one substrate's work
+    than the stream does not bias it.  The signal error against FP64 walks on
+    the same draws is taken on --c4-err-jobs jobs spread over the stream."""
     from dsim_gb300 import jobs as JB
     t0 = time.time()
     subs = mix_substrates(W, m)
@@ -844,12 +847,19 @@ def run_c4_full(args, W, m):
     shapes = [JB.job_shape(np.random.default_rng([seed, k]), subs, spins_range, steps_range) for k in range(n_jobs)]
     work = np.array([float(n) * st for _, n, st in shapes])
     K = min(args.c4_plain_jobs, n_jobs)
+    while K < n_jobs and len({id(sb) for sb, _, _ in shapes[:K]}) < len({id(sb) for sb, _, _ in shapes}):
+        K += 1                                   # every substrate of the stream in the sample
     sample = [job(k) for k in range(K)]
     best, _ = tune_mix(subs, sample)
     cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
     per = (run_plain_bar_mix(subs, sample) if form == "bar" else run_plain_mix(sample))[0]
-    plain_rate = work[:K].sum() / sum(per)
-    cap_jobs = plain_rate / work.mean()
+    sub_rate = {}
+    for sb in {id(sb): sb for sb, _, _ in shapes[:K]}.values():
+        ks = [k for k in range(K) if shapes[k][0] is sb]
+        sub_rate[id(sb)] = sum(work[k] for k in ks) / sum(per[k] for k in ks)
+    plain_s = sum(work[k] / sub_rate[id(shapes[k][0])] for k in range(n_jobs))
+    plain_rate = work.sum() / plain_s
+    cap_jobs = n_jobs / plain_s
     step = max(1, n_jobs // max(1, args.c4_err_jobs))
     err_ids = list(range(step // 2, n_jobs, step))[:args.c4_err_jobs]
     log("c4 full: %d jobs, %.3g spin-steps, plain %.3g spin-steps/s = %.3f jobs/s; setup %.0f s" % (
@@ -860,8 +870,10 @@ def run_c4_full(args, W, m):
            "form": ("mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
                     if form == "bar" else "fp32: the plain FP32 step, Kahan moments"),
            "plain": {"spin_steps_per_s": plain_rate, "jobs_per_s": cap_jobs, "sample_jobs": K,
-                     "note": "one job at a time, same form, on the stream's first jobs; jobs/s = spin-steps/s over "
-                             "the stream's mean job"},
+                     "sample_spin_steps_per_s": float(work[:K].sum() / sum(per)),
+                     "per_substrate_spin_steps_per_s": [sub_rate.get(id(sb)) for sb in subs],
+                     "note": "one job at a time, same form, on the stream's first jobs; the stream's plain time is "
+                             "its work on each substrate over that substrate's sample rate"},
            "autotuned": best, "spin_capacity": args.c4_spin_capacity, "rates": []}
     keep = set(err_ids)
     sigs_by_rate = []
@@ -1416,9 +1428,10 @@ def main():
     ap.add_argument("--c4-rates", type=float, nargs="+", default=[0.5, 1.0, 1.5])
     ap.add_argument("--c4-form", default="fp32", choices=["fp32", "bar"])
     ap.add_argument("--c4-seed", type=int, default=13)
-    ap.add_argument("--c4-plain-jobs", type=int, default=24)
+    ap.add_argument("--c4-plain-jobs", type=int, default=48)
     ap.add_argument("--c4-err-jobs", type=int, default=8)
-    ap.add_argument("--c4-spin-capacity", type=int, default=1 << 26)
+    ap.add_argument("--c4-spin-capacity", type=int, default=1 << 22,
+                    help="server spin slots: enough to fill the GPU; more slots slow every admitted job")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

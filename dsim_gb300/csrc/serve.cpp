@@ -4,9 +4,12 @@
 // One worker thread owns the batch.  Each loop: admit pending jobs in arrival
 // order while spin slots, job slots and the HBM cap allow (a job that does not
 // fit yet waits; smaller jobs behind it may pass), advance every admitted job
-// by one quantum, then read the signals of the jobs that finished, retire
-// them and repack the batch so their slots go to the next arrivals.
+// by one quantum (whole chunks, about kQuantumSeconds of device time), then
+// read the signals of the jobs that finished, retire them and repack the
+// batch so their slots go to the next arrivals.
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -25,6 +28,7 @@
 namespace {
 
 using Clock = std::chrono::steady_clock;
+constexpr double kQuantumSeconds = 0.2;  // device time between admissions
 
 struct Request {
     dsim_job_desc d{};
@@ -69,7 +73,7 @@ struct dsim_server {
     std::thread worker;
     bool started = false, stopping = false;
     Clock::time_point t0;
-    double busy = 0, spinSteps = 0;
+    double busy = 0, spinSteps = 0, secPerStep = 0;
     uint64_t jobsDone = 0, maxInflight = 0, quanta = 0, compactions = 0, errors = 0;
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
 };
@@ -150,11 +154,21 @@ void worker_loop(dsim_server* s) {
             if (s->inflight.size() > s->maxInflight) s->maxInflight = s->inflight.size();
         }
         if (s->inflight.empty()) continue;
-        // one quantum for every admitted job
+        // one quantum for every admitted job: whole chunks, about
+        // kQuantumSeconds at the last quantum's rate (at most chunk x
+        // graphChunks steps), so arrivals wait about that long for admission
+        const uint32_t maxSteps = s->chunk * (s->graphChunks ? s->graphChunks : 1);
+        uint32_t steps = maxSteps;
+        if (s->secPerStep > 0.0) {
+            const double whole = std::floor(kQuantumSeconds / s->secPerStep / s->chunk) * s->chunk;
+            steps = (uint32_t)std::min<double>(maxSteps, std::max<double>(s->chunk, whole));
+        }
         const double ta = s->now();
-        int rc = dsim_batch_advance(s->b, s->chunk * (s->graphChunks ? s->graphChunks : 1));
+        int rc = dsim_batch_advance(s->b, steps);
         if (!rc) rc = dsim_batch_sync(s->b);
-        s->busy += s->now() - ta;
+        const double el = s->now() - ta;
+        s->busy += el;
+        s->secPerStep = el / steps;
         s->quanta++;
         if (rc) {
             // the device is unusable for this batch: fail every job in flight

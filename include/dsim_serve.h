@@ -8,9 +8,13 @@
  * gradients whose signals they want) at any time; the worker admits pending
  * jobs in arrival order while the batch has free spin slots and the device
  * footprint of the admitted jobs and the resident substrates stays within
- * the HBM cap, advances all admitted jobs together in quanta of
- * chunk x graphChunks steps, and when a job finishes computes its signals,
- * records the time and frees its slots for the next arrivals.  A job's result
+ * the HBM cap, advances all admitted jobs together in quanta of whole chunks
+ * (about 0.2 s of device time at the last quantum's rate, at most
+ * chunk x graphChunks steps), and when a job finishes computes its signals,
+ * records the time and frees its slots for the next arrivals.  Every admitted
+ * job advances at the batch's step rate, so the spin capacity also bounds a
+ * job's time in the batch: a few million slots keep the GPU full while jobs
+ * finish quickly.  A job's result
  * does not depend on which other jobs share the batch (dsim_batch.h).
  *
  * Times are seconds since dsim_server_start on a steady clock.
