@@ -1291,7 +1291,8 @@ def run_precision(args, W, m):
         bb = Batch(W.N + 64, 1)
         sid = bb.add_mesh(m)
         jid = bb.submit(sid, W.pos, W.comp, W.fiber.astype(np.uint32), args.c5_rate_steps, dt, sd, W.T2, pc, 5,
-                        waveform="table", table=waves[1][:args.c5_rate_steps], precise=(form == "precise"),
+                        waveform="table", table=np.resize(waves[1], args.c5_rate_steps).astype(F),
+                        precise=(form == "precise"),
                         local=(form == "local"))
         bb.sync()
         t0 = time.time()

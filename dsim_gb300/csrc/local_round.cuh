@@ -138,25 +138,79 @@ __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWa
     return local_fp64(H, Lw, g, t, o, h, pc);
 }
 
-// The chosen hit's point in FP64 from the same FP32 operands, rounded once to
-// the local frame: the float nearest the exact crossing.  In FP32 the point o
-// + d r would carry an error comparable to the local coordinates' finer ulp,
-// so a spin leaving a hit could start off a plane it lies on (an axis-aligned
-// plane, or a coincident membrane) and meet that plane again at r ~ 1e-7.
-// Hits decided in FP64 carry their point already (no kLocalRefine).
+// ---- float-float arithmetic (pairs hi + lo of floats, ~48-bit significand):
+// Knuth's TwoSum and the fma-based TwoProduct are error-free; the rest keeps
+// the pair's error near 2^-44 relative.
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ FF ff_two_prod(float a, float b) {
+    const float p = a * b;
+    return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_norm(float hi, float lo) {
+    const float s = hi + lo;
+    return {s, lo - (s - hi)};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    const FF s = ff_two_sum(a.hi, b.hi);
+    return ff_norm(s.hi, s.lo + (a.lo + b.lo));
+}
+// n . (e - o) for float vectors: e - o exactly (TwoSum), each product exactly
+// (TwoProduct) up to the small term's rounding
+__device__ __forceinline__ FF ff_dot_diff(float nx, float ny, float nz, float ex, float ey, float ez, float ox,
+                                          float oy, float oz) {
+    const FF ux = ff_two_sum(ex, -ox), uy = ff_two_sum(ey, -oy), uz = ff_two_sum(ez, -oz);
+    FF px = ff_two_prod(nx, ux.hi), py = ff_two_prod(ny, uy.hi), pz = ff_two_prod(nz, uz.hi);
+    px.lo += nx * ux.lo;
+    py.lo += ny * uy.lo;
+    pz.lo += nz * uz.lo;
+    return ff_add(ff_add(px, py), pz);
+}
+__device__ __forceinline__ FF ff_dot(float nx, float ny, float nz, float dx, float dy, float dz) {
+    return ff_add(ff_add(ff_two_prod(nx, dx), ff_two_prod(ny, dy)), ff_two_prod(nz, dz));
+}
+// a / b: the float quotient and one correction from the remainder
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q = a.hi / b.hi;
+    const FF p = ff_two_prod(q, b.hi);
+    const float rem = (((a.hi - p.hi) - p.lo) + a.lo) - q * b.lo;
+    return ff_norm(q, rem / b.hi);
+}
+// o + d r rounded once to float
+__device__ __forceinline__ float ff_axpy(float o, float d, FF r) {
+    FF m = ff_two_prod(d, r.hi);
+    m.lo = fmaf(d, r.lo, m.lo);
+    const FF s = ff_two_sum(o, m.hi);
+    return s.hi + (s.lo + m.lo);
+}
+
+// The chosen hit's point from the same FP32 operands in float-float
+// arithmetic, rounded once to the local frame: the float nearest the exact
+// crossing (but where the exact value lies within about 2^-44 of a rounding
+// boundary).  In plain FP32 the point o + d r would carry an error comparable
+// to the local coordinates' finer ulp, so a spin leaving a hit could start off
+// a plane it lies on (an axis-aligned plane, or a coincident membrane) and
+// meet that plane again at r ~ 1e-7.  Float-float keeps this on the FP32
+// pipe: GB300's FP64 rate is a small fraction of its FP32 rate.  Hits decided
+// in FP64 carry their point already (no kLocalRefine).
 __device__ __forceinline__ void local_refine(const MeshDev& g, float gx, float gy, float gz, float ox, float oy,
                                              float oz, float dx, float dy, float dz, FastHit& h) {
     if (!(h.type & kLocalRefine)) return;
     h.type &= ~kLocalRefine;
     const float4* pp = reinterpret_cast<const float4*>(g.plane + h.t);
     const float4 a = __ldg(pp), c = __ldg(pp + 1);  // {n, p1.x}, {p1.y, p1.z, vv, info}
-    const double n64 = (double)a.x * ((double)(a.w - gx) - (double)ox) + (double)a.y * ((double)(c.x - gy) - (double)oy) +
-                       (double)a.z * ((double)(c.y - gz) - (double)oz);
-    const double d64 = (double)a.x * dx + (double)a.y * dy + (double)a.z * dz;
-    const double r64 = n64 / d64;
-    h.x = (float)((double)ox + (double)dx * r64);
-    h.y = (float)((double)oy + (double)dy * r64);
-    h.z = (float)((double)oz + (double)dz * r64);
+    const FF num = ff_dot_diff(a.x, a.y, a.z, a.w - gx, c.x - gy, c.y - gz, ox, oy, oz);
+    const FF den = ff_dot(a.x, a.y, a.z, dx, dy, dz);
+    const FF r = ff_div(num, den);
+    h.x = ff_axpy(ox, dx, r);
+    h.y = ff_axpy(oy, dy, r);
+    h.z = ff_axpy(oz, dz, r);
 }
 
 // record k of the fine grid
