@@ -659,12 +659,12 @@ def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False, sub
 def _submit_kw(j, form="fp32"):
     """Job keywords; form "fp32": the plain FP32 step with Kahan moments;
     "bar": the forms that hold the 1e-3 signal-error bar (mesh jobs
-    cell-local, DSIM_JOB_LOCAL; cylinder jobs FP64 positions, DSIM_JOB_PRECISE)."""
+    and cylinder jobs in the cell-local form, DSIM_JOB_LOCAL)."""
     kw = dict(steps=j["steps"], dt=j["dt"], step_sd=j["step_sd"], T2=j["T2"], phase_constant=j["phase_constant"],
               seed=j["seed"], permeability=j["permeability"], waveform="pgse", delta=j["delta"],
               Delta=j["Delta"], inner_radius_proportion=j["inner"])
     if form == "bar":
-        kw.update(local=j["sub"].kind == "mesh", precise=j["sub"].kind != "mesh")
+        kw.update(local=True)
     return kw
 
 
@@ -699,7 +699,7 @@ def run_plain_mix(mix):
 
 def run_plain_bar_mix(subs, mix):
     """One job at a time in the forms that hold the 1e-3 error bar (mesh jobs
-    cell-local, cylinder jobs FP64 positions): a batch holding that job alone,
+    and cylinder jobs cell-local): a batch holding that job alone,
     from submission to its first gradient's signal."""
     from dsim_gb300.engine import Batch
     per, sig0 = [], []
@@ -867,7 +867,7 @@ def run_c4_full(args, W, m):
     out = {"jobs": n_jobs, "seed": seed, "spins": list(spins_range), "steps": list(steps_range),
            "spin_steps": float(work.sum()), "mesh_jobs": int(sum(sb.kind == "mesh" for sb, _, _ in shapes)),
            "permeability": "log-uniform 1e-4 - 1e-2 per hit", "hbm_cap_GB": 150,
-           "form": ("mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
+           "form": ("cell-local FP32 (DSIM_JOB_LOCAL) for mesh and cylinder jobs"
                     if form == "bar" else "fp32: the plain FP32 step, Kahan moments"),
            "plain": {"spin_steps_per_s": plain_rate, "jobs_per_s": cap_jobs, "sample_jobs": K,
                      "sample_spin_steps_per_s": float(work[:K].sum() / sum(per)),
@@ -1010,7 +1010,7 @@ def run_forms(args, W, m):
         "plain_bar": {"spin_steps_per_s": plainbar_rate, "seconds": plainbar_s,
                       "err_vs_fp64": mix_err(mix, first(bsig), {i: r[:1] for i, r in ref.items()}, {}),
                       "note": "one job at a time in the forms that hold the 1e-3 bar (a batch holding that job "
-                              "alone: mesh jobs cell-local, cylinder jobs FP64 positions), first gradient"},
+                              "alone: cell-local mesh and cylinder jobs), first gradient"},
         "batched": {"spin_steps_per_s": work / el, "seconds": el, "speedup_vs_plain": (work / el) / plain_rate,
                     "signals_speedup_vs_plain": (grad_work / el) / plain_rate,
                     "note": "all jobs in one batch; signals_speedup counts one plain walk per gradient, as the "
@@ -1025,8 +1025,7 @@ def run_forms(args, W, m):
                           "speedup_vs_plain": (work / el_b) / plain_rate,
                           "signals_speedup_vs_plain_bar": (grad_work / el_b) / plainbar_rate,
                           "status": st_b, "err_vs_fp64": mix_err(mix, sigs_b, ref, cyl_err),
-                          "form": "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions "
-                                  "(DSIM_JOB_PRECISE)"}
+                          "form": "cell-local FP32 (DSIM_JOB_LOCAL) for mesh and cylinder jobs"}
     # serving: the same substrates and ranges with permeable membranes (per-hit
     # permeation log-uniform 1e-4 - 1e-2), in the error-bar forms; arrival
     # rates relative to the capacity of the plain form at the same bar (one
@@ -1048,7 +1047,7 @@ def run_forms(args, W, m):
             o["rate_x_plain_bar_capacity"] = r
             o["speedup_vs_plain_bar"] = o["spin_steps_per_s"] / (pwork / pbar_s)
             o["err_vs_fp64"] = mix_err(pmix, ssig, pref, pcyl)
-            o["form"] = "mesh jobs cell-local FP32 (DSIM_JOB_LOCAL), cylinder jobs FP64 positions (DSIM_JOB_PRECISE)"
+            o["form"] = "cell-local FP32 (DSIM_JOB_LOCAL) for mesh and cylinder jobs"
             out["served"].append(o)
     return out
 
@@ -1136,11 +1135,29 @@ def run_cylinders(args):
     prec_s = time.perf_counter() - t0
     S_prec = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
     b.close()
+    # and in the cylinder cell-local form
+    b = Batch((N + 31) // 32 * 32, 1)
+    sid = b.add_cyl(c)
+    t0 = time.perf_counter()
+    j = b.submit(sid, pos.reshape(-1), imo, near, steps, dt, sd, T2, pc, 1, waveform="pgse", delta=delta,
+                 Delta=Delta, inner_radius_proportion=1.0, local=True)
+    b.run()
+    sums = b.signal(j, gs, region=0.8)
+    loc_s = time.perf_counter() - t0
+    S_loc = np.hypot(sums[:, 0, 0], sums[:, 0, 1]) / sums[:, 0, 2]
+    loc_tests, loc_exact = b.precision_counts(j)
+    b.close()
     err = {"shared_walk": _err_summary(err_shared, "FP64 oracle walk on the same Philox draws, all 48 gradients"),
            "shared_walk_precise": dict(_err_summary(np.abs(S_prec - _S(z64, in_box(p64))), "FP64 oracle walk on "
                                                     "the same Philox draws, all 48 gradients"),
                                        form="DSIM_JOB_PRECISE: the dSim2 step with FP64 positions",
                                        spin_steps_per_s=N * steps / prec_s),
+           "shared_walk_local": dict(_err_summary(np.abs(S_loc - _S(z64, in_box(p64))), "FP64 oracle walk on "
+                                                  "the same Philox draws, all 48 gradients"),
+                                     form="DSIM_JOB_LOCAL: the dSim2 step on FP32 offsets from a 1/16 lattice, "
+                                          "FP64 decisions inside the FP32 error band",
+                                     spin_steps_per_s=N * steps / loc_s,
+                                     fp64_decision_fraction=loc_exact / max(loc_tests, 1)),
            "plain": _err_summary(err_plain, "FP64 oracle walk on each walk's Philox draws, 80 mT/m along the "
                                             "6 directions"),
            "seconds": time.perf_counter() - t_err}

@@ -275,7 +275,7 @@ k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
-    if (!(J.flags & DSIM_JOB_LOCAL)) return;  // warp-uniform
+    if (!(J.flags & DSIM_JOB_LOCAL) || subS[wi].kind != kSubMesh) return;  // warp-uniform
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;
@@ -704,7 +704,7 @@ struct dsim_batch {
     // the step kernels of a chunk (one per record layout and form) advance
     // disjoint jobs: they run side by side on these streams, forked from st
     // after the sort and joined before the step counter advances
-    static constexpr int kSide = 5;
+    static constexpr int kSide = 6;
     cudaStream_t side[kSide] = {};
     cudaEvent_t forkEv = nullptr, joinEv[kSide] = {};
     uint64_t cap = 0;
@@ -730,6 +730,7 @@ struct dsim_batch {
     uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
     bool anyPrecise = false, anyLocal = false;  // precision-form / cell-local mesh jobs
     bool anyPreciseCyl = false;                 // precision-form cylinder jobs
+    bool anyLocalCyl = false;                   // cell-local cylinder jobs
     cudaGraphExec_t exec = nullptr;
     bool graphValid = false;
     int graphCur = -1;
@@ -820,7 +821,7 @@ uint32_t step_layouts(const dsim_batch* b) {
 uint64_t chunk_launches(const dsim_batch* b) {
     const uint32_t mask = step_layouts(b);
     return 5ull + (uint64_t)__builtin_popcount(mask & 0xEu) + (b->anyPrecise ? 1ull : 0ull) +
-           (b->anyLocal ? 1ull : 0ull) + (b->anyPreciseCyl ? 1ull : 0ull) + 1ull;
+           (b->anyLocal ? 1ull : 0ull) + (b->anyPreciseCyl ? 1ull : 0ull) + (b->anyLocalCyl ? 1ull : 0ull) + 1ull;
 }
 
 // Precision-form cylinder jobs (DSIM_JOB_PRECISE): the dSim2 step of
@@ -903,6 +904,101 @@ k_batch_step_cyl64(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
     if (st) atomicOr(status, st);
 }
 
+// Cell-local FP32 cylinder jobs (DSIM_JOB_LOCAL): the dSim2 step with the
+// position as a lattice origin (multiple of 1/16) plus an FP32 offset in
+// [0, 1/16), membrane decisions near their FP32 error band taken in FP64
+// (cyl_membranes_local), Kahan moments.  Between chunks the position is kept
+// in the double fields as origin + offset.
+__global__ void __launch_bounds__(kFlatThreads, 4)
+k_batch_step_cyl_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
+                       const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
+                       unsigned long long* jobCounts) {
+    __shared__ float mom[6][kFlatThreads];
+    const uint32_t FULL = 0xFFFFFFFFu;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t tx = threadIdx.x;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i & ~31u) >= S.N) return;  // whole warp: N is a multiple of 32
+    const uint32_t jb = S.u[U_JOB][i & ~31u];
+    const JobDev& J = jobs[jb];
+    if (!(__ldg(&J.flags) & DSIM_JOB_LOCAL)) return;  // warp-uniform
+    const SubDev& sub = subs[__ldg(&J.sub)];
+    if (__ldg(&sub.kind) != kSubCyl) return;
+    const uint32_t now = *stepNow;
+    const uint32_t start = __ldg(&J.start), steps = __ldg(&J.steps);
+    if (now < start || now - start >= steps) return;
+    const uint32_t ls0 = now - start;
+    const uint32_t nsteps = min(chunk, steps - ls0);
+    const uint32_t id = S.u[U_ID][i];
+    const bool valid = id != 0xFFFFFFFFu;
+    uint32_t nrefl = 0, nperm = 0, st = 0, ntests = 0, nexact = 0;
+    if (valid) {
+        const CylDev g = sub.c;
+        const double X = S.d[D_X][i], Y = S.d[D_Y][i], Z = S.d[D_Z][i];
+        CylOrigin G;
+        G.x = (float)(floor(X * 16.0) * 0.0625);
+        G.y = (float)(floor(Y * 16.0) * 0.0625);
+        G.z = (float)(floor(Z * 16.0) * 0.0625);
+        float x = (float)(X - (double)G.x), y = (float)(Y - (double)G.y), z = (float)(Z - (double)G.z);
+        float mag = S.f[F_MAG][i];
+        mom[0][tx] = S.f[F_MX][i]; mom[1][tx] = S.f[F_MY][i]; mom[2][tx] = S.f[F_MZ][i];
+        mom[3][tx] = S.f[F_CX][i]; mom[4][tx] = S.f[F_CY][i]; mom[5][tx] = S.f[F_CZ][i];
+        const uint32_t meta = S.u[U_META][i];
+        uint32_t imo = meta & 0xFFu, nearest = meta >> 8;
+        if (imo < 2 && nearest >= g.nF) imo = 2;
+        const float perm = __ldg(&J.perm), inR = __ldg(&J.inR);
+        const float clampHi = __ldg(&J.clampHi), clampLo = __ldg(&J.clampLo), dt = __ldg(&J.dt);
+        const uint32_t k0 = __ldg(&J.key0), k1 = __ldg(&J.key1);
+        const float* __restrict__ wave = J.wave;
+        for (uint32_t it = 0; it < nsteps; it++) {
+            const Draw d = philox_draw(id, (uint64_t)(ls0 + it), 0u, k0, k1);
+            const float ox = x, oy = y, oz = z;
+            const float sd = __ldg(&J.sd[imo < 3 ? imo : 2]);
+            float px = x + d.nx * sd, py = y + d.ny * sd, pz = z + d.nz * sd;
+            cyl_membranes_local(g, G, ox, oy, oz, px, py, pz, d.u, perm, inR, imo, nearest, nrefl, nperm, st, ntests,
+                                nexact);
+            // clamp in absolute coordinates, then move the origin so the
+            // offset is back in [0, 1/16)
+            if (G.x + px > clampHi) px = clampHi - G.x; else if (G.x + px < clampLo) px = clampLo - G.x;
+            if (G.y + py > clampHi) py = clampHi - G.y; else if (G.y + py < clampLo) py = clampLo - G.y;
+            if (G.z + pz > clampHi) pz = clampHi - G.z; else if (G.z + pz < clampLo) pz = clampLo - G.z;
+            const float sx = floorf(px * 16.0f) * kLatticeH, sy = floorf(py * 16.0f) * kLatticeH,
+                        sz = floorf(pz * 16.0f) * kLatticeH;
+            G.x += sx; G.y += sy; G.z += sz;
+            x = px - sx; y = py - sy; z = pz - sz;
+            const float T2 = __ldg(&J.T2[imo < 3 ? imo : 2]);
+            if (T2 > 0.0f) mag += -mag / T2 * dt;
+            const float w = __ldg(wave + ls0 + it);
+            kahan_add(mom[0][tx], mom[3][tx], w * (G.x + x));
+            kahan_add(mom[1][tx], mom[4][tx], w * (G.y + y));
+            kahan_add(mom[2][tx], mom[5][tx], w * (G.z + z));
+        }
+        const double Xn = (double)G.x + (double)x, Yn = (double)G.y + (double)y, Zn = (double)G.z + (double)z;
+        S.d[D_X][i] = Xn; S.d[D_Y][i] = Yn; S.d[D_Z][i] = Zn; S.d[D_MAG][i] = (double)mag;
+        S.f[F_X][i] = (float)Xn; S.f[F_Y][i] = (float)Yn; S.f[F_Z][i] = (float)Zn;
+        S.f[F_MAG][i] = mag;
+        S.f[F_MX][i] = mom[0][tx]; S.f[F_MY][i] = mom[1][tx]; S.f[F_MZ][i] = mom[2][tx];
+        S.f[F_CX][i] = mom[3][tx]; S.f[F_CY][i] = mom[4][tx]; S.f[F_CZ][i] = mom[5][tx];
+        S.u[U_META][i] = (imo & 0xFFu) | ((nearest & 0xFFFFFFu) << 8);
+    }
+    // per-job counters {reflections, permeations, distance tests, FP64 decisions}
+    unsigned long long r = nrefl, p = nperm, te = ntests, ex = nexact;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        r += __shfl_down_sync(FULL, r, o);
+        p += __shfl_down_sync(FULL, p, o);
+        te += __shfl_down_sync(FULL, te, o);
+        ex += __shfl_down_sync(FULL, ex, o);
+    }
+    if (lane == 0) {
+        if (r) atomicAdd(jobCounts + 4 * jb, r);
+        if (p) atomicAdd(jobCounts + 4 * jb + 1, p);
+        if (te) atomicAdd(jobCounts + 4 * jb + 2, te);
+        if (ex) atomicAdd(jobCounts + 4 * jb + 3, ex);
+    }
+    if (st) atomicOr(status, st);
+}
+
 template <int LAYOUT>
 void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D, cudaStream_t st) {
     if (b->occupancy >= 8)
@@ -938,6 +1034,7 @@ int enqueue_chunk(dsim_batch* b) {
     if (b->anyLocal) kinds[nk++] = 4;
     if (b->anyPrecise) kinds[nk++] = 5;
     if (b->anyPreciseCyl) kinds[nk++] = 6;
+    if (b->anyLocalCyl) kinds[nk++] = 7;
     const bool fork = nk > 1;
     if (fork) DSIM_CUDA_TRY(cudaEventRecord(b->forkEv, b->st));
     for (int q = 0; q < nk; q++) {
@@ -955,9 +1052,13 @@ int enqueue_chunk(dsim_batch* b) {
                 k_batch_step64<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
                                                               b->d_status, b->d_counts);
                 break;
-            default:
+            case 6:
                 k_batch_step_cyl64<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
                                                                   b->d_status, b->d_counts);
+                break;
+            default:
+                k_batch_step_cyl_local<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow,
+                                                                      b->chunk, b->d_status, b->d_counts);
                 break;
         }
         if (fork) {
@@ -1189,10 +1290,6 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
         return kErrInvalid;
     }
     J.spinR = d->spinRadius;
-    if ((J.flags & DSIM_JOB_LOCAL) && cyl) {
-        set_last_error(kErrInvalid, "dsim_batch_submit: the cell-local form applies to mesh jobs");
-        return kErrInvalid;
-    }
     if (J.flags) {
         int rc = ensure_precise(b, d->substrate);
         if (rc) return rc;
@@ -1253,7 +1350,7 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
     DSIM_CUDA_TRY(cudaMemsetAsync(b->d_counts + 4 * jobIndex, 0, 32, b->st));
     DSIM_CUDA_TRY(cudaStreamSynchronize(b->st));
     if (J.flags & DSIM_JOB_PRECISE) (cyl ? b->anyPreciseCyl : b->anyPrecise) = true;
-    if (J.flags & DSIM_JOB_LOCAL) b->anyLocal = true;
+    if (J.flags & DSIM_JOB_LOCAL) (cyl ? b->anyLocalCyl : b->anyLocal) = true;
     invalidate_graph(b);
     *jobId = j.id;
     return kOk;
@@ -1519,11 +1616,11 @@ int dsim_batch_compact(dsim_batch* b) {
     b->cur = 1 - b->cur;
     b->jobs = kept;
     b->N = slot;
-    b->anyPrecise = b->anyLocal = b->anyPreciseCyl = false;
+    b->anyPrecise = b->anyLocal = b->anyPreciseCyl = b->anyLocalCyl = false;
     for (const auto& j : b->jobs) {
         const bool jc = b->subs[j.d.sub].kind == kSubCyl;
         (jc ? b->anyPreciseCyl : b->anyPrecise) |= (j.d.flags & DSIM_JOB_PRECISE) != 0;
-        b->anyLocal |= (j.d.flags & DSIM_JOB_LOCAL) != 0;
+        (jc ? b->anyLocalCyl : b->anyLocal) |= (j.d.flags & DSIM_JOB_LOCAL) != 0;
     }
     if ((rc = layout_keys(b)) || (rc = upload_jobs(b))) return rc;
     if (!newCounts.empty())

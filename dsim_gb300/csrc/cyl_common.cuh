@@ -355,4 +355,184 @@ __device__ __forceinline__ void cyl_membranes64(const CylDev& g, double ox, doub
     }
 }
 
+// ---- the cell-local FP32 form (DSIM_JOB_LOCAL cylinder jobs) ---------------
+// A position is a lattice origin G (a multiple of 1/16, exact in float) plus an
+// FP32 offset p.  The distance to a fiber's axis is formed in the local frame,
+// ((G - f) + p) per axis, which rounds about 16x finer than the absolute FP32
+// coordinates of the reference's step.  Each membrane decision compares d^2
+// with inR r^2 and r^2; where the FP32 d^2 lies within its error band of
+// either, the decision is taken from the FP64 distance at the exact position
+// G + p, as the FP64 form would take it there.  Grid and fine-grid lookups use
+// the absolute position rounded to float (the fine lists are registered
+// against cells widened by 1e-5).
+struct CylOrigin {
+    float x, y, z;
+};
+
+__device__ __forceinline__ float cyl_dist_sq_local(const CylOrigin& G, float px, float py, float pz, float4 f) {
+    if (f.x == 2.0f) {
+        const float ez = (G.z - f.z) + pz, ey = (G.y - f.y) + py;
+        return ez * ez + ey * ey;
+    } else if (f.z == 2.0f) {
+        const float ex = (G.x - f.x) + px, ey = (G.y - f.y) + py;
+        return ex * ex + ey * ey;
+    }
+    const float ex = (G.x - f.x) + px, ez = (G.z - f.z) + pz;
+    return ex * ex + ez * ez;
+}
+
+// Signs of d^2 - inR r^2 (in) and d^2 - r^2 (out).  Error of the FP32 d^2,
+// u = 2^-24: a local coordinate e = (G - f) + p is off by at most
+// u (|G - f| + |e|) <= u (2|e| + |p|) (two roundings); the squares and the sum
+// add u d^2 each, so d^2 is off by at most u (6 d^2 + 2.83 |p| d), and the
+// FP32 threshold inR r^2 by u inR r^2.  The band is 4x their sum at
+// d^2 = max(inR r^2, r^2) = M.  nexact counts the FP64 decisions.
+struct CylSides {
+    int in, out;
+};
+__device__ __forceinline__ CylSides cyl_sides_local(const CylOrigin& G, float px, float py, float pz, float4 f,
+                                                    float inR, uint32_t& ntests, uint32_t& nexact) {
+    ntests++;
+    const float cur = cyl_dist_sq_local(G, px, py, pz, f);
+    const float A = inR * f.w, B = f.w;
+    const float M = fmaxf(A, B);
+    const float pm = fmaxf(fabsf(px), fmaxf(fabsf(py), fabsf(pz)));
+    const float band = 2.4e-7f * (7.0f * M + 2.83f * pm * sqrtf(M));
+    if (fabsf(cur - A) > band && fabsf(cur - B) > band) return {cur < A ? -1 : 1, cur < B ? -1 : 1};
+    nexact++;
+    const double c = cyl_dist_sq64((double)G.x + (double)px, (double)G.y + (double)py, (double)G.z + (double)pz, f);
+    const double A64 = (double)inR * (double)f.w, B64 = (double)f.w;
+    return {(int)(c > A64) - (int)(c < A64), (int)(c > B64) - (int)(c < B64)};
+}
+
+__device__ __forceinline__ void cyl_outside_entry_local(const CylOrigin& G, float4 f, const uint32_t* list,
+                                                        uint32_t j, float ox, float oy, float oz, float& px,
+                                                        float& py, float& pz, float u, float perm, float inR,
+                                                        uint32_t& imo, uint32_t& nearest, uint32_t& nrej,
+                                                        uint32_t& nperm, bool& moved, bool& inside,
+                                                        uint32_t& ntests, uint32_t& nexact) {
+    const CylSides s = cyl_sides_local(G, px, py, pz, f, inR, ntests, nexact);
+    inside |= (s.in < 0) | (s.out < 0);
+    if ((s.out <= 0) & (s.in > 0)) {
+        if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else { imo = 1; nearest = __ldg(list + j); nperm++; }
+    } else if (s.in < 0) {
+        if (u < 1.0f - perm) { px = ox; py = oy; pz = oz; nrej++; moved = true; }
+        else if ((1.0f - perm < u) & (u < 1.0f - perm * perm)) {
+            px = ox; py = oy; pz = oz; nearest = __ldg(list + j); imo = 1; nrej++;
+            moved = true;
+        } else { imo = 0; nearest = __ldg(list + j); nperm++; }
+    }
+}
+
+// cyl_membranes with local positions (origin G; o, p local to it) and the
+// decisions of cyl_sides_local
+__device__ __forceinline__ void cyl_membranes_local(const CylDev& g, const CylOrigin& G, float ox, float oy, float oz,
+                                                    float& px, float& py, float& pz, float u, float perm, float inR,
+                                                    uint32_t& imo, uint32_t& nearest, uint32_t& nrej,
+                                                    uint32_t& nperm, uint32_t& status, uint32_t& ntests,
+                                                    uint32_t& nexact) {
+    if (!(perm < 1.0f)) return;
+    if (imo < 2) {
+        const float4 f = __ldg(g.fibers + nearest);
+        const CylSides s = cyl_sides_local(G, px, py, pz, f, inR, ntests, nexact);
+        if (imo == 0) {
+            if ((s.in > 0) & (s.out <= 0)) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 1; nperm++; }
+            } else if (s.out > 0) {
+                if (u < 1.0f - perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else if ((1.0f - perm < u) & (u < 1.0f - perm * perm)) {
+                    px = ox; py = oy; pz = oz; imo = 1; nrej++;
+                } else { imo = 2; nperm++; }
+            }
+        } else {
+            if (s.out > 0) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 2; nperm++; }
+            } else if (s.in < 0) {
+                if (u >= perm) { px = ox; py = oy; pz = oz; nrej++; }
+                else { imo = 0; nperm++; }
+            }
+        }
+        const CylSides e = cyl_sides_local(G, px, py, pz, f, inR, ntests, nexact);
+        if (e.out > 0) imo = 2;
+        else if (e.in < 0) imo = 0;
+        else imo = 1;
+        return;
+    }
+    uint32_t cube = cyl_cell(G.x + px, G.y + py, G.z + pz, g.L, g.n);
+    uint32_t cnt = __ldg(g.cube_count + cube);
+    const uint32_t* list = g.cubes + (size_t)cube * g.maxFPC;
+    const float4* inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
+    bool moved = false, inside = false;
+    const bool fine = g.fine_start != nullptr && inR <= 1.0f;
+    uint32_t j = 0;
+    if (fine) {
+        const uint32_t fc = cyl_fine_cell(g, G.x + px, G.y + py, G.z + pz, cube);
+        const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+        j = cnt;
+        uint32_t jm = 0;
+        for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+            const uint32_t jj = __ldg(g.fine_pos + e);
+            cyl_outside_entry_local(G, __ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm, inR, imo,
+                                    nearest, nrej, nperm, moved, inside, ntests, nexact);
+            if (moved) { jm = jj; break; }
+        }
+        if (moved) {
+            if (cyl_cell(G.x + px, G.y + py, G.z + pz, g.L, g.n) == cube) {
+                const uint32_t fo = cyl_fine_cell(g, G.x + px, G.y + py, G.z + pz, cube);
+                const uint32_t eo1 = __ldg(g.fine_start + fo + 1);
+                for (uint32_t e = __ldg(g.fine_start + fo); e < eo1; e++) {
+                    const uint32_t jj = __ldg(g.fine_pos + e);
+                    if (jj <= jm) continue;
+                    cyl_outside_entry_local(G, __ldg(g.fine_rec + e), list, jj, ox, oy, oz, px, py, pz, u, perm,
+                                            inR, imo, nearest, nrej, nperm, moved, inside, ntests, nexact);
+                }
+            } else {
+                j = jm + 1;
+            }
+        }
+    }
+    for (; j < cnt; j++) {
+        float4 f;
+        if (inl) {
+            f = __ldg(inl + j);
+        } else {
+            const uint32_t fi = __ldg(list + j);
+            if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+            f = __ldg(g.fibers + fi);
+        }
+        cyl_outside_entry_local(G, f, list, j, ox, oy, oz, px, py, pz, u, perm, inR, imo, nearest, nrej, nperm,
+                                moved, inside, ntests, nexact);
+    }
+    if (imo == 2 && (moved || inside)) {
+        cube = cyl_cell(G.x + px, G.y + py, G.z + pz, g.L, g.n);
+        cnt = __ldg(g.cube_count + cube);
+        list = g.cubes + (size_t)cube * g.maxFPC;
+        inl = g.cube_fibers ? g.cube_fibers + (size_t)cube * g.maxFPC : nullptr;
+        if (fine && moved) {
+            const uint32_t fc = cyl_fine_cell(g, G.x + px, G.y + py, G.z + pz, cube);
+            const uint32_t e1 = __ldg(g.fine_start + fc + 1);
+            for (uint32_t e = __ldg(g.fine_start + fc); e < e1; e++) {
+                const CylSides s = cyl_sides_local(G, px, py, pz, __ldg(g.fine_rec + e), inR, ntests, nexact);
+                if ((s.in < 0) | (s.out < 0)) { px = ox; py = oy; pz = oz; nrej++; }
+            }
+        } else {
+            for (uint32_t j2 = 0; j2 < cnt; j2++) {
+                float4 f;
+                if (inl) {
+                    f = __ldg(inl + j2);
+                } else {
+                    const uint32_t fi = __ldg(list + j2);
+                    if (fi >= g.nF) { status |= kStatusBadCell; continue; }
+                    f = __ldg(g.fibers + fi);
+                }
+                const CylSides s = cyl_sides_local(G, px, py, pz, f, inR, ntests, nexact);
+                if ((s.in < 0) | (s.out < 0)) { px = ox; py = oy; pz = oz; nrej++; }
+            }
+        }
+    }
+}
+
 }  // namespace dsim

@@ -53,7 +53,7 @@ typedef struct {
     float frequency;               /* Hz (OGSE) */
     const float* table;            /* DSIM_WAVE_TABLE: `steps` values (host) */
     uint64_t seed;                 /* Philox key; counter = (spin, step, 0) */
-    uint32_t flags;                /* DSIM_JOB_PRECISE (mesh or cylinder jobs) or DSIM_JOB_LOCAL (mesh jobs) */
+    uint32_t flags;                /* DSIM_JOB_PRECISE or DSIM_JOB_LOCAL (mesh or cylinder jobs) */
     uint32_t reserved;
 } dsim_job_desc;
 
@@ -75,8 +75,14 @@ typedef struct {
  * intersections whose FP32 outcome lies within the FP32 error band of a
  * decision boundary (crossing parameter near 0 or 1, a barycentric coordinate
  * within 1e-5 of an edge) are decided again in FP64 on the FP64 triangle
- * helpers; moments are Kahan-compensated FP32.  Exclusive with
- * DSIM_JOB_PRECISE.  dsim_batch_get_precise returns origin + offset. */
+ * helpers; moments are Kahan-compensated FP32.  For a cylinder job the
+ * distances to the fibers are formed in the local frame, and a membrane
+ * decision whose FP32 distance lies within its error band of inR r^2 or r^2
+ * is taken from the FP64 distance at the exact position, as the FP64 form
+ * takes it there (grid lookups use the position rounded to float).
+ * dsim_batch_precision_counts then reports distance tests and FP64
+ * decisions.  Exclusive with DSIM_JOB_PRECISE.  dsim_batch_get_precise
+ * returns origin + offset. */
 #define DSIM_JOB_LOCAL 2u
 
 /* spinCapacity: packed spin slots (each job is padded to a multiple of 32) */
@@ -120,7 +126,7 @@ int dsim_batch_get(dsim_batch* b, uint32_t jobId, float* pos3, float* mag, float
 /* per-job {reflections or rejections, permeations} and status bits */
 int dsim_batch_counts(dsim_batch* b, uint32_t jobId, uint64_t counts[2]);
 /* precision and cell-local forms: {fine-grid records examined, FP64 triangle
- * tests} */
+ * tests}; cell-local cylinder jobs: {distance tests, FP64 decisions} */
 int dsim_batch_precision_counts(dsim_batch* b, uint32_t jobId, uint64_t out[2]);
 /* precision and cell-local forms: FP64 positions (3 per spin) and magnitudes
  * in spin order; DSIM_EINVAL for a plain job.  Synchronous. */

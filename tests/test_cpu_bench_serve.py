@@ -100,7 +100,7 @@ def test_stream_submits_every_job_once_in_order(bench, ahead):
         assert srv.sub_list[sid][0] == j["sub"].kind
         assert np.array_equal(pos, j["pos"]) and np.array_equal(grads, j["grads"])
         assert kw["steps"] == j["steps"] and kw["seed"] == k
-        assert kw.get("local") == (j["sub"].kind == "mesh") and kw.get("precise") == (j["sub"].kind != "mesh")
+        assert kw.get("local") is True and not kw.get("precise")     # the error-bar form: cell-local
     assert set(sigs) == keep
     for k in keep:
         assert sigs[k].shape == (3, 5, 3) and np.all(sigs[k] == k)
