@@ -748,6 +748,9 @@ def tune_mix(subs, mix):
     return best, ms
 
 
+SERVE_MAX_CHUNK = 200
+
+
 def serve_stream(subs, get_job, n_jobs, cfg, rate, form, spin_capacity, seed=3, ahead=0, keep=None):
     """Poisson arrivals at `rate` jobs/s of jobs get_job(0..n_jobs-1) into the
     request loop (150 GB HBM cap).  With `ahead` > 0, host threads generate the
@@ -758,7 +761,9 @@ def serve_stream(subs, get_job, n_jobs, cfg, rate, form, spin_capacity, seed=3, 
     from dsim_gb300.engine import Server
     srv = Server(spin_capacity=spin_capacity, job_capacity=n_jobs, hbm_cap=150e9)
     sids = {id(sb): (srv.add_mesh(sb.handle) if sb.kind == "mesh" else srv.add_cyl(sb.handle)) for sb in subs}
-    srv.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
+    # the server admits at chunk boundaries: at most 200 steps per chunk keeps
+    # admission prompt whatever chunk the batch autotuner chose
+    srv.configure(chunk=min(cfg["chunk"], SERVE_MAX_CHUNK), occupancy=cfg["occupancy"], graph_chunks=8)
     pool = ThreadPoolExecutor(8) if ahead else None
     futs = {}
 
@@ -810,7 +815,7 @@ def serve_stream(subs, get_job, n_jobs, cfg, rate, form, spin_capacity, seed=3, 
     return {"rate_jobs_per_s": rate, "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "spin_steps_per_s": work / (last - first), "max_jobs_in_flight": int(st["max_inflight"]),
             "errors": int(st["errors"]), "hbm_peak_GB": st["hbm_peak"] / 1e9, "late_submissions": late,
-            "wall_s": last - first}, sigs
+            "wall_s": last - first, "chunk": min(cfg["chunk"], SERVE_MAX_CHUNK), "spin_capacity": spin_capacity}, sigs
 
 
 def run_served_mix(subs, mix, cfg, rate, seed=3, form="bar"):

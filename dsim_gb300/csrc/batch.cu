@@ -1630,10 +1630,11 @@ int dsim_batch_compact(dsim_batch* b) {
     return kOk;
 }
 
-// Autotuner: times `trialSteps` steps of the current jobs for each candidate
-// (step-kernel occupancy x chunk length x fine-grid cells per reference cell
-// edge of every mesh substrate) from a snapshot of the spin state, restores
-// the snapshot and keeps the fastest configuration.
+// Autotuner: times the same max(trialSteps, 1000) steps (a multiple of every
+// candidate chunk) of the current jobs for each candidate (step-kernel
+// occupancy x chunk length x fine-grid cells per reference cell edge of every
+// mesh substrate) from a snapshot of the spin state, restores the snapshot and
+// keeps the fastest configuration.
 int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], float* bestMs) {
     if (!b || !best || trialSteps == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: bad argument"); return kErrInvalid; }
     if (b->N == 0) { set_last_error(kErrInvalid, "dsim_batch_autotune: no jobs"); return kErrInvalid; }
@@ -1679,7 +1680,9 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
     // fine-grid resolutions: cells per reference-cell edge x 2
     const uint32_t gridHalves[] = {2, 3, 4, 5};  // 1, 1.5, 2, 2.5 fine cells per reference cell
     const uint32_t occs[] = {4, 6, 8};
-    const uint32_t chunks[] = {20, 40, 100, 200};
+    const uint32_t chunks[] = {20, 40, 100, 200, 500, 1000};
+    // the same steps for every candidate (a multiple of every chunk)
+    const uint32_t T = std::max<uint32_t>((trialSteps + 999u) / 1000u * 1000u, 1000u);
     bool haveMesh = false;
     for (auto* m : b->meshes) haveMesh |= (m != nullptr);
     cudaEvent_t e0, e1;
@@ -1710,12 +1713,12 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
                 b->occupancy = oc; b->chunk = ch; b->graphChunks = 0;
                 invalidate_graph(b);
                 cudaEventRecord(e0, b->st);
-                if ((rc = dsim_batch_advance(b, trialSteps))) break;
+                if ((rc = dsim_batch_advance(b, T))) break;
                 cudaEventRecord(e1, b->st);
                 if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
                 float ms = 0.0f;
                 cudaEventElapsedTime(&ms, e0, e1);
-                ms *= (float)trialSteps / (float)(((trialSteps + ch - 1) / ch) * ch);  // per requested step
+                ms *= (float)trialSteps / (float)T;  // per trialSteps steps
                 if (ms < bestT) { bestT = ms; bg = haveMesh ? gridHalves[gi] : 0; bo = oc; bc = ch; }
             }
             if (rc || e != cudaSuccess) break;

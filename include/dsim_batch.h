@@ -135,13 +135,15 @@ uint32_t dsim_batch_status(dsim_batch* b);
 /* drop finished jobs whose results were read and repack the others */
 int dsim_batch_retire(dsim_batch* b, uint32_t jobId);
 int dsim_batch_compact(dsim_batch* b);
-/* Autotuner: runs trialSteps steps of the current jobs from a snapshot of the
+/* Autotuner: runs the current jobs from a snapshot of the
  * spin state for every candidate -- step-kernel occupancy {4, 6, 8} x chunk
- * {20, 40, 100, 200} x fine-grid cells per reference-cell edge {1, 1.5, 2, 2.5}
+ * {20, 40, 100, 200, 500, 1000} x fine-grid cells per reference-cell edge
+ * {1, 1.5, 2, 2.5}; every candidate runs the same max(trialSteps, 1000) steps,
+ * so longer chunks are not favoured by jobs finishing inside the trial
  * (every mesh substrate's fine grid is rebuilt; meshes must not be in use
  * elsewhere meanwhile) -- restores the snapshot and keeps the fastest.
  * best = {occupancy, chunk, 2 x fine cells per reference cell edge (0: no
- * mesh)}, bestMs = its time for trialSteps steps. */
+ * mesh)}, bestMs = its time per trialSteps steps. */
 int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], float* bestMs);
 /* {packed spins, jobs, jobs running, device bytes, kernels launched, graph launches} */
 int dsim_batch_info(dsim_batch* b, uint64_t info[6]);
