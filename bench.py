@@ -386,6 +386,26 @@ def pinned_factory():
 
 
 # --------------------------------------------------------------------------
+def run_mix_only(args):
+    """--mix-only FORM: the 48-job mix of the forms leg in one batch, once, in
+    FORM ("fp32" or "bar"), configured by --mix-config (else autotuned); for
+    profiling the batch step kernels on their own."""
+    W = Workload(axons=args.axons, spins=4096, seed=1)
+    m = make_mesh(W)
+    subs, mix = build_mix(W, m, args.mix_jobs, 11, (4096, args.mix_max_spins),
+                          (args.mix_min_steps, args.mix_max_steps))
+    if args.mix_config:
+        cfg = {"occupancy": args.mix_config[0], "chunk": args.mix_config[1]}
+    else:
+        best, _ = tune_mix(subs, mix)
+        cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+    work = sum(j["n"] * j["steps"] for j in mix)
+    el, sigs, info, st = run_batched_mix(subs, mix, cfg, form=args.mix_only)
+    return {"metric": "spin-steps/s", "value": work / el, "unit": "spin-steps/s", "form": args.mix_only,
+            "config": dict(cfg, jobs=len(mix), spin_steps=work), "seconds": el, "kernel_launches": info["launches"],
+            "status": st}
+
+
 def run_ours(args, rank, world):
     from dsim_gb300.engine import DeviceInfo, Spins, mesh_run
     dev = DeviceInfo()
@@ -1444,6 +1464,8 @@ def main():
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
     ap.add_argument("--c5-full", action="store_true",
                     help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
+    ap.add_argument("--mix-only", choices=["fp32", "bar"], default=None,
+                    help="only run the 48-job mix once in one batch in this form (for profiling)")
     ap.add_argument("--c4-full", action="store_true",
                     help="also run the serving configuration at full size (--c4-jobs Poisson jobs of the full "
                          "batching ranges, permeable, 150 GB cap, at --c4-rates x the plain capacity)")
@@ -1465,7 +1487,10 @@ def main():
         import ctypes
         # one GPU per rank
         os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")
-    res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if args.mix_only:
+        res = run_mix_only(args) if rank == 0 else None
+    else:
+        res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
     if rank == 0 and res is not None:
         print(json.dumps(res))
     if world > 1:
