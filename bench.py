@@ -679,12 +679,15 @@ def build_mix(W, m, n_jobs, seed, spins_range, steps_range, permeable=False, sub
 def _submit_kw(j, form="fp32"):
     """Job keywords; form "fp32": the plain FP32 step with Kahan moments;
     "bar": the forms that hold the 1e-3 signal-error bar (mesh jobs
-    and cylinder jobs in the cell-local form, DSIM_JOB_LOCAL)."""
+    and cylinder jobs in the cell-local form, DSIM_JOB_LOCAL); "fp64": the
+    step in FP64 (DSIM_JOB_PRECISE)."""
     kw = dict(steps=j["steps"], dt=j["dt"], step_sd=j["step_sd"], T2=j["T2"], phase_constant=j["phase_constant"],
               seed=j["seed"], permeability=j["permeability"], waveform="pgse", delta=j["delta"],
               Delta=j["Delta"], inner_radius_proportion=j["inner"])
     if form == "bar":
         kw.update(local=True)
+    elif form == "fp64":
+        kw.update(precise=True)
     return kw
 
 
@@ -1464,7 +1467,7 @@ def main():
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
     ap.add_argument("--c5-full", action="store_true",
                     help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
-    ap.add_argument("--mix-only", choices=["fp32", "bar"], default=None,
+    ap.add_argument("--mix-only", choices=["fp32", "bar", "fp64"], default=None,
                     help="only run the 48-job mix once in one batch in this form (for profiling)")
     ap.add_argument("--c4-full", action="store_true",
                     help="also run the serving configuration at full size (--c4-jobs Poisson jobs of the full "
