@@ -246,6 +246,7 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
 // near-degenerate intersections, Kahan moments.  Between chunks the position
 // is kept in the double fields as origin + offset; the float fields get its
 // rounded value (sort keys, float readers).
+template <int LAYOUT>
 __global__ void __launch_bounds__(kFlatThreads, 4)
 k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
                    const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
@@ -275,7 +276,8 @@ k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
         __syncwarp();
     }
     const JobDev& J = jobS[wi];
-    if (!(J.flags & DSIM_JOB_LOCAL) || subS[wi].kind != kSubMesh) return;  // warp-uniform
+    if (!(J.flags & DSIM_JOB_LOCAL) || subS[wi].kind != kSubMesh || subS[wi].acc.wide != (uint32_t)LAYOUT)
+        return;  // warp-uniform
     const uint32_t now = *stepNow;
     const uint32_t start = J.start, steps = J.steps;
     if (now < start || now - start >= steps) return;
@@ -327,7 +329,7 @@ k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
         const bool open = active;
         bool found;
         FastHit best;
-        local_round(H, Lw, g, acc, lane, open, gx, gy, gz, ox, oy, oz, px, py, pz, excluded, found, best, pc);
+        local_round<LAYOUT>(H, Lw, g, acc, lane, open, gx, gy, gz, ox, oy, oz, px, py, pz, excluded, found, best, pc);
         if (open) {
             bool finish = !found;
             if (found) {
@@ -805,13 +807,15 @@ int upload_jobs(dsim_batch* b) {
 }
 
 // which plain step instantiations a chunk launches: bit 1 / 2 for mesh jobs
-// on 32- / 64-byte fine-grid records, bit 3 for cylinder jobs
+// on 32- / 64-byte fine-grid records, bit 3 for cylinder jobs; bits 5 / 6 for
+// cell-local mesh jobs on 32- / 64-byte records
 uint32_t step_layouts(const dsim_batch* b) {
     uint32_t mask = 0;
     for (const auto& j : b->jobs) {
         const SubDev& s = b->subs[j.d.sub];
-        if (s.kind == kSubCyl) mask |= 1u << 3;
+        if (s.kind == kSubCyl) { if (!j.d.flags) mask |= 1u << 3; }
         else if (!j.d.flags) mask |= 1u << (s.acc.wide == 2 ? 2u : 1u);
+        else if (j.d.flags & DSIM_JOB_LOCAL) mask |= 1u << (s.acc.wide == 2 ? 6u : 5u);
     }
     return mask;
 }
@@ -820,8 +824,8 @@ uint32_t step_layouts(const dsim_batch* b) {
 // instantiations, advance
 uint64_t chunk_launches(const dsim_batch* b) {
     const uint32_t mask = step_layouts(b);
-    return 5ull + (uint64_t)__builtin_popcount(mask & 0xEu) + (b->anyPrecise ? 1ull : 0ull) +
-           (b->anyLocal ? 1ull : 0ull) + (b->anyPreciseCyl ? 1ull : 0ull) + (b->anyLocalCyl ? 1ull : 0ull) + 1ull;
+    return 5ull + (uint64_t)__builtin_popcount(mask & 0x6Eu) + (b->anyPrecise ? 1ull : 0ull) +
+           (b->anyPreciseCyl ? 1ull : 0ull) + (b->anyLocalCyl ? 1ull : 0ull) + 1ull;
 }
 
 // Precision-form cylinder jobs (DSIM_JOB_PRECISE): the dSim2 step of
@@ -1031,7 +1035,8 @@ int enqueue_chunk(dsim_batch* b) {
     int kinds[8], nk = 0;
     for (int L = 1; L <= 3; L++)
         if (mask & (1u << L)) kinds[nk++] = L;
-    if (b->anyLocal) kinds[nk++] = 4;
+    for (int L = 5; L <= 6; L++)
+        if (mask & (1u << L)) kinds[nk++] = 4 + 4 * (L - 5);  // 4, 8: cell-local mesh, 32- / 64-byte records
     if (b->anyPrecise) kinds[nk++] = 5;
     if (b->anyPreciseCyl) kinds[nk++] = 6;
     if (b->anyLocalCyl) kinds[nk++] = 7;
@@ -1045,8 +1050,12 @@ int enqueue_chunk(dsim_batch* b) {
             case 2: launch_step_layout<2>(b, grid, D, st); break;
             case 3: launch_step_layout<3>(b, grid, D, st); break;
             case 4:
-                k_batch_step_local<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                                  b->d_status, b->d_counts);
+                k_batch_step_local<1><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow,
+                                                                     b->chunk, b->d_status, b->d_counts);
+                break;
+            case 8:
+                k_batch_step_local<2><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow,
+                                                                     b->chunk, b->d_status, b->d_counts);
                 break;
             case 5:
                 k_batch_step64<<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,

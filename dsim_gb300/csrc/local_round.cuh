@@ -300,13 +300,15 @@ __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const 
 // One collision round of the local form for every lane of the warp (all 32
 // lanes call it).  The sub-segment o -> p is in the lane's local frame at
 // origin (gx, gy, gz); on return, for open lanes, found / best hold the
-// collision result with the hit point in the same frame.
+// collision result with the hit point in the same frame.  LAYOUT 1 or 2
+// compiles only the 32- or 64-byte record path; 0 dispatches on acc.wide.
+template <int LAYOUT = 0>
 __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, const AccelDev& acc,
                                             uint32_t lane, bool open, float gx, float gy, float gz, float ox,
                                             float oy, float oz, float px, float py, float pz, uint32_t excluded,
                                             bool& found, FastHit& best, PrecCount& pc) {
     const uint32_t FULL = 0xFFFFFFFFu;
-    const bool full = acc.wide == 2;
+    const bool full = LAYOUT == 0 ? acc.wide == 2 : LAYOUT == 2;  // LAYOUT 1 / 2: one record path compiled
     const float invLf = acc.invLf;
     const uint32_t nf = acc.nf;
     const float dx = px - ox, dy = py - oy, dz = pz - oz;
