@@ -348,8 +348,8 @@ k_batch_step_local(const SubDev* __restrict__ subs, const JobDev* __restrict__ j
                 if (ax > J.clampHi) px = J.clampHi - gx; else if (ax < J.clampLo) px = J.clampLo - gx;
                 if (ay > J.clampHi) py = J.clampHi - gy; else if (ay < J.clampLo) py = J.clampLo - gy;
                 if (az > J.clampHi) pz = J.clampHi - gz; else if (az < J.clampLo) pz = J.clampLo - gz;
-                const float sx = floorf(px * 16.0f) * kLatticeH, sy = floorf(py * 16.0f) * kLatticeH,
-                            sz = floorf(pz * 16.0f) * kLatticeH;
+                const float sx = floor_small(px * 16.0f) * kLatticeH, sy = floor_small(py * 16.0f) * kLatticeH,
+                            sz = floor_small(pz * 16.0f) * kLatticeH;
                 gx += sx; gy += sy; gz += sz;
                 x = px - sx; y = py - sy; z = pz - sz;
                 const float T2 = J.T2[comp & 3u];
@@ -966,8 +966,8 @@ k_batch_step_cyl_local(const SubDev* __restrict__ subs, const JobDev* __restrict
             if (G.x + px > clampHi) px = clampHi - G.x; else if (G.x + px < clampLo) px = clampLo - G.x;
             if (G.y + py > clampHi) py = clampHi - G.y; else if (G.y + py < clampLo) py = clampLo - G.y;
             if (G.z + pz > clampHi) pz = clampHi - G.z; else if (G.z + pz < clampLo) pz = clampLo - G.z;
-            const float sx = floorf(px * 16.0f) * kLatticeH, sy = floorf(py * 16.0f) * kLatticeH,
-                        sz = floorf(pz * 16.0f) * kLatticeH;
+            const float sx = floor_small(px * 16.0f) * kLatticeH, sy = floor_small(py * 16.0f) * kLatticeH,
+                        sz = floor_small(pz * 16.0f) * kLatticeH;
             G.x += sx; G.y += sy; G.z += sz;
             x = px - sx; y = py - sy; z = pz - sz;
             const float T2 = __ldg(&J.T2[imo < 3 ? imo : 2]);

@@ -62,6 +62,22 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, ui
     return c;
 }
 
+#if defined(__CUDACC__)
+// floorf(t) for |t| < 2^22 on the FP32 pipe, without a rounding or
+// conversion instruction: adding and subtracting 1.5 * 2^23 rounds t to an
+// integer (the sum's ulp is 1), and a step down undoes rounding up.  The same
+// value as floorf (a zero result is +0).
+__device__ __forceinline__ float floor_small(float t) {
+    const float r = __fsub_rn(__fadd_rn(t, 12582912.0f), 12582912.0f);
+    return r > t ? __fsub_rn(r, 1.0f) : r;
+}
+// (uint32_t)f for an integer-valued f in [0, 2^23): f + 2^23 holds f in its
+// significand.
+__device__ __forceinline__ uint32_t uint_small(float f) {
+    return __float_as_uint(__fadd_rn(f, 8388608.0f)) - 0x4B000000u;
+}
+#endif
+
 // One step's draws for one spin: counter = (spin, step lo, step hi, stream),
 // key = 64-bit job seed.  The four words map to the reference's myRandn
 // layout (dSim3/src/spinKernelCpu.cpp:53-63): Box-Muller on (u1,u2) gives

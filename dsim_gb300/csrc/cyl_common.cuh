@@ -13,14 +13,17 @@ namespace dsim {
 // multiplies by the reciprocal; clamping happens in the hash.
 __device__ __forceinline__ uint32_t cyl_cell(float px, float py, float pz, float L, uint32_t n) {
     float inv = 1.0f / L;
-    float cx = floorf((px + 1.0f) * inv);
-    float cy = floorf((py + 1.0f) * inv);
-    float cz = floorf((pz + 1.0f) * inv);
+    float cx = floor_small((px + 1.0f) * inv);
+    float cy = floor_small((py + 1.0f) * inv);
+    float cz = floor_small((pz + 1.0f) * inv);
     float hi = (float)(n - 1);
     cx = fmaxf(fminf(cx, hi), 0.0f);
     cy = fmaxf(fminf(cy, hi), 0.0f);
     cz = fmaxf(fminf(cz, hi), 0.0f);
-    return (uint32_t)((int)((float)(n * n) * cz) + (int)((float)n * cy) + (int)cx);
+    // the reference's float products (float)(n*n) * cz etc. are exact integers
+    // while n^3 < 2^24 (its grid has at most 100 cells per axis), so integer
+    // arithmetic gives the same index
+    return n * n * uint_small(cz) + n * uint_small(cy) + uint_small(cx);
 }
 
 __device__ __forceinline__ float cyl_dist_sq(float px, float py, float pz, float4 f) {
@@ -35,10 +38,10 @@ __device__ __forceinline__ uint32_t cyl_fine_cell(const CylDev& g, float px, flo
     const uint32_t n = g.n, k = g.fineK, nk = n * k;
     const uint32_t cx = cube % n, cy = (cube / n) % n, cz = cube / (n * n);
     const float hi = (float)(k - 1);
-    const float sx = fminf(fmaxf(floorf((px + 1.0f) * g.fineInv) - (float)(cx * k), 0.0f), hi);
-    const float sy = fminf(fmaxf(floorf((py + 1.0f) * g.fineInv) - (float)(cy * k), 0.0f), hi);
-    const float sz = fminf(fmaxf(floorf((pz + 1.0f) * g.fineInv) - (float)(cz * k), 0.0f), hi);
-    return ((cz * k + (uint32_t)sz) * nk + (cy * k + (uint32_t)sy)) * nk + cx * k + (uint32_t)sx;
+    const float sx = fminf(fmaxf(floor_small((px + 1.0f) * g.fineInv) - (float)(cx * k), 0.0f), hi);
+    const float sy = fminf(fmaxf(floor_small((py + 1.0f) * g.fineInv) - (float)(cy * k), 0.0f), hi);
+    const float sz = fminf(fmaxf(floor_small((pz + 1.0f) * g.fineInv) - (float)(cz * k), 0.0f), hi);
+    return ((cz * k + uint_small(sz)) * nk + (cy * k + uint_small(sy))) * nk + cx * k + uint_small(sx);
 }
 
 // One list entry (fiber record f, list position j) of the first pass of a

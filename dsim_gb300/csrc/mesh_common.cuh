@@ -8,10 +8,13 @@
 
 namespace dsim {
 
+// the fine-grid coordinate of p: floor((p + 1) / Lf) clamped to [0, nf - 1]
+// (floor_small / uint_small: the values of floorf and the conversion, on the
+// FP32 pipe)
 __device__ __forceinline__ uint32_t fine_coord(float p, float invLf, uint32_t nf) {
-    float f = floorf((p + 1.0f) * invLf);
+    float f = floor_small((p + 1.0f) * invLf);
     f = fminf(fmaxf(f, 0.0f), (float)(nf - 1));
-    return (uint32_t)f;
+    return uint_small(f);
 }
 
 __host__ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
