@@ -31,9 +31,11 @@ static constexpr uint32_t kLocalRefine = 0x100u;  // hit type flag: point from F
 
 // per-warp table of the local form: each owner's lattice origin and the queue
 // of records past the plane test
+// record queue: at most 31 left over + both records of 32 lanes appended
+static constexpr uint32_t kLocalQueue = 96;
 struct LocalWarp {
     float gx[32], gy[32], gz[32];
-    uint32_t qe[kPrecQueue], qo[kPrecQueue];  // records past the plane test
+    uint32_t qe[kLocalQueue], qo[kLocalQueue];  // records past the plane test
     uint32_t ft[kPrecQueue], fo[kPrecQueue];  // (triangle, owner) pairs for the FP64 re-test
 };
 
@@ -252,16 +254,10 @@ __device__ __forceinline__ bool local_test_tri(const FlatWarp& H, const LocalWar
 
 // appends the lanes' deferred (t, o) to the FP64 queue (fn: warp-uniform
 // length) and re-tests full groups of 32 in FP64; all lanes call it
-__device__ __forceinline__ void local_enqueue64(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, uint32_t lane,
-                                                uint32_t t, uint32_t o, uint32_t& fn, PrecCount& pc) {
-    const bool live = t != 0xFFFFFFFFu;
-    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
-    if (live) {
-        const uint32_t at = fn + __popc(b & ((1u << lane) - 1u));
-        Lw.ft[at] = t; Lw.fo[at] = o;
-    }
-    fn += __popc(b);
-    __syncwarp();
+// full groups of 32 from the top of the FP64 queue (rare within a round: out
+// of line, so the record loop's code stays small)
+__device__ __noinline__ void local_flush64(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, uint32_t lane, uint32_t& fn,
+                                           PrecCount& pc) {
     while (fn >= 32) {
         const uint32_t at = fn - 32 + lane;
         const uint32_t tq = Lw.ft[at], oq = Lw.fo[at];
@@ -272,18 +268,38 @@ __device__ __forceinline__ void local_enqueue64(FlatWarp& H, LocalWarp& Lw, cons
     }
 }
 
+__device__ __forceinline__ void local_enqueue64(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, uint32_t lane,
+                                                uint32_t t, uint32_t o, uint32_t& fn, PrecCount& pc) {
+    const bool live = t != 0xFFFFFFFFu;
+    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
+    if (live) {
+        const uint32_t at = fn + __popc(b & ((1u << lane) - 1u));
+        Lw.ft[at] = t; Lw.fo[at] = o;
+    }
+    fn += __popc(b);
+    __syncwarp();
+    if (fn >= 32) local_flush64(H, Lw, g, lane, fn, pc);
+}
+
 // appends the lanes' surviving (k, o) to the warp's queue (qn: warp-uniform
 // length) and tests full groups of 32 from its top, their near cases going to
 // the FP64 queue; all lanes call it
 __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, const AccelDev& acc,
-                                              bool full, uint32_t lane, bool live, uint32_t k, uint32_t o,
-                                              uint32_t& qn, uint32_t& fn, PrecCount& pc) {
-    const uint32_t b = __ballot_sync(0xFFFFFFFFu, live);
-    if (live) {
-        const uint32_t at = qn + __popc(b & ((1u << lane) - 1u));
-        Lw.qe[at] = k; Lw.qo[at] = o;
+                                              bool full, uint32_t lane, bool live0, uint32_t k0, uint32_t o0,
+                                              bool live1, uint32_t k1, uint32_t o1, uint32_t& qn, uint32_t& fn,
+                                              PrecCount& pc) {
+    // both records of the lane's pair in one append (one copy of the test below)
+    const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, live0), b1 = __ballot_sync(0xFFFFFFFFu, live1);
+    const uint32_t below = (1u << lane) - 1u;
+    if (live0) {
+        const uint32_t at = qn + __popc(b0 & below);
+        Lw.qe[at] = k0; Lw.qo[at] = o0;
     }
-    qn += __popc(b);
+    if (live1) {
+        const uint32_t at = qn + __popc(b0) + __popc(b1 & below);
+        Lw.qe[at] = k1; Lw.qo[at] = o1;
+    }
+    qn += __popc(b0) + __popc(b1);
     __syncwarp();
     while (qn >= 32) {
         const uint32_t at = qn - 32 + lane;
@@ -377,8 +393,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
                 pc.records++;
                 s1 = t != H.excl[o1] && local_plane(H, Lw, q, o1);
             }
-            local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, qn, fn, pc);
-            local_enqueue(H, Lw, g, acc, full, lane, s1, e1, o1, qn, fn, pc);
+            local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, s1, e1, o1, qn, fn, pc);
         }
     }
     {
