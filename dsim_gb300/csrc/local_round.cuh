@@ -313,6 +313,63 @@ __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const 
     }
 }
 
+// The rare paths of a round, out of line so that the record loop's code stays
+// small (each holds its own copy of the exact test and the FP64 re-test).
+// A lane whose cell box is too large for the warp's flattened pass: its own
+// records, cell by cell.
+__device__ __noinline__ void local_solo(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, const AccelDev& acc, bool full,
+                                        uint32_t lane, uint32_t lo0, uint32_t lo1, uint32_t lo2, uint32_t w1,
+                                        uint32_t w2, uint32_t nc, uint32_t excluded, PrecCount& pc) {
+    for (uint32_t q = 0; q < nc; q++) {
+        const uint32_t iz = q % w2, r = q / w2, iy = r % w1, ix = r / w1;
+        const uint32_t key = morton3(lo0 + ix, lo1 + iy, lo2 + iz);
+        const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
+        for (uint32_t k = b0; k < b1; k++) {
+            float4 qq; float3 p1; uint32_t t;
+            record_load(acc, k, full, qq, p1, t);
+            pc.records++;
+            if (t == excluded || !local_plane(H, Lw, qq, lane)) continue;
+            FastHit h;
+            if (local_test(H, Lw, g, acc, k, full, lane, h, pc)) flat_file_hit(H, lane, h);
+        }
+    }
+}
+
+// A lane whose hit slots overflowed: every triangle of the reference cells
+// from the start cell s towards the end cell t, in order, stopping at the
+// first cell with a hit (the reference's cell walk); returns found.
+__device__ __noinline__ bool local_overflow(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, uint32_t lane, uint32_t sx,
+                                            uint32_t sy, uint32_t sz, uint32_t tx, uint32_t ty, uint32_t tz,
+                                            uint32_t ix, uint32_t iy, uint32_t iz, uint32_t excluded, FastHit& best,
+                                            PrecCount& pc) {
+    const uint32_t gn = g.n;
+    bool found = false;
+    uint32_t cx = sx;
+    do {
+        uint32_t cy = sy;
+        do {
+            uint32_t cz = sz;
+            do {
+                const uint32_t c = gn * gn * cz + gn * cy + cx;
+                const uint32_t c0 = __ldg(g.cell_start + c), c1 = __ldg(g.cell_start + c + 1);
+                float bd2 = 400000000.0f;
+                for (uint32_t k = c0; k < c1; k++) {
+                    const uint32_t t = __ldg(g.cell_tri + k);
+                    if (t == excluded) continue;
+                    FastHit h;
+                    if (local_test_tri(H, Lw, g, t, lane, h, pc) && h.d2 < bd2) {
+                        bd2 = h.d2; best = h; found = true;
+                    }
+                }
+                cz += iz;
+            } while ((cz != tz + iz) && !found);
+            cy += iy;
+        } while ((cy != ty + iy) && !found);
+        cx += ix;
+    } while ((cx != tx + ix) && !found);
+    return found;
+}
+
 // One collision round of the local form for every lane of the warp (all 32
 // lanes call it).  The sub-segment o -> p is in the lane's local frame at
 // origin (gx, gy, gz); on return, for open lanes, found / best hold the
@@ -405,21 +462,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
         local_enqueue64(H, Lw, g, lane, (lane < qn) ? tdef : 0xFFFFFFFFu, oq, fn, pc);
         if (lane < fn && local_fp64(H, Lw, g, Lw.ft[lane], Lw.fo[lane], h, pc)) flat_file_hit(H, Lw.fo[lane], h);
     }
-    if (solo) {
-        for (uint32_t q = 0; q < nc; q++) {
-            const uint32_t iz = q % w2, r = q / w2, iy = r % w1, ix = r / w1;
-            const uint32_t key = morton3(lo0 + ix, lo1 + iy, lo2 + iz);
-            const uint32_t b0 = __ldg(acc.start + key), b1 = __ldg(acc.start + key + 1);
-            for (uint32_t k = b0; k < b1; k++) {
-                float4 qq; float3 p1; uint32_t t;
-                record_load(acc, k, full, qq, p1, t);
-                pc.records++;
-                if (t == excluded || !local_plane(H, Lw, qq, lane)) continue;
-                FastHit h;
-                if (local_test(H, Lw, g, acc, k, full, lane, h, pc)) flat_file_hit(H, lane, h);
-            }
-        }
-    }
+    if (solo) local_solo(H, Lw, g, acc, full, lane, lo0, lo1, lo2, w1, w2, nc, excluded, pc);
     __syncwarp();
     found = false;
     if (!open) return;
@@ -432,30 +475,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
     const uint32_t iy = (uint32_t)((int)(ty > sy) - (int)(ty < sy));
     const uint32_t iz = (uint32_t)((int)(tz > sz) - (int)(tz < sz));
     if (n > (uint32_t)kFlatSlots) {
-        // slots overflowed: every triangle of the reference cells in order
-        uint32_t cx = sx;
-        do {
-            uint32_t cy = sy;
-            do {
-                uint32_t cz = sz;
-                do {
-                    const uint32_t c = gn * gn * cz + gn * cy + cx;
-                    const uint32_t c0 = __ldg(g.cell_start + c), c1 = __ldg(g.cell_start + c + 1);
-                    float bd2 = 400000000.0f;
-                    for (uint32_t k = c0; k < c1; k++) {
-                        const uint32_t t = __ldg(g.cell_tri + k);
-                        if (t == excluded) continue;
-                        FastHit h;
-                        if (local_test_tri(H, Lw, g, t, lane, h, pc) && h.d2 < bd2) {
-                            bd2 = h.d2; best = h; found = true;
-                        }
-                    }
-                    cz += iz;
-                } while ((cz != tz + iz) && !found);
-                cy += iy;
-            } while ((cy != ty + iy) && !found);
-            cx += ix;
-        } while ((cx != tx + ix) && !found);
+        found = local_overflow(H, Lw, g, lane, sx, sy, sz, tx, ty, tz, ix, iy, iz, excluded, best, pc);
         if (found) local_refine(g, gx, gy, gz, ox, oy, oz, dx, dy, dz, best);
         return;
     }
