@@ -287,8 +287,10 @@ __device__ __forceinline__ void local_enqueue64(FlatWarp& H, LocalWarp& Lw, cons
 __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const MeshDev& g, const AccelDev& acc,
                                               bool full, uint32_t lane, bool live0, uint32_t k0, uint32_t o0,
                                               bool live1, uint32_t k1, uint32_t o1, uint32_t& qn, uint32_t& fn,
-                                              PrecCount& pc) {
-    // both records of the lane's pair in one append (one copy of the test below)
+                                              PrecCount& pc, bool last) {
+    // both records of the lane's pair in one append (one copy of the test
+    // below); `last` (warp-uniform, after the last records) also tests the
+    // partial group left at the bottom of the queue
     const uint32_t b0 = __ballot_sync(0xFFFFFFFFu, live0), b1 = __ballot_sync(0xFFFFFFFFu, live1);
     const uint32_t below = (1u << lane) - 1u;
     if (live0) {
@@ -301,15 +303,17 @@ __device__ __forceinline__ void local_enqueue(FlatWarp& H, LocalWarp& Lw, const 
     }
     qn += __popc(b0) + __popc(b1);
     __syncwarp();
-    while (qn >= 32) {
-        const uint32_t at = qn - 32 + lane;
+    while (qn >= 32 || (last && qn > 0)) {
+        const uint32_t cnt = min(qn, 32u);
+        const bool act = lane < cnt;
+        const uint32_t at = qn - cnt + (act ? lane : 0u);
         const uint32_t kq = Lw.qe[at], oq = Lw.qo[at];
         __syncwarp();
-        qn -= 32;
+        qn -= cnt;
         FastHit h;
-        uint32_t tdef;
-        if (local_test_defer(H, Lw, g, acc, kq, full, oq, h, pc, tdef)) flat_file_hit(H, oq, h);
-        local_enqueue64(H, Lw, g, lane, tdef, oq, fn, pc);
+        uint32_t tdef = 0xFFFFFFFFu;
+        if (act && local_test_defer(H, Lw, g, acc, kq, full, oq, h, pc, tdef)) flat_file_hit(H, oq, h);
+        local_enqueue64(H, Lw, g, lane, act ? tdef : 0xFFFFFFFFu, oq, fn, pc);
     }
 }
 
@@ -412,32 +416,42 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
     const uint32_t itotal = __shfl_sync(FULL, iincl, 31);
     uint32_t qn = 0, fn = 0;  // queue lengths (warp-uniform)
     __syncwarp();
-    for (uint32_t ib = 0; ib < itotal; ib += 32) {
-        const uint32_t m = ib + lane;
-        const uint32_t ow = min(warp_find(iincl, m), 31u);
-        const uint32_t ofs = __shfl_sync(FULL, iexcl, ow);
-        uint32_t b0 = 0, cnt = 0;
-        if (m < itotal) {
-            const uint32_t q = m - ofs;
-            const uint32_t wd = H.wd[ow], bx = H.box[ow];
-            const uint32_t ww1 = (wd >> 8) & 0xFFu, ww2 = wd >> 16;
-            const uint32_t iz = q % ww2, r = q / ww2, iy = r % ww1, ix = r / ww1;
-            const uint32_t key = morton3((bx & 1023u) + ix, ((bx >> 10) & 1023u) + iy, (bx >> 20) + iz);
-            b0 = __ldg(acc.start + key);
-            cnt = __ldg(acc.start + key + 1) - b0;
+    // the warp's records pair by pair, item block after item block, and then
+    // one last pass that tests the record queue's partial group: one inlined
+    // copy of the exact test for the whole round
+    uint32_t ib = 0, rb = 0, rtotal = 0, rincl = 0, rbase = 0, ow = 0;
+    for (;;) {
+        while (rb >= rtotal && ib < itotal) {  // warp-uniform
+            const uint32_t m = ib + lane;
+            ow = min(warp_find(iincl, m), 31u);
+            const uint32_t ofs = __shfl_sync(FULL, iexcl, ow);
+            uint32_t b0 = 0, cnt = 0;
+            if (m < itotal) {
+                const uint32_t q = m - ofs;
+                const uint32_t wd = H.wd[ow], bx = H.box[ow];
+                const uint32_t ww1 = (wd >> 8) & 0xFFu, ww2 = wd >> 16;
+                const uint32_t iz = q % ww2, r = q / ww2, iy = r % ww1, ix = r / ww1;
+                const uint32_t key = morton3((bx & 1023u) + ix, ((bx >> 10) & 1023u) + iy, (bx >> 20) + iz);
+                b0 = __ldg(acc.start + key);
+                cnt = __ldg(acc.start + key + 1) - b0;
+            }
+            rincl = warp_incl_scan(cnt, lane);
+            rtotal = __shfl_sync(FULL, rincl, 31);
+            rbase = b0 - (rincl - cnt);
+            rb = 0;
+            ib += 32;
         }
-        const uint32_t rincl = warp_incl_scan(cnt, lane);
-        const uint32_t rtotal = __shfl_sync(FULL, rincl, 31);
-        const uint32_t rbase = b0 - (rincl - cnt);
-        for (uint32_t rb = 0; rb < rtotal; rb += 64) {
+        const bool more = rb < rtotal;  // warp-uniform
+        bool s0 = false, s1 = false;
+        uint32_t e0 = 0, e1 = 0, o0 = 0, o1 = 0;
+        if (more) {
             const uint32_t r0 = rb + lane, r1 = rb + 32 + lane;
             const uint32_t j0 = min(warp_find(rincl, r0), 31u);
             const uint32_t j1 = min(warp_find(rincl, r1), 31u);
-            const uint32_t e0 = __shfl_sync(FULL, rbase, j0) + r0;
-            const uint32_t e1 = __shfl_sync(FULL, rbase, j1) + r1;
-            const uint32_t o0 = __shfl_sync(FULL, ow, j0);
-            const uint32_t o1 = __shfl_sync(FULL, ow, j1);
-            bool s0 = false, s1 = false;
+            e0 = __shfl_sync(FULL, rbase, j0) + r0;
+            e1 = __shfl_sync(FULL, rbase, j1) + r1;
+            o0 = __shfl_sync(FULL, ow, j0);
+            o1 = __shfl_sync(FULL, ow, j1);
             if (r0 < rtotal) {
                 float4 q; float3 p1; uint32_t t;
                 record_load(acc, e0, full, q, p1, t);
@@ -450,16 +464,14 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
                 pc.records++;
                 s1 = t != H.excl[o1] && local_plane(H, Lw, q, o1);
             }
-            local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, s1, e1, o1, qn, fn, pc);
+            rb += 64;
         }
+        local_enqueue(H, Lw, g, acc, full, lane, s0, e0, o0, s1, e1, o1, qn, fn, pc, !more);
+        if (!more) break;
     }
     {
-        // the record queue's remainder, then the FP64 queue's
+        // the FP64 queue's remainder
         FastHit h;
-        uint32_t tdef = 0xFFFFFFFFu;
-        const uint32_t oq = Lw.qo[lane];
-        if (lane < qn && local_test_defer(H, Lw, g, acc, Lw.qe[lane], full, oq, h, pc, tdef)) flat_file_hit(H, oq, h);
-        local_enqueue64(H, Lw, g, lane, (lane < qn) ? tdef : 0xFFFFFFFFu, oq, fn, pc);
         if (lane < fn && local_fp64(H, Lw, g, Lw.ft[lane], Lw.fo[lane], h, pc)) flat_file_hit(H, Lw.fo[lane], h);
     }
     if (solo) local_solo(H, Lw, g, acc, full, lane, lo0, lo1, lo2, w1, w2, nc, excluded, pc);
