@@ -508,7 +508,7 @@ __device__ __forceinline__ void local_round(FlatWarp& H, LocalWarp& Lw, const Me
                 for (uint32_t q = 0; q < (uint32_t)kFlatSlots; q++) {
                     if (q >= n) break;
                     const uint32_t t = H.t[q][lane];
-                    if (!hit_in_cell(g, hc[q], c, t)) continue;
+                    if (!hit_in_cell_compact(g, hc[q], c, t)) continue;
                     const float d2 = H.d2[q][lane];
                     if (!found || d2 < H.d2[bq][lane] || (d2 == H.d2[bq][lane] && t < H.t[bq][lane])) {
                         bq = q;
