@@ -5,9 +5,10 @@
   libdsim2.so       dSim2 plugin boundary (include/dsim2_abi.h)
 
 Translation units are compiled in parallel with nvcc; objects are reused when
-they are newer than their sources and headers.  The step kernels (mesh.cu,
-cyl.cu) are compiled with -fmad=false so that each float operation rounds as
-in the reference's CPU build; host code is compiled with -ffp-contract=off.
+they are newer than their sources and headers.  The units holding step and
+grid kernels (EXACT below) are compiled with -fmad=false, IEEE division and
+square root and no flush to zero, so that each float operation rounds as in
+the reference's CPU build; host code is compiled with -ffp-contract=off.
 """
 import os
 import subprocess
@@ -61,8 +62,6 @@ def _compile(unit, verbose=False):
         return obj, None
     cmd = [nvcc(), "-c", src, "-o", obj + ".tmp", "-O3", "-std=c++17", "-lineinfo",
            "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-I", SRC, "-I", INC] + ARCH
-    if unit.endswith(".cpp"):
-        cmd += ["-x", "cu"] if False else []
     if unit in EXACT:
         cmd += ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
     if verbose:
