@@ -305,11 +305,19 @@ int dsim_server_submit(dsim_server* s, const dsim_job_desc* d, const float* pos3
     r->nG = nG;
     r->footprint = footprint(*d, nG);
     const uint64_t pad = (d->nSpins + 31u) & ~31u;
-    if (pad > s->spinCap || s->hbmSubs + r->footprint > s->hbmCap) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    // a job that cannot fit even with no other job admitted would wait
+    // forever: refused here (a precision-form job also needs the FP64 arena
+    // and its mesh's FP64 triangle table, unless they are held already)
+    uint64_t need = s->hbmSubs + r->footprint;
+    if (d->flags & (DSIM_JOB_PRECISE | DSIM_JOB_LOCAL)) {
+        if (!s->fp64Arena) need += s->spinCap * 64;
+        if (!s->tri64Held[d->substrate]) need += s->tri64Bytes[d->substrate];
+    }
+    if (pad > s->spinCap || need > s->hbmCap) {
         set_last_error(kErrTooLarge, "dsim_server_submit: job of %u spins never fits the arena or the HBM cap", d->nSpins);
         return kErrTooLarge;
     }
-    std::lock_guard<std::mutex> lk(s->mu);
     r->tSubmit = s->started ? s->now() : 0.0;
     *ticket = (uint32_t)s->reqs.size();
     s->reqs.push_back(std::move(r));

@@ -115,3 +115,51 @@ def test_autotune_restores_state(engine, tmp_path):
     for a, w in zip(got, want):
         assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(w).view(np.uint8))
     b.close()
+
+
+def test_admission_counts_the_precision_forms_device_memory(engine, tmp_path):
+    """The HBM cap counts, from the first job of a precision form on, the
+    arena's FP64 fields (64 B per spin slot) and that mesh's FP64 triangle
+    table (128 B per triangle): a cell-local job that can never fit under the
+    cap with them is refused at submission (instead of waiting forever), the
+    same job in the plain form is served, and the peak admitted bytes of a
+    served cell-local job include them."""
+    from dsim_gb300.engine import Mesh, Server
+    am, gl, cy, jobs, grads = _jobs(tmp_path)
+    m = Mesh.load(am.path, am.spaceScale)
+    sub, kw, n = jobs[0]
+    kw = dict(kw)
+    pos, comp, fib = kw.pop("pos"), kw.pop("comp"), kw.pop("fiber")
+    cap_slots = 1 << 14
+    probe = Server(spin_capacity=cap_slots, job_capacity=2, hbm_cap=64e9)
+    sid = probe.add_mesh(m)
+    probe.configure(chunk=10, occupancy=4, graph_chunks=2)
+    probe.start()
+    t = probe.submit(sid, pos, comp, fib, grads, **kw)
+    probe.drain()
+    plain_peak = probe.stats()["hbm_peak"]
+    probe.stop()
+    probe.close()
+    # a cap just above the plain job's peak: the plain job is served, the cell-local one refused
+    srv = Server(spin_capacity=cap_slots, job_capacity=2, hbm_cap=plain_peak + 1024)
+    sid = srv.add_mesh(m)
+    srv.configure(chunk=10, occupancy=4, graph_chunks=2)
+    srv.start()
+    with pytest.raises(Exception):
+        srv.submit(sid, pos, comp, fib, grads, local=True, **kw)
+    t = srv.submit(sid, pos, comp, fib, grads, **kw)
+    srv.drain()
+    assert srv.poll(t)[0] and srv.stats()["errors"] == 0
+    srv.stop()
+    srv.close()
+    # with room, the cell-local job's peak includes the arena's FP64 fields
+    srv = Server(spin_capacity=cap_slots, job_capacity=2, hbm_cap=64e9)
+    sid = srv.add_mesh(m)
+    srv.configure(chunk=10, occupancy=4, graph_chunks=2)
+    srv.start()
+    t = srv.submit(sid, pos, comp, fib, grads, local=True, **kw)
+    srv.drain()
+    assert srv.poll(t)[0]
+    assert srv.stats()["hbm_peak"] >= plain_peak + cap_slots * 64
+    srv.stop()
+    srv.close()
