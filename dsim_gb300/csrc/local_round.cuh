@@ -124,7 +124,7 @@ __device__ __forceinline__ bool local_test_core(const FlatWarp& H, const LocalWa
         near = (s <= kLocalEpsST) | (tt <= kLocalEpsST) | (s + tt >= 1.0f - kLocalEpsST);
         if (!near) {
             // FP32 point for choosing the nearest hit; the chosen one gets its
-            // point again from FP64 (local_refine)
+            // point again in float-float arithmetic (local_refine)
             h.t = t;
             h.x = ox + dx * r; h.y = oy + dy * r; h.z = oz + dz * r;
             h.d2 = (ox - h.x) * (ox - h.x) + (oy - h.y) * (oy - h.y) + (oz - h.z) * (oz - h.z);
