@@ -515,7 +515,9 @@ def run_ours(args, rank, world):
         res["forms"] = run_forms(args, W, m)
     if rank == 0 and not args.no_precision:
         res["precision"] = run_precision(args, W, m)
-    if rank == 0 and args.c5_full:
+    # the precision configuration at full size runs by default on one GPU
+    # (about two minutes: 1M spins x 20,000 steps x 3 waveforms in each form)
+    if rank == 0 and (args.c5_full or (world == 1 and not args.no_c5_full)):
         res["precision_full"] = run_precision_full(args, W, m)
     if rank == 0 and args.c4_full:
         res["serving_full"] = run_c4_full(args, W, m)
@@ -1465,6 +1467,8 @@ def main():
     ap.add_argument("--c5-steps", type=int, default=20000)
     ap.add_argument("--c5-sample", type=int, default=512)
     ap.add_argument("--c5-rate-steps", type=int, default=2000)
+    ap.add_argument("--no-c5-full", action="store_true",
+                    help="skip the full-size precision comparison that a one-GPU run does by default")
     ap.add_argument("--c5-full", action="store_true",
                     help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
     ap.add_argument("--mix-only", choices=["fp32", "bar", "fp64"], default=None,
