@@ -395,10 +395,10 @@ def run_mix_only(args):
     subs, mix = build_mix(W, m, args.mix_jobs, 11, (4096, args.mix_max_spins),
                           (args.mix_min_steps, args.mix_max_steps))
     if args.mix_config:
-        cfg = {"occupancy": args.mix_config[0], "chunk": args.mix_config[1]}
+        cfg = {"occupancy": args.mix_config[0], "chunk": args.mix_config[1], "block": args.mix_block}
     else:
         best, _ = tune_mix(subs, mix)
-        cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+        cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"], "block": best.get("block")}
     work = sum(j["n"] * j["steps"] for j in mix)
     el, sigs, info, st = run_batched_mix(subs, mix, cfg, form=args.mix_only)
     return {"metric": "spin-steps/s", "value": work / el, "unit": "spin-steps/s", "form": args.mix_only,
@@ -747,7 +747,7 @@ def run_batched_mix(subs, mix, cfg, form="fp32"):
     cap = sum((j["n"] + 31) // 32 * 32 for j in mix)
     b = Batch(cap, len(mix))
     sids = {id(sb): (b.add_mesh(sb.handle) if sb.kind == "mesh" else b.add_cyl(sb.handle)) for sb in subs}
-    b.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8)
+    b.configure(chunk=cfg["chunk"], occupancy=cfg["occupancy"], graph_chunks=8, block=cfg.get("block"))
     t0 = time.perf_counter()
     ids = [b.submit(sids[id(j["sub"])], j["pos"], j["comp"], j["fiber"], **_submit_kw(j, form)) for j in mix]
     b.run()
@@ -881,7 +881,7 @@ def run_c4_full(args, W, m):
         K += 1                                   # every substrate of the stream in the sample
     sample = [job(k) for k in range(K)]
     best, _ = tune_mix(subs, sample)
-    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"], "block": best.get("block")}
     per = (run_plain_bar_mix(subs, sample) if form == "bar" else run_plain_mix(sample))[0]
     sub_rate = {}
     for sb in {id(sb): sb for sb, _, _ in shapes[:K]}.values():
@@ -1011,11 +1011,11 @@ def run_forms(args, W, m):
     grad_work = sum(j["n"] * j["steps"] * len(j["grads"]) for j in mix)
     if args.mix_config:
         occ, chunk = args.mix_config
-        best = {"occupancy": occ, "chunk": chunk, "fine_per_ref": None, "fixed": True}
+        best = {"occupancy": occ, "chunk": chunk, "fine_per_ref": None, "block": args.mix_block, "fixed": True}
     else:
         best, tune_ms = tune_mix(subs, mix)
         log("autotune: %s (%.1f ms for 60 steps of 8 jobs)" % (best, tune_ms))
-    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"]}
+    cfg = {"occupancy": best["occupancy"], "chunk": best["chunk"], "block": best.get("block")}
     per, psig = run_plain_mix(mix)
     plain_s = sum(per)
     per_b, bsig = run_plain_bar_mix(subs, mix)
@@ -1471,6 +1471,8 @@ def main():
                     help="skip the full-size precision comparison that a one-GPU run does by default")
     ap.add_argument("--c5-full", action="store_true",
                     help="also run the precision comparison at full size (every spin, --c5-steps steps, 3 waveforms)")
+    ap.add_argument("--mix-block", type=int, default=None, choices=[64, 128, 256],
+                    help="block size of the plain batch step kernels with --mix-config")
     ap.add_argument("--mix-only", choices=["fp32", "bar", "fp64"], default=None,
                     help="only run the 48-job mix once in one batch in this form (for profiling)")
     ap.add_argument("--c4-full", action="store_true",

@@ -163,6 +163,8 @@ def _declare_batch(L):
         "dsim_batch_add_cyl": (i32, [VP, VP, C.POINTER(u32)]),
         "dsim_batch_submit": (i32, [VP, C.POINTER(JobDesc), F32, U8, OU32, C.POINTER(u32)]),
         "dsim_batch_configure": (i32, [VP, u32, u32, u32]),
+        "dsim_batch_set_block": (i32, [VP, u32]),
+        "dsim_batch_block": (i32, [VP, C.POINTER(u32)]),
         "dsim_batch_advance": (i32, [VP, u32]),
         "dsim_batch_run": (i32, [VP]),
         "dsim_batch_job_status": (i32, [VP, u32, C.POINTER(u32), C.POINTER(i32)]),

@@ -84,17 +84,19 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 // 32-byte, 2: 64-byte records), each advancing only the mesh jobs whose
 // substrate uses it, and one for cylinder jobs (LAYOUT 3), so no kernel
 // carries the registers of a path it does not run.  Precision-form and
-// cell-local jobs run in k_batch_step64 and k_batch_step_local.
-template <int MINB, int LAYOUT>
-__global__ void __launch_bounds__(kFlatThreads, MINB)
+// cell-local jobs run in k_batch_step64 and k_batch_step_local.  THREADS:
+// block size (64, 128 or 256); MINB counts 128-thread blocks per SM, so every
+// block shape of one occupancy has the same register budget per thread.
+template <int MINB, int LAYOUT, int THREADS = kFlatThreads>
+__global__ void __launch_bounds__(THREADS, MINB * kFlatThreads / THREADS)
 k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, BatchSpins S,
              const uint32_t* __restrict__ stepNow, uint32_t chunk, uint32_t* status,
              unsigned long long* jobCounts) {
     constexpr int MESH = LAYOUT == 3 ? 1 : LAYOUT;  // the record path of the mesh instantiations
-    __shared__ FlatWarp wh[LAYOUT == 3 ? 1 : kFlatWarps];
+    __shared__ FlatWarp wh[LAYOUT == 3 ? 1 : THREADS / 32];
     // gradient moments and their compensation live in shared memory (touched
     // once per step), which keeps the collision loop's registers free
-    __shared__ float mom[6][kFlatThreads];
+    __shared__ float mom[6][THREADS];
     const uint32_t FULL = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t tx = threadIdx.x;
@@ -104,8 +106,8 @@ k_batch_step(const SubDev* __restrict__ subs, const JobDev* __restrict__ jobs, B
     const uint32_t jb = S.u[U_JOB][i & ~31u];
     // the warp's job and substrate records, copied to shared memory once and
     // read from there (kept out of the collision loop's registers)
-    __shared__ JobDev jobS[kFlatWarps];
-    __shared__ SubDev subS[kFlatWarps];
+    __shared__ JobDev jobS[THREADS / 32];
+    __shared__ SubDev subS[THREADS / 32];
     const uint32_t wi = threadIdx.x >> 5;
     {
         const uint32_t* src = reinterpret_cast<const uint32_t*>(jobs + jb);
@@ -730,6 +732,7 @@ struct dsim_batch {
     uint32_t *hist = nullptr, *hstart = nullptr, *scratch = nullptr;
     uint64_t keyCap = 0, K = 0;
     uint32_t chunk = 20, occupancy = 4, graphChunks = 8;
+    uint32_t blockThreads = kFlatThreads;  // block size of the plain step kernels (64, 128, 256)
     bool anyPrecise = false, anyLocal = false;  // precision-form / cell-local mesh jobs
     bool anyPreciseCyl = false;                 // precision-form cylinder jobs
     bool anyLocalCyl = false;                   // cell-local cylinder jobs
@@ -1003,17 +1006,25 @@ k_batch_step_cyl_local(const SubDev* __restrict__ subs, const JobDev* __restrict
     if (st) atomicOr(status, st);
 }
 
-template <int LAYOUT>
-void launch_step_layout(dsim_batch* b, uint32_t grid, const BatchSpins& D, cudaStream_t st) {
+template <int LAYOUT, int THREADS>
+void launch_step_shape(dsim_batch* b, const BatchSpins& D, cudaStream_t st) {
+    const uint32_t grid = (uint32_t)((b->N + THREADS - 1) / THREADS);
     if (b->occupancy >= 8)
-        k_batch_step<8, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                             b->d_status, b->d_counts);
+        k_batch_step<8, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
     else if (b->occupancy >= 6)
-        k_batch_step<6, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                             b->d_status, b->d_counts);
+        k_batch_step<6, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
     else
-        k_batch_step<4, LAYOUT><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
-                                                             b->d_status, b->d_counts);
+        k_batch_step<4, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
+}
+
+template <int LAYOUT>
+void launch_step_layout(dsim_batch* b, const BatchSpins& D, cudaStream_t st) {
+    if (b->blockThreads == 64) launch_step_shape<LAYOUT, 64>(b, D, st);
+    else if (b->blockThreads == 256) launch_step_shape<LAYOUT, 256>(b, D, st);
+    else launch_step_shape<LAYOUT, kFlatThreads>(b, D, st);
 }
 
 // one chunk: sort into the other buffer, step, advance the step counter
@@ -1046,9 +1057,9 @@ int enqueue_chunk(dsim_batch* b) {
         cudaStream_t st = fork ? b->side[q % dsim_batch::kSide] : b->st;
         if (fork) DSIM_CUDA_TRY(cudaStreamWaitEvent(st, b->forkEv, 0));
         switch (kinds[q]) {
-            case 1: launch_step_layout<1>(b, grid, D, st); break;
-            case 2: launch_step_layout<2>(b, grid, D, st); break;
-            case 3: launch_step_layout<3>(b, grid, D, st); break;
+            case 1: launch_step_layout<1>(b, D, st); break;
+            case 2: launch_step_layout<2>(b, D, st); break;
+            case 3: launch_step_layout<3>(b, D, st); break;
             case 4:
                 k_batch_step_local<1><<<grid, kFlatThreads, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow,
                                                                      b->chunk, b->d_status, b->d_counts);
@@ -1373,6 +1384,22 @@ int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint
     b->chunk = chunk;
     b->occupancy = occupancy;
     b->graphChunks = graphChunks;
+    invalidate_graph(b);
+    return kOk;
+}
+
+int dsim_batch_block(const dsim_batch* b, uint32_t* threads) {
+    if (!b || !threads) return kErrInvalid;
+    *threads = b->blockThreads;
+    return kOk;
+}
+
+int dsim_batch_set_block(dsim_batch* b, uint32_t threads) {
+    if (!b || (threads != 64 && threads != 128 && threads != 256)) {
+        set_last_error(kErrInvalid, "dsim_batch_set_block: 64, 128 or 256 threads");
+        return kErrInvalid;
+    }
+    b->blockThreads = threads;
     invalidate_graph(b);
     return kOk;
 }
@@ -1734,6 +1761,26 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
         }
     }
     if (!rc && e == cudaSuccess && haveMesh) rc = set_grid(bg);
+    // then the block size of the plain step kernels at that configuration
+    uint32_t bt = b->blockThreads;
+    const uint32_t shapes[] = {64, 128, 256};
+    float bestShape = 3.4e38f;
+    for (uint32_t th : shapes) {
+        if (rc || e != cudaSuccess) break;
+        if ((e = restore()) != cudaSuccess) break;
+        b->occupancy = bo; b->chunk = bc; b->graphChunks = 0; b->blockThreads = th;
+        invalidate_graph(b);
+        cudaEventRecord(e0, b->st);
+        if ((rc = dsim_batch_advance(b, T))) break;
+        cudaEventRecord(e1, b->st);
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms *= (float)trialSteps / (float)T;
+        if (ms < bestShape) { bestShape = ms; bt = th; }
+    }
+    if (bestShape < bestT) bestT = bestShape;
+    b->blockThreads = bt;
     if (!rc && e == cudaSuccess) e = restore();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

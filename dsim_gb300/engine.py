@@ -382,8 +382,10 @@ class Batch:
         check(native().dsim_batch_submit(self.h, C.byref(d), pos, comp, fib, C.byref(jid)))
         return jid.value
 
-    def configure(self, chunk=20, occupancy=4, graph_chunks=8):
+    def configure(self, chunk=20, occupancy=4, graph_chunks=8, block=None):
         check(native().dsim_batch_configure(self.h, int(chunk), int(occupancy), int(graph_chunks)))
+        if block is not None:
+            check(native().dsim_batch_set_block(self.h, int(block)))
 
     def advance(self, steps):
         check(native().dsim_batch_advance(self.h, int(steps)))
@@ -443,11 +445,14 @@ class Batch:
 
     def autotune(self, trial_steps=40):
         """Times every candidate configuration on a snapshot; returns
-        ({occupancy, chunk, fine_cells_per_ref_cell}, ms)."""
+        ({occupancy, chunk, fine_cells_per_ref_cell, block}, ms)."""
         best = np.zeros(3, np.uint32)
         ms = C.c_float()
         check(native().dsim_batch_autotune(self.h, int(trial_steps), best, C.byref(ms)))
-        return {"occupancy": int(best[0]), "chunk": int(best[1]), "fine_per_ref": best[2] / 2.0}, ms.value
+        th = C.c_uint32()
+        check(native().dsim_batch_block(self.h, C.byref(th)))
+        return {"occupancy": int(best[0]), "chunk": int(best[1]), "fine_per_ref": best[2] / 2.0,
+                "block": int(th.value)}, ms.value
 
     def info(self):
         a = np.zeros(6, np.uint64)

@@ -102,6 +102,11 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* job, const float* pos3
  * resident blocks per SM for the step kernel; graphChunks: chunks captured in
  * one CUDA graph launch (0 = plain launches, default 8) */
 int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint32_t graphChunks);
+/* block size of the plain step kernels: 64, 128 (default) or 256 threads, at
+ * the register budget of the configured occupancy (the other forms' kernels
+ * run 128-thread blocks); dsim_batch_autotune sets it too */
+int dsim_batch_set_block(dsim_batch* b, uint32_t threads);
+int dsim_batch_block(const dsim_batch* b, uint32_t* threads);
 /* advance every unfinished job by `steps` steps (rounded up to whole chunks) */
 int dsim_batch_advance(dsim_batch* b, uint32_t steps);
 /* advance until every job has finished */
@@ -139,7 +144,9 @@ int dsim_batch_compact(dsim_batch* b);
  * spin state for every candidate -- step-kernel occupancy {4, 6, 8} x chunk
  * {20, 40, 100, 200, 500, 1000} x fine-grid cells per reference-cell edge
  * {1, 1.5, 2, 2.5}; every candidate runs the same max(trialSteps, 1000) steps,
- * so longer chunks are not favoured by jobs finishing inside the trial
+ * so longer chunks are not favoured by jobs finishing inside the trial; then,
+ * at the best of those, the plain step kernels' block size {64, 128, 256}
+ * (left set; dsim_batch_block reads it)
  * (every mesh substrate's fine grid is rebuilt; meshes must not be in use
  * elsewhere meanwhile) -- restores the snapshot and keeps the fastest.
  * best = {occupancy, chunk, 2 x fine cells per reference cell edge (0: no
