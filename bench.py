@@ -470,13 +470,13 @@ def run_ours(args, rank, world):
 
     hbm, kind = peaks()
     # DRAM bytes of the step kernel per spin-step, from one ncu capture of
-    # k_mesh_step_flat<0,6,1,1,0> (default kernel 8, 112^3 fine grid, 32-byte
+    # k_mesh_step_flat<0,6,1,1,0> (kernel 8 at 6 blocks per SM, 112^3 fine grid, 32-byte
     # records) on 262,144 spins x 60 steps of this mesh: 2.7997 GB read + 0.1021 GB
     # written per launch = 184.5 B per spin-step; scaled to this call's spin-steps
     default_cfg = args.kernel <= 0 and args.accel < 0 and args.records <= 0 and args.sort_every < 0
     traffic = DRAM_BYTES_PER_SPIN_STEP * it * W.N if default_cfg else None
     traffic_note = ("bytes per launch (one %d-step call) = 184.5 B per spin-step from an ncu capture of "
-                    "the default step kernel, scaled by spin-steps" % it) if default_cfg else "no capture for this configuration"
+                    "the default step kernel (at 6 blocks per SM), scaled by spin-steps" % it) if default_cfg else "no capture for this configuration"
     S_bytes = 12 + 4 + 4
     B_step = 2 * S_bytes + 40 * Tbar
     mean_launch_ms = (sum(times) / len(times))

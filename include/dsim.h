@@ -72,8 +72,8 @@ int dsim_mesh_set_accel(dsim_mesh* m, uint32_t cellsPerAxis);
 /* step kernel on the fine grid (all give the same results; default 8; other
  * values are refused): 5, 6, 7 the warp's candidate records flattened into one
  * list, lanes stepping independently (8, 6, 4 resident blocks of 128 threads
- * per SM); 8 as 6, with the records that pass the plane test queued and
- * finished 32 at a time; 9 as 6, with each lane's part of every 64-record
+ * per SM); 8 as 6 at 5 blocks per SM (96 registers, no spills), with the
+ * records that pass the plane test queued and finished 32 at a time; 9 as 6, with each lane's part of every 64-record
  * window copied into shared memory by TMA bulk copies (cp.async.bulk,
  * mbarrier completion) while the previous window is tested (8 and 9: 32-byte
  * records) */
