@@ -1015,6 +1015,9 @@ void launch_step_shape(dsim_batch* b, const BatchSpins& D, cudaStream_t st) {
     else if (b->occupancy >= 6)
         k_batch_step<6, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
                                                                   b->d_status, b->d_counts);
+    else if (b->occupancy == 5)
+        k_batch_step<5, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
+                                                                  b->d_status, b->d_counts);
     else
         k_batch_step<4, LAYOUT, THREADS><<<grid, THREADS, 0, st>>>(b->d_subs, b->d_jobs, D, b->d_stepNow, b->chunk,
                                                                   b->d_status, b->d_counts);
@@ -1377,8 +1380,8 @@ int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* d, const float* pos3, 
 }
 
 int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint32_t graphChunks) {
-    if (!b || chunk == 0 || (occupancy != 4 && occupancy != 6 && occupancy != 8)) {
-        set_last_error(kErrInvalid, "dsim_batch_configure: chunk > 0, occupancy 4, 6 or 8");
+    if (!b || chunk == 0 || (occupancy != 4 && occupancy != 5 && occupancy != 6 && occupancy != 8)) {
+        set_last_error(kErrInvalid, "dsim_batch_configure: chunk > 0, occupancy 4, 5, 6 or 8");
         return kErrInvalid;
     }
     b->chunk = chunk;
@@ -1715,7 +1718,7 @@ int dsim_batch_autotune(dsim_batch* b, uint32_t trialSteps, uint32_t best[3], fl
     };
     // fine-grid resolutions: cells per reference-cell edge x 2
     const uint32_t gridHalves[] = {2, 3, 4, 5};  // 1, 1.5, 2, 2.5 fine cells per reference cell
-    const uint32_t occs[] = {4, 6, 8};
+    const uint32_t occs[] = {4, 5, 6, 8};
     const uint32_t chunks[] = {20, 40, 100, 200, 500, 1000};
     // the same steps for every candidate (a multiple of every chunk)
     const uint32_t T = std::max<uint32_t>((trialSteps + 999u) / 1000u * 1000u, 1000u);

@@ -98,7 +98,7 @@ int dsim_batch_add_cyl(dsim_batch* b, const dsim_cyl* c, uint32_t* substrate);
  * chunk.  DSIM_ENOMEM when spin or job capacity is exhausted. */
 int dsim_batch_submit(dsim_batch* b, const dsim_job_desc* job, const float* pos3,
                       const uint8_t* compartment, const uint32_t* fiber, uint32_t* jobId);
-/* chunk: steps between spin sorts (default 20); occupancy: 4 (default), 6 or 8
+/* chunk: steps between spin sorts (default 20); occupancy: 4 (default), 5, 6 or 8
  * resident blocks per SM for the step kernel; graphChunks: chunks captured in
  * one CUDA graph launch (0 = plain launches, default 8) */
 int dsim_batch_configure(dsim_batch* b, uint32_t chunk, uint32_t occupancy, uint32_t graphChunks);
@@ -141,7 +141,7 @@ uint32_t dsim_batch_status(dsim_batch* b);
 int dsim_batch_retire(dsim_batch* b, uint32_t jobId);
 int dsim_batch_compact(dsim_batch* b);
 /* Autotuner: runs the current jobs from a snapshot of the
- * spin state for every candidate -- step-kernel occupancy {4, 6, 8} x chunk
+ * spin state for every candidate -- step-kernel occupancy {4, 5, 6, 8} x chunk
  * {20, 40, 100, 200, 500, 1000} x fine-grid cells per reference-cell edge
  * {1, 1.5, 2, 2.5}; every candidate runs the same max(trialSteps, 1000) steps,
  * so longer chunks are not favoured by jobs finishing inside the trial; then,
